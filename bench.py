@@ -1,0 +1,490 @@
+"""Benchmark of the GB300 multifit engine (one JSON line on rank 0).
+
+Metric: channels fitted per second on one GB300. A step is one fit of the
+whole workload batch (every channel of it) already resident in HBM; `value`
+is channels / device time (CUDA events on the launching stream, L2 flushed
+between steps, max over ranks). `e2e` is the same fit through the host-pointer
+C-ABI entry (mf_fit_host): pinned host inputs copied in, results copied back,
+synchronised, every step inside the timed region.
+
+`--impl reference` times the reference's CPU path instead: the reference
+needs Eigen, which is absent, so its CPU implementation is the FP64 oracle
+restatement (oracle/), run on all host cores over a bounded sample.
+
+Multi-GPU: channels are independent, so N ranks each fit their own shard of
+the channel stream with no collective on the data path ("replicas"; weak
+scaling); the only collectives are the timing barrier and max-reduce.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib.util
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG_DIR = os.path.join(ROOT, "test-regression_gb300")
+METRIC = "channels fitted/s on 1 GB300: MLP-warm FP32 vs plain FNNLS FP64, ≤1e-4 amp err"
+UNIT = "channels/s"
+
+
+def load_pkg():
+    if "multifit_gb300" in sys.modules:
+        return sys.modules["multifit_gb300"]
+    spec = importlib.util.spec_from_file_location("multifit_gb300", os.path.join(PKG_DIR, "__init__.py"))
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["multifit_gb300"] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def build_pkg():
+    spec = importlib.util.spec_from_file_location("multifit_gb300_build", os.path.join(PKG_DIR, "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    mod.build()
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if args.impl != "reference" else "gloo"
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def max_over_ranks(x: float, world: int, device=None) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+WORKLOAD_DESC = {
+    "ecal-1m-pu2": "1,000,000 ECAL 10x10 channels, CRRC4 tau=43ns, sigma=0.044, rho=0.7, in-time U[1,100], "
+                   "pileup Poisson(2)xExp(1 GeV) per out-of-time BX, seed 2",
+    "ecal-10k-pu0.5": "10,000 ECAL 10x10 channels, pileup 0.5, seed 1",
+    "ecal-10m-logamp-pu4": "10,000,000 ECAL channels, in-time log-uniform [0.1,1000], pileup 4, seed 3",
+    "mixed-10m-ecal-hcal": "10,000,000 channels, 40% HCAL 8x8, pileup U[0,8] per channel, seed 4",
+    "warm-eval-10m": "10,000,000 ECAL channels, log-uniform [0.1,1000], pileup 4, seed 6",
+}
+
+
+def fp64_peak_tflops(torch) -> float:
+    """cuBLAS DGEMM throughput measured in this run: the FP64-pipe roofline."""
+    n = 4096
+    a = torch.randn((n, n), dtype=torch.float64, device="cuda")
+    b = torch.randn((n, n), dtype=torch.float64, device="cuda")
+    best = 0.0
+    for _ in range(3):
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = max(best, 2.0 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    return best
+
+
+def run_ours(args, world, rank, local):
+    import numpy as np
+    import torch
+
+    torch.cuda.set_device(local)
+    build_pkg()
+    mf = load_pkg()
+    eng = mf.Engine(local)
+    wl = args.workload
+    p = mf.WORKLOADS[wl]()
+    n = int(args.channels or p.n)
+    p.n = n
+    mixed = p.hcal_fraction > 0
+    ecal, _ = mf.synth_conditions(mf.SYNTH_ECAL)
+    eng.set_conditions(0, ecal)
+    if mixed:
+        hcal, _ = mf.synth_conditions(mf.SYNTH_HCAL)
+        eng.set_conditions(1, hcal)
+    opt = mf.default_options(max_iter_nnls=args.max_iter, nnls_start=args.start)
+
+    dev = "cuda"
+    samples = torch.zeros((n, 10), dtype=torch.float64, device=dev)
+    pederr = torch.zeros(n, dtype=torch.float64, device=dev)
+    ctype = torch.zeros(n, dtype=torch.uint8, device=dev) if mixed else None
+    amp = torch.zeros((n, 10), dtype=torch.float64, device=dev)
+    chi2 = torch.zeros(n, dtype=torch.float64, device=dev)
+    intime = torch.zeros(n, dtype=torch.float64, device=dev)
+    mask = torch.zeros(n, dtype=torch.int16, device=dev)
+    status = torch.zeros(n, dtype=torch.uint8, device=dev)
+    first = rank * n  # each rank fits its own shard of the channel stream
+    mf.synth_generate_device(p, first, n, samples.data_ptr(), pederr.data_ptr(),
+                             ctype.data_ptr() if mixed else None)
+    batch = mf.Engine._batch(n, 10, 10, samples.data_ptr(), pederr.data_ptr(),
+                             ctype.data_ptr() if mixed else None, amp.data_ptr(), chi2.data_ptr(),
+                             intime.data_ptr(), None, mask.data_ptr(), status.data_ptr(), None)
+    stream = torch.cuda.Stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 256 MB > 129 MB L2
+    torch.cuda.synchronize()
+
+    # algorithmic work of one launch (instrumented kernel, untimed)
+    flops = torch.zeros(n, dtype=torch.float64, device=dev)
+    eng.fit_count_flops(batch, flops.data_ptr(), opt, stream.cuda_stream)
+    torch.cuda.synchronize()
+    flops_per_launch = float(flops.sum().item())
+    del flops
+
+    def step():
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            eng.fit_device(batch, opt, stream.cuda_stream)
+            e1.record(stream)
+        return e0, e1
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    evs = [step() for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    times = [e0.elapsed_time(e1) for e0, e1 in evs]
+    step_ms = sum(times) / len(times)
+    step_ms_max = max_over_ranks(step_ms, world, device=dev)
+    value = n * world / (step_ms_max * 1e-3)
+
+    # parity spot check of this run's output against the oracle (bitwise)
+    parity = None
+    if rank == 0 and not args.no_parity:
+        sys.path.insert(0, ROOT)
+        import oracle
+
+        m = min(n, 2000)
+        inp_s = samples[:m].cpu().numpy()
+        inp_p = pederr[:m].cpu().numpy()
+        ct = ctype[:m].cpu().numpy() if mixed else np.zeros(m, np.uint8)
+        a_gpu = amp[:m].cpu().numpy()
+        ok = True
+        for t, cond in eng.conditions.items():
+            sel = np.nonzero(ct == t)[0]
+            if sel.size == 0:
+                continue
+            P, R, bxs, _ = mf.conditions_arrays(cond)
+            ref = oracle.fit_batch(inp_s[sel], inp_p[sel], P, R, bxs, max_iter_nnls=args.max_iter,
+                                   start=args.start)
+            ok = ok and bool(np.array_equal(a_gpu[sel, : P.shape[1]], ref["amplitudes"]))
+        parity = {"sample_channels": m, "bitwise_equal_to_oracle": ok}
+
+    # end to end through the host-pointer entry point (pinned buffers)
+    h_s = torch.empty((n, 10), dtype=torch.float64).pin_memory()
+    h_p = torch.empty(n, dtype=torch.float64).pin_memory()
+    h_s.copy_(samples)
+    h_p.copy_(pederr)
+    h_ct = None
+    if mixed:
+        h_ct = torch.empty(n, dtype=torch.uint8).pin_memory()
+        h_ct.copy_(ctype)
+    h_amp = torch.empty((n, 10), dtype=torch.float64).pin_memory()
+    h_chi2 = torch.empty(n, dtype=torch.float64).pin_memory()
+    h_int = torch.empty(n, dtype=torch.float64).pin_memory()
+    h_mask = torch.empty(n, dtype=torch.int16).pin_memory()
+    h_st = torch.empty(n, dtype=torch.uint8).pin_memory()
+    hb = mf.Engine._batch(n, 10, 10, h_s.data_ptr(), h_p.data_ptr(), h_ct.data_ptr() if mixed else None,
+                          h_amp.data_ptr(), h_chi2.data_ptr(), h_int.data_ptr(), None, h_mask.data_ptr(),
+                          h_st.data_ptr(), None)
+    import ctypes as C
+
+    def e2e_step():
+        rc = eng.lib.mf_fit_host(eng.h, C.byref(hb), C.byref(opt))
+        if rc:
+            raise RuntimeError(f"mf_fit_host rc={rc}")
+
+    for _ in range(args.warmup):
+        e2e_step()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    e2e_s = max_over_ranks(e2e_s, world, device=dev)
+    h2d = n * (10 * 8 + 8 + (1 if mixed else 0))
+    d2h = n * (10 * 8 + 8 + 8 + 2 + 1)
+
+    peaks, peak_src = measured_peaks()
+    fp64_peak = fp64_peak_tflops(torch)
+    achieved = flops_per_launch / (step_ms * 1e-3) / 1e12
+    bytes_per_launch = n * (10 * 8 + 8) + n * (10 * 8 + 8 + 8 + 2 + 1)
+    hbm_gbs = bytes_per_launch / (step_ms * 1e-3) / 1e9
+
+    out = None
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline:
+            cpu = cpu_baseline(mf, args, p, budget_s=args.cpu_seconds)
+        out = {
+            "metric": METRIC,
+            "value": value,
+            "unit": UNIT,
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": step_ms_max,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f64",
+            "data": "synthetic (seeded Philox generator; BASELINE shapes and distributions)",
+            "config": {
+                "workload": wl,
+                "description": WORKLOAD_DESC.get(wl, wl),
+                "channels_per_gpu": n,
+                "form": "plain-fp64",
+                "max_iter_nnls": args.max_iter,
+                "nnls_start": ["reference", "support"][args.start],
+                "l2": "flushed between steps (256 MB write)",
+                "parallelism": f"replicas x{world}",
+            },
+            "e2e": {"value": n * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "entry": "mf_fit_host (pinned host buffers)"},
+            "roofline": {
+                "bound": "fp64",
+                "achieved": achieved,
+                "peak": fp64_peak,
+                "unit": "TFLOP/s",
+                "frac": achieved / fp64_peak,
+                "traffic": None,
+                "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (MEASURED_PEAKS.json has no FP64 figure)",
+                "algorithmic_flops_per_launch": flops_per_launch,
+                "flops_per_channel": flops_per_launch / n,
+                "kernel": "fit_fp64_kernel",
+            },
+            "roofline_hbm": {"bound": "hbm", "achieved": hbm_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                             "frac": hbm_gbs / peaks["hbm_gbs"], "peak_source": peak_src,
+                             "algorithmic_bytes_per_launch": bytes_per_launch},
+            "cpu_baseline": cpu,
+            "gpu_launches": args.steps,
+            "clocks": clk,
+            "parity": parity,
+        }
+        print(json.dumps(out), flush=True)
+    eng.close()
+    return out
+
+
+def cpu_baseline(mf, args, p, budget_s: float = 3.0):
+    """The oracle (a port of the reference's CPU path) on the host cores over a
+    bounded sample of the same workload."""
+    sys.path.insert(0, ROOT)
+    import numpy as np
+
+    import oracle
+
+    nt = oracle.hardware_threads()
+    ecal, _ = mf.synth_conditions(mf.SYNTH_ECAL)
+    P, R, bxs, _ = mf.conditions_arrays(ecal)
+    m = 20_000
+    d = mf.synth_generate_host(p, 0, m, with_truth=False)
+    t0 = time.perf_counter()
+    oracle.fit_batch(d["samples"], d["pederr"], P, R, bxs, max_iter_nnls=args.max_iter, start=args.start,
+                     nthreads=nt)
+    dt = time.perf_counter() - t0
+    rate = m / dt
+    m2 = int(min(p.n, max(m, rate * budget_s)))
+    if m2 > m:
+        d = mf.synth_generate_host(p, 0, m2, with_truth=False)
+        t0 = time.perf_counter()
+        oracle.fit_batch(d["samples"], d["pederr"], P, R, bxs, max_iter_nnls=args.max_iter, start=args.start,
+                         nthreads=nt)
+        dt = time.perf_counter() - t0
+        m = m2
+        rate = m / dt
+    return {"value": rate, "unit": UNIT, "cores": nt, "kind": "port",
+            "sample": f"first {m} channels of the workload, ECAL set, all {nt} host threads, {dt:.2f} s"}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return None
+    build_pkg()
+    mf = load_pkg()
+    sys.path.insert(0, ROOT)
+    import oracle
+
+    nt = oracle.hardware_threads()
+    p = mf.WORKLOADS[args.workload]()
+    mixed = p.hcal_fraction > 0
+    conds = {0: mf.synth_conditions(mf.SYNTH_ECAL)[0]}
+    if mixed:
+        conds[1] = mf.synth_conditions(mf.SYNTH_HCAL)[0]
+    # size one step to about args.cpu_seconds of work on all cores
+    probe = 20_000
+    d = mf.synth_generate_host(p, 0, probe, with_truth=False)
+
+    def fit(d):
+        for t, c in conds.items():
+            sel = d["ctype"] == t
+            if not sel.any():
+                continue
+            P, R, bxs, _ = mf.conditions_arrays(c)
+            oracle.fit_batch(d["samples"][sel], d["pederr"][sel], P, R, bxs, max_iter_nnls=args.max_iter,
+                             start=args.start, nthreads=nt)
+
+    t0 = time.perf_counter()
+    fit(d)
+    rate = probe / (time.perf_counter() - t0)
+    m = int(min(p.n, max(probe, rate * args.cpu_seconds)))
+    d = mf.synth_generate_host(p, 0, m, with_truth=False)
+    for _ in range(args.warmup):
+        fit(d)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        fit(d)
+    dt = (time.perf_counter() - t0) / args.steps
+    value = m / dt
+    sample = f"first {m} channels of {args.workload} per step, all {nt} host threads"
+    out = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": dt * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded Philox generator; BASELINE shapes and distributions)",
+        "config": {"workload": args.workload, "description": WORKLOAD_DESC.get(args.workload, args.workload),
+                   "form": "reference multifit_cpu path (oracle port: Eigen absent, reference not buildable)",
+                   "max_iter_nnls": args.max_iter, "nnls_start": ["reference", "support"][args.start]},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nt, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+    return out
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="ecal-1m-pu2")
+    ap.add_argument("--channels", type=int, default=0, help="override the workload's channel count")
+    ap.add_argument("--max-iter", type=int, default=10)
+    ap.add_argument("--start", type=int, default=0, choices=[0, 1])
+    ap.add_argument("--cpu-seconds", type=float, default=3.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-parity", action="store_true")
+    args = ap.parse_args(argv)
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

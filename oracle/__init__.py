@@ -1,0 +1,163 @@
+"""CPU oracle of the multifit hot path -- TEST INFRASTRUCTURE ONLY.
+
+ctypes bindings of ``_build/liboracle.so`` (multifit_oracle.cpp: the C++17
+FP64 restatement of the reference's multifit_cpu fit) and of
+``_ref/libref_linalgebra.so`` (the reference's own linear-algebra headers,
+compiled in place where the reference tree exists). Only the tests, the smoke
+check and the benchmark's CPU-baseline leg use this package, always as the
+checker or the timed CPU baseline -- never on the engine's path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build_oracle
+
+_lib = None
+_ref = None
+
+KMAX = 10
+
+dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build_oracle.build_oracle()
+        L = C.CDLL(path)
+        L.oracle_cholesky.argtypes = [dp, dp, C.c_int, C.c_int]
+        L.oracle_forward.argtypes = [dp, C.c_int, dp, dp, C.c_int]
+        L.oracle_backward.argtypes = [dp, C.c_int, dp, dp, C.c_int]
+        L.oracle_rc_addition.argtypes = [dp, dp, C.c_int, dp, dp, C.c_int]
+        L.oracle_inbetween_removal.argtypes = [dp, dp, C.c_int, dp, dp, C.c_int, C.c_int]
+        L.oracle_swap_sym.argtypes = [dp, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.oracle_inplace_fnnls.argtypes = [dp, dp, dp, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int,
+                                           np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")]
+        L.oracle_fit_batch.restype = C.c_int
+        L.oracle_fit_batch.argtypes = [C.c_int64, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
+                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
+                                       C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
+                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_void_p]
+        L.oracle_kkt_violation.restype = C.c_double
+        L.oracle_kkt_violation.argtypes = [dp, dp, dp, C.c_int, C.c_int]
+        L.oracle_nnls_bruteforce.restype = C.c_double
+        L.oracle_nnls_bruteforce.argtypes = [dp, dp, C.c_int, C.c_int, dp]
+        L.oracle_nnls_lawson_hanson.restype = C.c_int
+        L.oracle_nnls_lawson_hanson.argtypes = [dp, dp, C.c_int, C.c_int, dp, C.c_int]
+        L.oracle_hardware_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def ref():
+    """The reference's own linalgebra primitives, or None where the reference tree is absent."""
+    global _ref
+    if _ref is None:
+        path = build_oracle.build_ref()
+        if path is None:
+            return None
+        R = C.CDLL(path)
+        R.ref_cholesky_decomp.argtypes = [dp, dp, C.c_int, C.c_int]
+        R.ref_forward.argtypes = [dp, dp, dp, C.c_int, C.c_int]
+        R.ref_backward.argtypes = [dp, dp, dp, C.c_int, C.c_int]
+        R.ref_rc_addition.argtypes = [dp, dp, dp, dp, C.c_int, C.c_int]
+        R.ref_inbetween_removal.argtypes = [dp, dp, dp, dp, C.c_int, C.c_int, C.c_int]
+        R.ref_eigen_rc_addition.argtypes = [dp, dp, dp, dp, C.c_int, C.c_int]
+        R.ref_eigen_inbetween_removal.argtypes = [dp, dp, dp, dp, C.c_int, C.c_int, C.c_int]
+        R.ref_swap_row_column.argtypes = [dp, C.c_int, C.c_int, C.c_int, C.c_int]
+        _ref = R
+    return _ref
+
+
+def hardware_threads() -> int:
+    return int(lib().oracle_hardware_threads())
+
+
+def inplace_fnnls(A: np.ndarray, b: np.ndarray, x0: np.ndarray | None = None, eps: float = 1e-11,
+                  max_iter: int = 1000, variant: int = 0, start: int = 0):
+    """FNNLS on a whitened problem. A: (N, K). Returns (x, stats dict)."""
+    A = np.asarray(A, dtype=np.float64)
+    N, K = A.shape
+    Acm = np.ascontiguousarray(A.T)  # column-major flat
+    x = np.zeros(K) if x0 is None else np.array(x0, dtype=np.float64)
+    st = np.zeros(5, dtype=np.int32)
+    lib().oracle_inplace_fnnls(Acm.ravel(), np.ascontiguousarray(b, dtype=np.float64), x, N, K, eps, max_iter,
+                               variant, start, st)
+    return x, {"outer": int(st[0]), "inner": int(st[1]), "converged": int(st[2]), "passive": int(st[3]),
+               "mask": int(st[4])}
+
+
+def fit_batch(samples: np.ndarray, pederr: np.ndarray, P: np.ndarray, R: np.ndarray, bxs=None,
+              fullpulsecov=None, eps: float = 1e-11, max_iter_nnls: int = 10, max_iter_outer: int = 50,
+              dchi2_tol: float = 1e-3, variant: int = 1, start: int = 0, compute_errors: bool = False,
+              nthreads: int = 0, count_flops: bool = False):
+    """Fits channels sharing one condition set. samples: (n, stride). P: (N, K), R: (N, N)."""
+    samples = np.ascontiguousarray(samples, dtype=np.float64)
+    pederr = np.ascontiguousarray(pederr, dtype=np.float64)
+    n, stride = samples.shape
+    P = np.asarray(P, dtype=np.float64)
+    N, K = P.shape
+    Pcm = np.ascontiguousarray(P.T)
+    Rcm = np.ascontiguousarray(np.asarray(R, dtype=np.float64).T)
+    if bxs is None:
+        bxs = np.arange(K, dtype=np.int8) - 5
+    bx = np.ascontiguousarray(bxs, dtype=np.int8)
+    F = None
+    if fullpulsecov is not None:
+        F = np.ascontiguousarray(np.asarray(fullpulsecov, dtype=np.float64).T)
+    out = {
+        "amplitudes": np.zeros((n, K)),
+        "chi2": np.zeros(n),
+        "active_mask": np.zeros(n, dtype=np.uint16),
+        "status": np.zeros(n, dtype=np.uint8),
+        "iters": np.zeros((n, 3), dtype=np.int32),
+        "errors": np.zeros(n),
+        "flops": np.zeros(n) if count_flops else None,
+    }
+    rc = lib().oracle_fit_batch(
+        n, N, K, samples.ctypes.data, stride, pederr.ctypes.data, Pcm.ctypes.data, Rcm.ctypes.data,
+        F.ctypes.data if F is not None else None, bx.ctypes.data, eps, max_iter_nnls, max_iter_outer,
+        dchi2_tol, variant, start, int(compute_errors), nthreads, out["amplitudes"].ctypes.data, out["chi2"].ctypes.data,
+        out["active_mask"].ctypes.data, out["status"].ctypes.data, out["iters"].ctypes.data,
+        out["errors"].ctypes.data, out["flops"].ctypes.data if count_flops else None)
+    if rc != 0:
+        raise ValueError(f"oracle_fit_batch rc={rc}")
+    return out
+
+
+def kkt_violation(A, b, x) -> float:
+    A = np.asarray(A, dtype=np.float64)
+    N, K = A.shape
+    return float(lib().oracle_kkt_violation(np.ascontiguousarray(A.T).ravel(), np.ascontiguousarray(b, float),
+                                            np.ascontiguousarray(x, float), N, K))
+
+
+def nnls_bruteforce(A, b):
+    A = np.asarray(A, dtype=np.float64)
+    N, K = A.shape
+    x = np.zeros(K)
+    r = lib().oracle_nnls_bruteforce(np.ascontiguousarray(A.T).ravel(), np.ascontiguousarray(b, float), N, K, x)
+    return x, float(r)
+
+
+def nnls_lawson_hanson(A, b, max_iter: int = 100):
+    A = np.asarray(A, dtype=np.float64)
+    N, K = A.shape
+    x = np.zeros(K)
+    lib().oracle_nnls_lawson_hanson(np.ascontiguousarray(A.T).ravel(), np.ascontiguousarray(b, float), N, K, x,
+                                    max_iter)
+    return x
+
+
+def whiten(P, R, pederr, samples):
+    """A = L^-1 P, b = L^-1 s with L = chol(pederr^2 R) (numpy, for cross-checks)."""
+    Lc = np.linalg.cholesky(pederr * pederr * np.asarray(R))
+    import scipy.linalg as sl
+    A = sl.solve_triangular(Lc, P, lower=True)
+    b = sl.solve_triangular(Lc, samples, lower=True)
+    return A, b

@@ -1,0 +1,86 @@
+"""Build recipe for the CPU oracle (test infrastructure).
+
+* ``oracle/_build/liboracle.so``: the C++17 FP64 restatement of the reference
+  path (multifit_oracle.cpp), built with ``-ffp-contract=off`` so that only its
+  explicit ``std::fma`` calls fuse. Built on every machine.
+* ``oracle/_ref/libref_linalgebra.so``: the reference project's own
+  header-only linear-algebra primitives (``linalgebra/interface/*.hpp``),
+  compiled in place from the reference tree with a small driver
+  (ref_linalgebra_driver.cpp). Built only where the reference tree exists.
+  gcc contracts each ``acc += a*b`` of those headers into one fused
+  multiply-add (``-ffp-contract=fast``, FMA hardware, and the
+  ``avoid-fma-max-bits`` heuristic off), which is the oracle's canonical
+  order; the tests check that claim bit for bit.
+
+The rest of the reference path (inplace_fnnls, PulseChiSqSNNLS) includes
+Eigen, which the reference does not vendor and which is absent here, so it is
+not built.
+"""
+from __future__ import annotations
+
+import os
+import platform
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+REF_OUT = os.path.join(HERE, "_ref")
+REFERENCE_ROOT = os.environ.get("MULTIFIT_REFERENCE_ROOT", "/root/reference")
+
+ORACLE_LIB = os.path.join(BUILD, "liboracle.so")
+REF_LIB = os.path.join(REF_OUT, "libref_linalgebra.so")
+
+
+def _fma_flag() -> list[str]:
+    # x86 needs -mfma for the instruction; gcc's avoid-fma-max-bits heuristic
+    # otherwise leaves loop-carried accumulations unfused, so it is switched off.
+    if platform.machine() in ("x86_64", "AMD64"):
+        return ["-mfma", "--param=avoid-fma-max-bits=0"]
+    return []
+
+
+def _stale(target: str, sources: list[str]) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(s) > t for s in sources)
+
+
+def build_oracle(force: bool = False) -> str:
+    src = os.path.join(HERE, "multifit_oracle.cpp")
+    if force or _stale(ORACLE_LIB, [src, __file__]):
+        os.makedirs(BUILD, exist_ok=True)
+        tmp = ORACLE_LIB + ".tmp"
+        cmd = ["g++", "-std=c++17", "-O3", "-ffp-contract=off", "-fPIC", "-shared", "-pthread",
+               src, "-o", tmp]
+        subprocess.check_call(cmd)
+        os.replace(tmp, ORACLE_LIB)
+    return ORACLE_LIB
+
+
+def build_ref(force: bool = False) -> str | None:
+    inc = os.path.join(REFERENCE_ROOT, "linalgebra", "interface")
+    if not os.path.isdir(inc):
+        return None
+    src = os.path.join(HERE, "ref_linalgebra_driver.cpp")
+    if force or _stale(REF_LIB, [src, __file__]):
+        os.makedirs(REF_OUT, exist_ok=True)
+        tmp = REF_LIB + ".tmp"
+        cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=fast", *_fma_flag(), "-fPIC", "-shared",
+               "-I", inc, src, "-o", tmp]
+        subprocess.check_call(cmd)
+        os.replace(tmp, REF_LIB)
+    return REF_LIB
+
+
+def main() -> int:
+    force = "--force" in sys.argv
+    print(build_oracle(force))
+    print(build_ref(force) or "reference tree absent: oracle/_ref not built")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,356 @@
+// C ABI of the engine (include/multifit_gb300.h).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+
+#include "mf_internal.h"
+
+namespace mfgb {
+
+static thread_local char g_last_error[256] = "";
+
+void set_last_error(const char* what, cudaError_t e) {
+  std::snprintf(g_last_error, sizeof(g_last_error), "%s: %s (%d)", what, cudaGetErrorString(e), int(e));
+}
+
+int make_dev_conditions(const mf_conditions& c, DevConditions* d) {
+  const int N = c.nsamples, K = c.npulses;
+  if (N < 1 || N > KMAX || K < 1 || K > KMAX) return MF_EINVAL;
+  std::memset(d, 0, sizeof(*d));
+  d->N = N;
+  d->K = K;
+  d->intime_col = -1;
+  for (int k = 0; k < K; ++k) {
+    d->bxs[k] = c.bxs[k];
+    if (d->intime_col < 0 && c.bxs[k] == 0) d->intime_col = k;
+  }
+  for (int k = 0; k < K; ++k) {
+    int fz = N;
+    for (int i = 0; i < N; ++i) {
+      const double v = c.pulse_matrix[k * N + i];
+      d->P[k * N + i] = v;
+      if (fz == N && v != 0.) fz = i;
+    }
+    d->fz[k] = int8_t(fz);
+  }
+  for (int j = 0; j < N; ++j)
+    for (int i = 0; i < N; ++i) d->R[j * N + i] = c.noise_cor[j * N + i];
+  d->has_fpc = c.has_fullpulsecov ? 1 : 0;
+  if (d->has_fpc) {
+    const int NF = N + 9;
+    for (int k = 0; k < K; ++k)  // the pulse-covariance block rule needs bx in [-N+1, 6]
+      if (c.bxs[k] < -(N - 1) || c.bxs[k] > 6) return MF_EINVAL;
+    std::memcpy(d->fpc, c.fullpulsecov, sizeof(double) * NF * NF);
+  }
+  return MF_OK;
+}
+
+}  // namespace mfgb
+
+using namespace mfgb;
+
+struct mf_context {
+  int device = 0;
+  DevConditions cond[MF_MAX_CTYPES];
+  int cond_set[MF_MAX_CTYPES] = {0, 0};
+  // staging area for mf_fit_host
+  int64_t cap = 0;
+  int cap_ss = 0, cap_as = 0;
+  double* d_samples = nullptr;
+  double* d_pederr = nullptr;
+  uint8_t* d_ctype = nullptr;
+  double* d_amp = nullptr;
+  double* d_chi2 = nullptr;
+  double* d_intime = nullptr;
+  double* d_errors = nullptr;
+  uint16_t* d_mask = nullptr;
+  uint8_t* d_status = nullptr;
+  int32_t* d_iters = nullptr;
+  cudaStream_t stream = nullptr;
+  std::mutex mu;
+};
+
+namespace {
+
+int check_options(const mf_options* o) {
+  if (!o) return MF_EINVAL;
+  if (o->max_iter_nnls < 0 || o->max_iter_outer < 0) return MF_EINVAL;
+  if (!(o->dchi2_tol >= 0) || !(o->nnls_eps >= 0)) return MF_EINVAL;
+  if (o->precision != MF_PREC_FP64 && o->precision != MF_PREC_MIXED) return MF_EINVAL;
+  if (o->schedule != MF_SCHED_GRID && o->schedule != MF_SCHED_PERSISTENT) return MF_EINVAL;
+  if (o->warm_start != MF_WARM_NONE && o->warm_start != MF_WARM_MLP) return MF_EINVAL;
+  if (o->nnls_start != MF_START_REFERENCE && o->nnls_start != MF_START_SUPPORT) return MF_EINVAL;
+  if (o->block_size < 0 || o->block_size > 1024 || (o->block_size % 32)) return MF_EINVAL;
+  return MF_OK;
+}
+
+int fill_args(mf_context* ctx, const mf_batch* b, const mf_options* o, FitArgs* a) {
+  if (!ctx || !b) return MF_EINVAL;
+  int rc = check_options(o);
+  if (rc) return rc;
+  if (b->n < 0 || (b->n > 0 && (!b->samples || !b->pederr || !b->amplitudes || !b->chi2))) return MF_EINVAL;
+  int nct = 0;
+  for (int t = 0; t < MF_MAX_CTYPES; ++t)
+    if (ctx->cond_set[t]) nct = t + 1;
+  if (nct == 0 || !ctx->cond_set[0]) return MF_EINVAL;
+  if (!b->ctype) nct = 1;
+  for (int t = 0; t < nct; ++t) {
+    if (!ctx->cond_set[t]) return MF_EINVAL;
+    if (b->sample_stride < ctx->cond[t].N || b->amp_stride < ctx->cond[t].K) return MF_EINVAL;
+    a->cond[t] = ctx->cond[t];
+  }
+  a->n_ctypes = nct;
+  a->opt.max_iter_nnls = o->max_iter_nnls;
+  a->opt.max_iter_outer = o->max_iter_outer;
+  a->opt.dchi2_tol = o->dchi2_tol;
+  a->opt.nnls_eps = o->nnls_eps;
+  a->opt.nnls_start = o->nnls_start;
+  a->opt.compute_errors = o->compute_errors;
+  a->n = b->n;
+  a->sample_stride = b->sample_stride;
+  a->amp_stride = b->amp_stride;
+  a->samples = b->samples;
+  a->pederr = b->pederr;
+  a->ctype = b->ctype;
+  a->amplitudes = b->amplitudes;
+  a->chi2 = b->chi2;
+  a->intime = b->intime;
+  a->errors = b->errors;
+  a->active_mask = b->active_mask;
+  a->status = b->status;
+  a->iters = b->iters;
+  a->flops = nullptr;
+  return MF_OK;
+}
+
+int dispatch(const FitArgs& a, const mf_options* o, cudaStream_t s, bool instrumented) {
+  if (o->precision != MF_PREC_FP64 || o->schedule != MF_SCHED_GRID || o->warm_start != MF_WARM_NONE)
+    return MF_EUNSUPPORTED;
+  cudaError_t e = launch_fit_fp64(a, o->block_size, s, instrumented);
+  if (e != cudaSuccess) {
+    set_last_error("fit_fp64 launch", e);
+    return MF_ECUDA;
+  }
+  return MF_OK;
+}
+
+void free_staging(mf_context* c) {
+  cudaFree(c->d_samples);
+  cudaFree(c->d_pederr);
+  cudaFree(c->d_ctype);
+  cudaFree(c->d_amp);
+  cudaFree(c->d_chi2);
+  cudaFree(c->d_intime);
+  cudaFree(c->d_errors);
+  cudaFree(c->d_mask);
+  cudaFree(c->d_status);
+  cudaFree(c->d_iters);
+  c->d_samples = nullptr;
+  c->d_pederr = nullptr;
+  c->d_ctype = nullptr;
+  c->d_amp = c->d_chi2 = c->d_intime = c->d_errors = nullptr;
+  c->d_mask = nullptr;
+  c->d_status = nullptr;
+  c->d_iters = nullptr;
+  c->cap = 0;
+}
+
+int grow_staging(mf_context* c, int64_t n, int ss, int as) {
+  if (n <= c->cap && ss <= c->cap_ss && as <= c->cap_as) return MF_OK;
+  free_staging(c);
+  cudaError_t e = cudaSuccess;
+  auto al = [&](void** p, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMalloc(p, bytes ? bytes : 1);
+  };
+  al((void**)&c->d_samples, sizeof(double) * n * ss);
+  al((void**)&c->d_pederr, sizeof(double) * n);
+  al((void**)&c->d_ctype, n);
+  al((void**)&c->d_amp, sizeof(double) * n * as);
+  al((void**)&c->d_chi2, sizeof(double) * n);
+  al((void**)&c->d_intime, sizeof(double) * n);
+  al((void**)&c->d_errors, sizeof(double) * n);
+  al((void**)&c->d_mask, sizeof(uint16_t) * n);
+  al((void**)&c->d_status, n);
+  al((void**)&c->d_iters, sizeof(int32_t) * n);
+  if (e != cudaSuccess) {
+    set_last_error("staging cudaMalloc", e);
+    free_staging(c);
+    return MF_ENOMEM;
+  }
+  c->cap = n;
+  c->cap_ss = ss;
+  c->cap_as = as;
+  return MF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mf_abi_version(void) { return MF_ABI_VERSION; }
+
+const char* mf_rc_string(int rc) {
+  switch (rc) {
+    case MF_OK: return "ok";
+    case MF_EINVAL: return "invalid argument";
+    case MF_ECUDA: return "CUDA error";
+    case MF_ETIMEOUT: return "device-side wait timed out";
+    case MF_ENOMEM: return "out of device memory";
+    case MF_EUNSUPPORTED: return "unsupported option combination";
+    case MF_ENOTRAINED: return "MLP weights not set";
+    default: return "unknown error";
+  }
+}
+
+const char* mf_last_error(void) { return g_last_error; }
+
+void mf_default_options(mf_options* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->max_iter_nnls = 10;
+  o->max_iter_outer = 50;
+  o->dchi2_tol = 1e-3;
+  o->nnls_eps = 1e-11;
+  o->nnls_start = MF_START_REFERENCE;
+  o->precision = MF_PREC_FP64;
+  o->schedule = MF_SCHED_GRID;
+  o->warm_start = MF_WARM_NONE;
+  o->compute_errors = 0;
+  o->block_size = 0;
+  o->blocks_per_sm = 0;
+}
+
+int mf_create(mf_context** out, int device) {
+  if (!out) return MF_EINVAL;
+  *out = nullptr;
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) {
+    set_last_error("cudaSetDevice", e);
+    return MF_ECUDA;
+  }
+  mf_context* c = new (std::nothrow) mf_context();
+  if (!c) return MF_ENOMEM;
+  c->device = device;
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    set_last_error("cudaStreamCreate", e);
+    delete c;
+    return MF_ECUDA;
+  }
+  *out = c;
+  return MF_OK;
+}
+
+void mf_destroy(mf_context* c) {
+  if (!c) return;
+  free_staging(c);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+int mf_set_conditions(mf_context* c, int t, const mf_conditions* cond) {
+  if (!c || !cond || t < 0 || t >= MF_MAX_CTYPES) return MF_EINVAL;
+  DevConditions d;
+  int rc = make_dev_conditions(*cond, &d);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> g(c->mu);
+  c->cond[t] = d;
+  c->cond_set[t] = 1;
+  return MF_OK;
+}
+
+int mf_fit(mf_context* c, const mf_batch* b, const mf_options* o, void* stream) {
+  FitArgs a;
+  int rc = fill_args(c, b, o, &a);
+  if (rc) return rc;
+  if (b->n == 0) return MF_OK;
+  return dispatch(a, o, (cudaStream_t)stream, false);
+}
+
+// Instrumented variant: same fit, plus the executed floating-point operation
+// count of every channel in flops[n] (device pointer). Used to measure the
+// algorithmic work of a workload; not part of the timed path.
+int mf_fit_count_flops(mf_context* c, const mf_batch* b, const mf_options* o, double* flops, void* stream) {
+  FitArgs a;
+  int rc = fill_args(c, b, o, &a);
+  if (rc) return rc;
+  if (!flops) return MF_EINVAL;
+  if (b->n == 0) return MF_OK;
+  a.flops = flops;
+  return dispatch(a, o, (cudaStream_t)stream, true);
+}
+
+int mf_fit_host(mf_context* c, const mf_batch* hb, const mf_options* o) {
+  if (!c || !hb) return MF_EINVAL;
+  std::lock_guard<std::mutex> g(c->mu);
+  const int64_t n = hb->n;
+  if (n < 0) return MF_EINVAL;
+  if (n == 0) return MF_OK;
+  int rc = grow_staging(c, n, hb->sample_stride, hb->amp_stride);
+  if (rc) return rc;
+  cudaStream_t s = c->stream;
+  cudaError_t e = cudaSuccess;
+  auto cp = [&](void* dst, const void* src, size_t bytes, cudaMemcpyKind k) {
+    if (e == cudaSuccess && src && dst) e = cudaMemcpyAsync(dst, src, bytes, k, s);
+  };
+  cp(c->d_samples, hb->samples, sizeof(double) * n * hb->sample_stride, cudaMemcpyHostToDevice);
+  cp(c->d_pederr, hb->pederr, sizeof(double) * n, cudaMemcpyHostToDevice);
+  if (hb->ctype) cp(c->d_ctype, hb->ctype, n, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    set_last_error("H2D copy", e);
+    return MF_ECUDA;
+  }
+  mf_batch db = *hb;
+  db.samples = c->d_samples;
+  db.pederr = c->d_pederr;
+  db.ctype = hb->ctype ? c->d_ctype : nullptr;
+  db.amplitudes = c->d_amp;
+  db.chi2 = c->d_chi2;
+  db.intime = hb->intime ? c->d_intime : nullptr;
+  db.errors = hb->errors ? c->d_errors : nullptr;
+  db.active_mask = hb->active_mask ? c->d_mask : nullptr;
+  db.status = hb->status ? c->d_status : nullptr;
+  db.iters = hb->iters ? c->d_iters : nullptr;
+  FitArgs a;
+  rc = fill_args(c, &db, o, &a);
+  if (rc) return rc;
+  rc = dispatch(a, o, s, false);
+  if (rc) return rc;
+  cp(hb->amplitudes, c->d_amp, sizeof(double) * n * hb->amp_stride, cudaMemcpyDeviceToHost);
+  cp(hb->chi2, c->d_chi2, sizeof(double) * n, cudaMemcpyDeviceToHost);
+  if (hb->intime) cp(hb->intime, c->d_intime, sizeof(double) * n, cudaMemcpyDeviceToHost);
+  if (hb->errors) cp(hb->errors, c->d_errors, sizeof(double) * n, cudaMemcpyDeviceToHost);
+  if (hb->active_mask) cp(hb->active_mask, c->d_mask, sizeof(uint16_t) * n, cudaMemcpyDeviceToHost);
+  if (hb->status) cp(hb->status, c->d_status, n, cudaMemcpyDeviceToHost);
+  if (hb->iters) cp(hb->iters, c->d_iters, sizeof(int32_t) * n, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    set_last_error("mf_fit_host", e);
+    return MF_ECUDA;
+  }
+  return MF_OK;
+}
+
+int mf_build_pulse_matrix(const double* fullpulse, const int8_t* bxs, int N, int K, double* P) {
+  if (!fullpulse || !bxs || !P || N < 1 || N > MF_MAX_SAMPLES || K < 1 || K > MF_MAX_PULSES) return MF_EINVAL;
+  const int NF = N + 9;
+  for (int k = 0; k < K; ++k) {
+    const int bx = bxs[k];
+    const int first = bx + 3 > 0 ? bx + 3 : 0;
+    const int offset = 7 - 3 - bx;
+    for (int i = 0; i < N; ++i) {
+      double v = 0.;
+      if (i >= first) {
+        const int idx = i + offset;
+        if (idx < 0 || idx >= NF) return MF_EINVAL;
+        v = fullpulse[idx];
+      }
+      P[k * N + i] = v;
+    }
+  }
+  return MF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,69 @@
+// Internal declarations shared by the engine's translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "multifit_gb300.h"
+
+namespace mfgb {
+
+constexpr int KMAX = 10;
+constexpr int NFMAX = MF_FULLPULSE_MAX;
+
+// Device copy of one condition set, passed to kernels by value (constant bank).
+struct DevConditions {
+  int N, K;
+  int intime_col;                // first k with bxs[k] == 0, or -1
+  int has_fpc;
+  double P[KMAX * KMAX];         // N x K column-major
+  double R[KMAX * KMAX];         // N x N column-major
+  int8_t bxs[KMAX];
+  int8_t fz[KMAX];               // first structurally non-zero row of column k (N if all zero)
+  double fpc[NFMAX * NFMAX];     // (N+9) x (N+9) column-major, valid when has_fpc
+};
+
+struct DevOptions {
+  int max_iter_nnls;
+  int max_iter_outer;
+  double dchi2_tol;
+  double nnls_eps;
+  int nnls_start;
+  int compute_errors;
+};
+
+// Everything a fit kernel needs, passed by value.
+struct FitArgs {
+  DevConditions cond[MF_MAX_CTYPES];
+  int n_ctypes;
+  DevOptions opt;
+  int64_t n;
+  int sample_stride;
+  int amp_stride;
+  const double* samples;
+  const double* pederr;
+  const uint8_t* ctype;
+  double* amplitudes;
+  double* chi2;
+  double* intime;
+  double* errors;
+  uint16_t* active_mask;
+  uint8_t* status;
+  int32_t* iters;
+  double* flops;  // optional per-channel executed-flop count (instrumented build only)
+};
+
+// Status bits (mirror of enum mf_channel_status).
+enum : uint8_t { CH_NNLS_MAXITER = 1, CH_OUTER_MAXITER = 2, CH_NONFINITE = 4, CH_BADINPUT = 8 };
+
+// Launchers (fit_fp64.cu).
+cudaError_t launch_fit_fp64(const FitArgs& a, int block, cudaStream_t s, bool instrumented);
+
+// Synthetic generator (synth.cu).
+int synth_conditions(int kind, mf_conditions* cond, double* sigma);
+
+// Host-side conversion of a public condition set.
+int make_dev_conditions(const mf_conditions& c, DevConditions* d);
+
+void set_last_error(const char* what, cudaError_t e);
+
+}  // namespace mfgb
