@@ -153,7 +153,11 @@ void mf_default_options(mf_options* opt);
 /* Creates a context bound to a CUDA device and allocates its workspace. */
 int mf_create(mf_context** out, int device);
 void mf_destroy(mf_context* ctx);
-/* Copies a condition set into the context (host memory; no device call). */
+/* Copies a condition set into the context. For a set without a pulse
+ * covariance it also builds, once, the tables of the mixed-precision and
+ * warm-start forms (whitening operator and the least-squares operator of every
+ * passive set, ~0.6 MB for N = K = 10) and uploads them to the device
+ * (synchronous; not a hot-path call). */
 int mf_set_conditions(mf_context* ctx, int ctype, const mf_conditions* cond);
 
 /* Fits a batch whose buffers are in device memory; asynchronous on `stream`
@@ -177,6 +181,12 @@ int mf_fit_host(mf_context* ctx, const mf_batch* host_batch, const mf_options* o
  * for i >= max(0, bx_k+3), else 0. Host-only. */
 int mf_build_pulse_matrix(const double* fullpulse, const int8_t* bxs, int nsamples, int npulses,
                           double* pulse_matrix);
+
+/* Host-only view of the mixed-form tables of a condition set (for checks):
+ * whiten [N][N] row-major = L_R^-1 with L_R = chol(samplecor); pinv [p][N]
+ * row-major = the least-squares operator of the passive set `mask` (columns in
+ * ascending order, p = popcount(mask)). Either output may be NULL. */
+int mf_table_operator(const mf_conditions* cond, uint32_t mask, double* whiten, double* pinv);
 
 /* Synthetic channels ---------------------------------------------------- */
 

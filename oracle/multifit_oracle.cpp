@@ -454,7 +454,7 @@ struct FitResult {
   double flops;
 };
 
-enum : uint8_t { CH_OK = 0, CH_NNLS_MAXITER = 1, CH_OUTER_MAXITER = 2, CH_NONFINITE = 4 };
+enum : uint8_t { CH_OK = 0, CH_NNLS_MAXITER = 1, CH_OUTER_MAXITER = 2, CH_NONFINITE = 4, CH_BADINPUT = 8 };
 
 // DoFit, multifit_cpu/src/PulseChiSqSNNLS.cpp:21-147
 void dofit(const FitConfig& cfg, const double* samples, double pederr, FitResult& out, bool count) {
@@ -525,6 +525,9 @@ void dofit(const FitConfig& cfg, const double* samples, double pederr, FitResult
   bool finite = std::isfinite(out.chisq);
   for (int k = 0; k < K; ++k) finite = finite && std::isfinite(out.amp[k]);
   if (!finite) status |= CH_NONFINITE;
+  bool bad = !std::isfinite(pederr);
+  for (int i = 0; i < N; ++i) bad = bad || !std::isfinite(samples[i]);
+  if (bad) status |= CH_BADINPUT;
   out.status = status;
   out.outer_iters = main_outer;
   out.fnnls_iters = main_st.outer_iters;

@@ -112,6 +112,7 @@ SIGNATURES = [
     ("mf_fit_count_flops", C.c_int, [C.c_void_p, C.POINTER(MfBatch), C.POINTER(MfOptions), C.c_void_p, C.c_void_p]),
     ("mf_fit_host", C.c_int, [C.c_void_p, C.POINTER(MfBatch), C.POINTER(MfOptions)]),
     ("mf_build_pulse_matrix", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
+    ("mf_table_operator", C.c_int, [C.POINTER(MfConditions), C.c_uint32, C.c_void_p, C.c_void_p]),
     ("mf_synth_conditions", C.c_int, [C.c_int, C.POINTER(MfConditions), C.POINTER(C.c_double)]),
     ("mf_synth_generate", C.c_int, [C.POINTER(MfSynthParams), C.c_int64, C.c_int64, C.c_int, C.c_void_p,
                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
@@ -213,6 +214,17 @@ def build_pulse_matrix(fullpulse, bxs, nsamples: int = 10) -> np.ndarray:
     _check(load_library().mf_build_pulse_matrix(fp.ctypes.data, bx.ctypes.data, nsamples, K, out.ctypes.data),
            "mf_build_pulse_matrix")
     return out.reshape(K, nsamples).T.copy()
+
+
+def table_operator(cond: MfConditions, mask: int):
+    """(L_R^-1 (N,N), pseudo-inverse (p,N)) of the mixed-form tables (host computation)."""
+    N = cond.nsamples
+    p = bin(mask).count("1")
+    W = np.zeros(N * N)
+    P = np.zeros(p * N)
+    _check(load_library().mf_table_operator(C.byref(cond), mask, W.ctypes.data, P.ctypes.data),
+           "mf_table_operator")
+    return W.reshape(N, N), P.reshape(p, N)
 
 
 # Workloads of the benchmark configurations: (n, synth params).

@@ -55,6 +55,12 @@ struct mf_context {
   int device = 0;
   DevConditions cond[MF_MAX_CTYPES];
   int cond_set[MF_MAX_CTYPES] = {0, 0};
+  // mixed / warm-start tables per condition set (built by mf_set_conditions)
+  HostTables tab[MF_MAX_CTYPES];
+  int tab_ok[MF_MAX_CTYPES] = {0, 0};
+  int* d_offset[MF_MAX_CTYPES] = {nullptr, nullptr};
+  double* d_pinv64[MF_MAX_CTYPES] = {nullptr, nullptr};
+  float* d_pinv32[MF_MAX_CTYPES] = {nullptr, nullptr};
   // staging area for mf_fit_host
   int64_t cap = 0;
   int cap_ss = 0, cap_as = 0;
@@ -125,7 +131,43 @@ int fill_args(mf_context* ctx, const mf_batch* b, const mf_options* o, FitArgs* 
   return MF_OK;
 }
 
-int dispatch(const FitArgs& a, const mf_options* o, cudaStream_t s, bool instrumented) {
+void fill_dev_mixed(const mf_context* c, int t, DevMixed* m);
+
+int dispatch_mixed(const mf_context* c, const FitArgs& a, const mf_options* o, cudaStream_t s) {
+  if (o->compute_errors || o->schedule != MF_SCHED_GRID || o->warm_start != MF_WARM_NONE) return MF_EUNSUPPORTED;
+  MixedArgs m;
+  std::memset(&m, 0, sizeof(m));
+  for (int t = 0; t < a.n_ctypes; ++t) {
+    if (!c->tab_ok[t]) return MF_EUNSUPPORTED;
+    fill_dev_mixed(c, t, &m.tab[t]);
+  }
+  m.n_ctypes = a.n_ctypes;
+  m.n = a.n;
+  m.sample_stride = a.sample_stride;
+  m.amp_stride = a.amp_stride;
+  m.max_iter32 = 3 * KMAX;
+  m.max_iter64 = o->max_iter_nnls > 0 ? o->max_iter_nnls : 1;
+  m.tol32 = 1e-5f;
+  m.eps = o->nnls_eps;
+  m.samples = a.samples;
+  m.pederr = a.pederr;
+  m.ctype = a.ctype;
+  m.amplitudes = a.amplitudes;
+  m.chi2 = a.chi2;
+  m.intime = a.intime;
+  m.active_mask = a.active_mask;
+  m.status = a.status;
+  m.iters = a.iters;
+  cudaError_t e = launch_fit_mixed(m, o->block_size, s);
+  if (e != cudaSuccess) {
+    set_last_error("fit_mixed launch", e);
+    return MF_ECUDA;
+  }
+  return MF_OK;
+}
+
+int dispatch(const mf_context* c, const FitArgs& a, const mf_options* o, cudaStream_t s, bool instrumented) {
+  if (o->precision == MF_PREC_MIXED && !instrumented) return dispatch_mixed(c, a, o, s);
   if (o->precision != MF_PREC_FP64 || o->schedule != MF_SCHED_GRID || o->warm_start != MF_WARM_NONE)
     return MF_EUNSUPPORTED;
   cudaError_t e = launch_fit_fp64(a, o->block_size, s, instrumented);
@@ -155,6 +197,65 @@ void free_staging(mf_context* c) {
   c->d_status = nullptr;
   c->d_iters = nullptr;
   c->cap = 0;
+}
+
+void free_tables(mf_context* c, int t) {
+  cudaFree(c->d_offset[t]);
+  cudaFree(c->d_pinv64[t]);
+  cudaFree(c->d_pinv32[t]);
+  c->d_offset[t] = nullptr;
+  c->d_pinv64[t] = nullptr;
+  c->d_pinv32[t] = nullptr;
+  c->tab_ok[t] = 0;
+}
+
+// Builds the mixed-form tables of set t and uploads them. A set the mixed form
+// cannot serve (pulse covariance, K > N, a shape without a build, or a
+// non-positive-definite samplecor) keeps tab_ok = 0; mf_fit then reports
+// MF_EUNSUPPORTED for the mixed precision on it.
+int upload_tables(mf_context* c, int t) {
+  free_tables(c, t);
+  const DevConditions& d = c->cond[t];
+  const bool shape_ok = (d.N == 10 && d.K == 10) || (d.N == 8 && d.K == 8);
+  if (d.has_fpc || !shape_ok) return MF_OK;
+  HostTables& h = c->tab[t];
+  if (build_mixed_tables(d, &h) != MF_OK) return MF_OK;
+  cudaError_t e = cudaSetDevice(c->device);
+  const size_t no = h.offset.size(), np = h.pinv64.size();
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_offset[t], sizeof(int) * no);
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_pinv64[t], sizeof(double) * np);
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_pinv32[t], sizeof(float) * np);
+  if (e == cudaSuccess) e = cudaMemcpy(c->d_offset[t], h.offset.data(), sizeof(int) * no, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(c->d_pinv64[t], h.pinv64.data(), sizeof(double) * np, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(c->d_pinv32[t], h.pinv32.data(), sizeof(float) * np, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    set_last_error("table upload", e);
+    free_tables(c, t);
+    return MF_ECUDA;
+  }
+  c->tab_ok[t] = 1;
+  return MF_OK;
+}
+
+void fill_dev_mixed(const mf_context* c, int t, DevMixed* m) {
+  const HostTables& h = c->tab[t];
+  const int N = h.N, K = h.K;
+  std::memset(m, 0, sizeof(*m));
+  m->N = N;
+  m->K = K;
+  m->intime_col = c->cond[t].intime_col;
+  std::memcpy(m->W64, h.W64, sizeof(h.W64));
+  std::memcpy(m->G64, h.G64, sizeof(h.G64));
+  std::memcpy(m->H64, h.H64, sizeof(h.H64));
+  std::memcpy(m->G32, h.G32, sizeof(h.G32));
+  std::memcpy(m->H32, h.H32, sizeof(h.H32));
+  for (int k = 0; k < K; ++k) {
+    m->gnorm32[k] = float(std::sqrt(h.gnorm2[k]));
+    m->gfz[k] = int8_t(h.gfz[k]);
+  }
+  m->offset = c->d_offset[t];
+  m->pinv64 = c->d_pinv64[t];
+  m->pinv32 = c->d_pinv32[t];
 }
 
 int grow_staging(mf_context* c, int64_t n, int ss, int as) {
@@ -246,6 +347,7 @@ int mf_create(mf_context** out, int device) {
 void mf_destroy(mf_context* c) {
   if (!c) return;
   free_staging(c);
+  for (int t = 0; t < MF_MAX_CTYPES; ++t) free_tables(c, t);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -258,7 +360,7 @@ int mf_set_conditions(mf_context* c, int t, const mf_conditions* cond) {
   std::lock_guard<std::mutex> g(c->mu);
   c->cond[t] = d;
   c->cond_set[t] = 1;
-  return MF_OK;
+  return upload_tables(c, t);
 }
 
 int mf_fit(mf_context* c, const mf_batch* b, const mf_options* o, void* stream) {
@@ -266,7 +368,7 @@ int mf_fit(mf_context* c, const mf_batch* b, const mf_options* o, void* stream) 
   int rc = fill_args(c, b, o, &a);
   if (rc) return rc;
   if (b->n == 0) return MF_OK;
-  return dispatch(a, o, (cudaStream_t)stream, false);
+  return dispatch(c, a, o, (cudaStream_t)stream, false);
 }
 
 // Instrumented variant: same fit, plus the executed floating-point operation
@@ -279,7 +381,7 @@ int mf_fit_count_flops(mf_context* c, const mf_batch* b, const mf_options* o, do
   if (!flops) return MF_EINVAL;
   if (b->n == 0) return MF_OK;
   a.flops = flops;
-  return dispatch(a, o, (cudaStream_t)stream, true);
+  return dispatch(c, a, o, (cudaStream_t)stream, true);
 }
 
 int mf_fit_host(mf_context* c, const mf_batch* hb, const mf_options* o) {
@@ -316,7 +418,7 @@ int mf_fit_host(mf_context* c, const mf_batch* hb, const mf_options* o) {
   FitArgs a;
   rc = fill_args(c, &db, o, &a);
   if (rc) return rc;
-  rc = dispatch(a, o, s, false);
+  rc = dispatch(c, a, o, s, false);
   if (rc) return rc;
   cp(hb->amplitudes, c->d_amp, sizeof(double) * n * hb->amp_stride, cudaMemcpyDeviceToHost);
   cp(hb->chi2, c->d_chi2, sizeof(double) * n, cudaMemcpyDeviceToHost);
@@ -329,6 +431,28 @@ int mf_fit_host(mf_context* c, const mf_batch* hb, const mf_options* o) {
   if (e != cudaSuccess) {
     set_last_error("mf_fit_host", e);
     return MF_ECUDA;
+  }
+  return MF_OK;
+}
+
+int mf_table_operator(const mf_conditions* cond, uint32_t mask, double* whiten, double* pinv) {
+  if (!cond) return MF_EINVAL;
+  DevConditions d;
+  int rc = make_dev_conditions(*cond, &d);
+  if (rc) return rc;
+  if (d.has_fpc || d.K > d.N) return MF_EUNSUPPORTED;
+  if (mask == 0 || mask >= (1u << d.K)) return MF_EINVAL;
+  HostTables h;
+  rc = build_mixed_tables(d, &h);
+  if (rc) return rc;
+  if (whiten) {
+    int w = 0;
+    for (int i = 0; i < d.N; ++i)
+      for (int j = 0; j < d.N; ++j) whiten[i * d.N + j] = j <= i ? h.W64[w++] : 0.;
+  }
+  if (pinv) {
+    const int p = __builtin_popcount(mask);
+    std::memcpy(pinv, h.pinv64.data() + h.offset[mask], sizeof(double) * p * d.N);
   }
   return MF_OK;
 }

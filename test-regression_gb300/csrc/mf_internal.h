@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "multifit_gb300.h"
 
 namespace mfgb {
@@ -57,6 +59,61 @@ enum : uint8_t { CH_NNLS_MAXITER = 1, CH_OUTER_MAXITER = 2, CH_NONFINITE = 4, CH
 
 // Launchers (fit_fp64.cu).
 cudaError_t launch_fit_fp64(const FitArgs& a, int block, cudaStream_t s, bool instrumented);
+
+// Host tables of one condition set for the mixed / warm forms (tables.cu).
+struct HostTables {
+  int N = 0, K = 0;
+  double W64[KMAX * (KMAX + 1) / 2];  // L_R^-1, packed lower rows
+  float W32[KMAX * (KMAX + 1) / 2];
+  double G64[KMAX * KMAX];            // G = L_R^-1 P, N x K column-major
+  float G32[KMAX * KMAX];
+  double H64[KMAX * KMAX];            // G^T G, row-major ld KMAX
+  float H32[KMAX * KMAX];
+  double gnorm2[KMAX];                // |G_k|^2
+  int gfz[KMAX];                      // first structurally non-zero row of G_k
+  std::vector<int> offset;            // per passive-set mask: offset of its p x N pseudo-inverse
+  std::vector<double> pinv64;
+  std::vector<float> pinv32;
+};
+int build_mixed_tables(const DevConditions& c, HostTables* t);
+
+// Device view of one condition set's tables, passed by value.
+struct DevMixed {
+  int N, K, intime_col;
+  double W64[KMAX * (KMAX + 1) / 2];
+  double G64[KMAX * KMAX];
+  double H64[KMAX * KMAX];
+  float G32[KMAX * KMAX];
+  float H32[KMAX * KMAX];
+  float gnorm32[KMAX];
+  int8_t gfz[KMAX];
+  const int* offset;
+  const double* pinv64;
+  const float* pinv32;
+};
+
+struct MixedArgs {
+  DevMixed tab[MF_MAX_CTYPES];
+  int n_ctypes;
+  int64_t n;
+  int sample_stride, amp_stride;
+  int max_iter32, max_iter64;
+  float tol32;
+  double eps;
+  const double* samples;
+  const double* pederr;
+  const uint8_t* ctype;
+  const uint16_t* warm_mask;  // learned warm start: predicted passive set, or null
+  const float* warm_amp;      // predicted amplitudes [n][warm_stride]
+  int warm_stride;
+  double* amplitudes;
+  double* chi2;
+  double* intime;
+  uint16_t* active_mask;
+  uint8_t* status;
+  int32_t* iters;
+};
+cudaError_t launch_fit_mixed(const MixedArgs& a, int block, cudaStream_t s);
 
 // Synthetic generator (synth.cu).
 int synth_conditions(int kind, mf_conditions* cond, double* sigma);

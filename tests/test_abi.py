@@ -101,3 +101,24 @@ def test_build_pulse_matrix_reference_rule(mf):
             assert P[i, k] == exp
     with pytest.raises(mf.MultifitError):
         mf.build_pulse_matrix(fp, np.array([-9]), 10)  # reads before fullpulse(0)
+
+
+@pytest.mark.parametrize("kind", [0, 1])
+def test_mixed_tables_are_least_squares_operators(mf, kind):
+    """The pseudo-inverse of every passive set equals numpy's least-squares
+    solution of the whitened problem (the tables behind the mixed form)."""
+    cond, sigma = mf.synth_conditions(kind)
+    P, R, bxs, _ = mf.conditions_arrays(cond)
+    N, K = P.shape
+    Lr = np.linalg.cholesky(R)
+    G = np.linalg.solve(Lr, P)
+    W, _ = mf.table_operator(cond, 1)
+    np.testing.assert_allclose(W, np.linalg.inv(Lr), rtol=1e-12, atol=1e-14)
+    rng = np.random.default_rng(kind)
+    y = rng.standard_normal(N)
+    for mask in list(rng.integers(1, 1 << K, size=40)) + [(1 << K) - 1, 1]:
+        cols = [k for k in range(K) if mask >> k & 1]
+        _, Pi = mf.table_operator(cond, int(mask))
+        x = Pi @ y
+        xr = np.linalg.lstsq(G[:, cols], y, rcond=None)[0]
+        np.testing.assert_allclose(x, xr, rtol=1e-9, atol=1e-12 * np.abs(xr).max())

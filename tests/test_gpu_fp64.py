@@ -157,16 +157,18 @@ def test_edge_cases(mf, oracle, engine, cuda):
     assert np.isfinite(out["amplitudes"][5]).all()
 
 
-def test_bad_condition_index(mf, engine, cuda):
-    ecal_engine(mf, engine)
+def test_bad_condition_index(mf, cuda):
+    eng = mf.Engine(0)
+    ecal_engine(mf, eng)
     n = 4
     s = np.zeros((n, 10))
     ct = np.array([0, 1, 0, 7], dtype=np.uint8)
     with pytest.raises(mf.MultifitError):  # set 1 was never given
-        engine.fit_host(s, np.full(n, 0.044), ctype=ct)
-    mixed_engine(mf, engine)
-    out = engine.fit_host(s, np.full(n, 0.044), ctype=ct)
+        eng.fit_host(s, np.full(n, 0.044), ctype=ct)
+    mixed_engine(mf, eng)
+    out = eng.fit_host(s, np.full(n, 0.044), ctype=ct)
     assert out["status"][3] == mf.CH_BADINPUT
+    eng.close()
 
 
 def test_pulsechisq_mirror_matches_oracle(mf, oracle, cuda):

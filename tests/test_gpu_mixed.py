@@ -1,0 +1,104 @@
+"""GPU mixed-precision form (FP32 active-set search with table solves, FP64
+judge, FP64 chi2) against the FP64 oracle run to KKT convergence (support
+start, max_iter 1000), on the same seeded inputs.
+
+Tolerances (floating point): per channel the normwise relative amplitude
+error max_k |a_k - a_ref_k| / max_k |a_ref_k| must be <= 1e-4 (the headline
+bound) on at least 99.9 % of channels and <= 1e-6 on the median; chi2 relative
+error <= 1e-6 where the active sets agree; active sets (support of X())
+identical on at least 99.9 % of channels. The FP64 oracle's own error on the
+worst-conditioned passive sets is ~cond(G)^2 * 1.1e-16 ~ 3e-7 relative.
+"""
+import numpy as np
+import pytest
+
+from _helpers import DeviceBatch, oracle_fit_sets
+
+pytestmark = pytest.mark.gpu
+
+AMP_TOL = 1e-4
+CHI2_TOL = 1e-6
+
+
+def relerr(a, r):
+    scale = np.maximum(np.abs(r).max(axis=1), 1e-300)
+    return np.abs(a[:, : r.shape[1]] - r).max(axis=1) / scale
+
+
+def run_mixed(mf, cuda, eng, params, n, ctype=False, **opt):
+    db = DeviceBatch(mf, cuda, n, ctype=ctype)
+    db.generate(mf, params)
+    eng.fit_device(db.batch, mf.default_options(precision=mf.PREC_MIXED, max_iter_nnls=1000, **opt))
+    return db.inputs_host(), db.outputs_host()
+
+
+def check_against_oracle(mf, oracle, eng, inp, gpu, frac=0.999):
+    ref = oracle_fit_sets(mf, oracle, eng, inp, max_iter_nnls=1000, start=1)
+    err = relerr(gpu["amplitudes"], ref["amplitudes"])
+    same = gpu["active_mask"] == ref["active_mask"]
+    assert (err <= AMP_TOL).mean() >= frac, f"amp err p99.9={np.percentile(err, 99.9):.3g} max={err.max():.3g}"
+    assert np.median(err) <= 1e-6
+    assert same.mean() >= frac, f"active-set agreement {same.mean():.5f}"
+    c = ref["chi2"][same]
+    assert (np.abs(gpu["chi2"][same] - c) <= CHI2_TOL * np.maximum(c, 1.0)).mean() >= frac
+    assert (gpu["status"] == 0).all()
+    return err, same
+
+
+@pytest.mark.parametrize("wl", ["ecal-pu2", "ecal-logamp-pu4"])
+def test_mixed_vs_oracle_ecal(mf, oracle, cuda, wl):
+    params = {"ecal-pu2": mf.synth_params(2, 50_000, pileup_mean=2.0),
+              "ecal-logamp-pu4": mf.synth_params(3, 50_000, intime_log=True, lo=0.1, hi=1000.0,
+                                                 pileup_mean=4.0)}[wl]
+    eng = mf.Engine(0)
+    cond, _ = mf.synth_conditions(mf.SYNTH_ECAL)
+    eng.set_conditions(0, cond)
+    inp, gpu = run_mixed(mf, cuda, eng, params, 50_000)
+    check_against_oracle(mf, oracle, eng, inp, gpu)
+    eng.close()
+
+
+def test_mixed_vs_oracle_ecal_hcal(mf, oracle, cuda):
+    eng = mf.Engine(0)
+    eng.set_conditions(0, mf.synth_conditions(mf.SYNTH_ECAL)[0])
+    eng.set_conditions(1, mf.synth_conditions(mf.SYNTH_HCAL)[0])
+    params = mf.synth_params(4, 40_000, pileup_mean=-8.0, hcal_fraction=0.4)
+    inp, gpu = run_mixed(mf, cuda, eng, params, 40_000, ctype=True)
+    check_against_oracle(mf, oracle, eng, inp, gpu)
+    eng.close()
+
+
+def test_mixed_matches_fp64_gpu_path(mf, cuda):
+    """Mixed form vs the plain FP64 kernel run to convergence, full batch on the GPU."""
+    eng = mf.Engine(0)
+    eng.set_conditions(0, mf.synth_conditions(mf.SYNTH_ECAL)[0])
+    n = 200_000
+    p = mf.synth_params(3, n, intime_log=True, lo=0.1, hi=1000.0, pileup_mean=4.0)
+    from _helpers import DeviceBatch
+
+    db = DeviceBatch(mf, cuda, n)
+    db.generate(mf, p)
+    eng.fit_device(db.batch, mf.default_options(max_iter_nnls=1000, nnls_start=mf.START_SUPPORT))
+    f64 = db.outputs_host()
+    eng.fit_device(db.batch, mf.default_options(precision=mf.PREC_MIXED, max_iter_nnls=1000))
+    mix = db.outputs_host()
+    err = relerr(mix["amplitudes"], f64["amplitudes"])
+    assert (err <= AMP_TOL).mean() >= 0.999
+    assert (mix["active_mask"] == f64["active_mask"]).mean() >= 0.999
+    eng.close()
+
+
+def test_mixed_rejects_unsupported(mf, cuda):
+    eng = mf.Engine(0)
+    cond, _ = mf.synth_conditions(mf.SYNTH_ECAL)
+    eng.set_conditions(0, cond)
+    s = np.zeros((2, 10))
+    with pytest.raises(mf.MultifitError):
+        eng.fit_host(s, np.full(2, 0.044), options=mf.default_options(precision=mf.PREC_MIXED, compute_errors=1))
+    P, R, bxs, _ = mf.conditions_arrays(cond)
+    F = np.zeros((19, 19))
+    F[7:, 7:] = 1e-6
+    eng.set_conditions(0, mf.make_conditions(P, R, bxs, F))
+    with pytest.raises(mf.MultifitError):
+        eng.fit_host(s, np.full(2, 0.044), options=mf.default_options(precision=mf.PREC_MIXED))
+    eng.close()
