@@ -182,6 +182,41 @@ int mf_fit_host(mf_context* ctx, const mf_batch* host_batch, const mf_options* o
 int mf_build_pulse_matrix(const double* fullpulse, const int8_t* bxs, int nsamples, int npulses,
                           double* pulse_matrix);
 
+/* Learned warm start ------------------------------------------------------
+ * A small MLP (16 -> 128 -> 128 -> 32, GELU, BF16 tensor-core GEMMs with FP32
+ * accumulate, FP32 master weights) predicts from a channel's whitened
+ * samples and noise scale its passive set and amplitudes; the mixed form
+ * (warm_start = MF_WARM_MLP) then starts FNNLS there and still runs it to KKT
+ * convergence with the FP64 judge, so a wrong prediction costs iterations,
+ * never accuracy. It serves one condition set with N = K = 10; channels of
+ * other sets start cold. No counterpart in the reference. */
+typedef struct mf_mlp_train_params {
+  int32_t epochs;
+  int32_t batch;      /* multiple of 64 */
+  float lr;           /* Adam learning rate */
+  float amp_weight;   /* weight of the amplitude loss against the passive-set BCE */
+} mf_mlp_train_params;
+
+int mf_mlp_param_count(void);
+/* Allocates the network (He-normal init from `seed`) for condition set `ctype`,
+ * plus an inference workspace of `chunk` channels (0 = 1,048,576). */
+int mf_mlp_init(mf_context* ctx, int ctype, uint64_t seed, int64_t chunk);
+/* Trains on device data: batch.samples/pederr/ctype are the inputs and
+ * batch.amplitudes holds their converged fits (the targets). Writes the mean
+ * loss of each epoch to epoch_loss (host, may be NULL). Synchronous. */
+int mf_mlp_train(mf_context* ctx, const mf_batch* data, const mf_mlp_train_params* p, float* epoch_loss, void* stream);
+/* Gradient check: one forward/backward on the first p->batch channels of
+ * `data` without an update. Host outputs: grads[mf_mlp_param_count()], the
+ * bf16 bit patterns of the input features [batch][16], the targets
+ * [batch][20] (10 support bits, 10 scaled amplitudes) and the batch loss. */
+int mf_mlp_gradient(mf_context* ctx, const mf_batch* data, const mf_mlp_train_params* p, float* grads,
+                    uint16_t* features_bf16, float* targets, float* loss);
+int mf_mlp_get_weights(mf_context* ctx, float* host_params);
+int mf_mlp_set_weights(mf_context* ctx, const float* host_params);
+/* Inference on device pointers: predicted passive set mask[n], amplitudes
+ * amp[n][10] (GeV) and optionally the raw outputs logits[n][32]. */
+int mf_mlp_predict(mf_context* ctx, const mf_batch* batch, uint16_t* mask, float* amp, float* logits, void* stream);
+
 /* Host-only view of the mixed-form tables of a condition set (for checks):
  * whiten [N][N] row-major = L_R^-1 with L_R = chol(samplecor); pinv [p][N]
  * row-major = the least-squares operator of the passive set `mask` (columns in

@@ -99,6 +99,10 @@ class MfSynthParams(C.Structure):
     ]
 
 
+class MfMlpTrainParams(C.Structure):
+    _fields_ = [("epochs", C.c_int32), ("batch", C.c_int32), ("lr", C.c_float), ("amp_weight", C.c_float)]
+
+
 # Exported symbols and their signatures: (name, restype, argtypes).
 SIGNATURES = [
     ("mf_abi_version", C.c_int, []),
@@ -113,6 +117,14 @@ SIGNATURES = [
     ("mf_fit_host", C.c_int, [C.c_void_p, C.POINTER(MfBatch), C.POINTER(MfOptions)]),
     ("mf_build_pulse_matrix", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
     ("mf_table_operator", C.c_int, [C.POINTER(MfConditions), C.c_uint32, C.c_void_p, C.c_void_p]),
+    ("mf_mlp_param_count", C.c_int, []),
+    ("mf_mlp_init", C.c_int, [C.c_void_p, C.c_int, C.c_uint64, C.c_int64]),
+    ("mf_mlp_train", C.c_int, [C.c_void_p, C.POINTER(MfBatch), C.POINTER(MfMlpTrainParams), C.c_void_p, C.c_void_p]),
+    ("mf_mlp_gradient", C.c_int, [C.c_void_p, C.POINTER(MfBatch), C.POINTER(MfMlpTrainParams), C.c_void_p,
+                                  C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("mf_mlp_get_weights", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("mf_mlp_set_weights", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("mf_mlp_predict", C.c_int, [C.c_void_p, C.POINTER(MfBatch), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("mf_synth_conditions", C.c_int, [C.c_int, C.POINTER(MfConditions), C.POINTER(C.c_double)]),
     ("mf_synth_generate", C.c_int, [C.POINTER(MfSynthParams), C.c_int64, C.c_int64, C.c_int, C.c_void_p,
                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
@@ -341,6 +353,91 @@ class Engine:
                         out["iters"].ctypes.data)
         _check(self.lib.mf_fit_host(self.h, C.byref(b), C.byref(options or default_options())), "mf_fit_host")
         return out
+
+
+def mlp_params(epochs=3, batch=8192, lr=2e-3, amp_weight=1.0) -> MfMlpTrainParams:
+    p = MfMlpTrainParams()
+    p.epochs, p.batch, p.lr, p.amp_weight = epochs, batch, lr, amp_weight
+    return p
+
+
+# Flat parameter layout of the MLP: (name, shape) in order.
+MLP_LAYOUT = [("W1", (128, 16)), ("b1", (128,)), ("W2", (128, 128)), ("b2", (128,)), ("W3", (32, 128)),
+              ("b3", (32,))]
+
+
+def mlp_unflatten(flat: np.ndarray) -> dict:
+    out, o = {}, 0
+    for name, shape in MLP_LAYOUT:
+        size = int(np.prod(shape))
+        out[name] = flat[o:o + size].reshape(shape)
+        o += size
+    return out
+
+
+def _mlp_engine_methods():
+    def mlp_init(self, ctype=0, seed=1, chunk=0):
+        _check(self.lib.mf_mlp_init(self.h, ctype, seed, chunk), "mf_mlp_init")
+
+    def mlp_train(self, batch: MfBatch, params: MfMlpTrainParams, stream=None):
+        losses = np.zeros(max(params.epochs, 1), dtype=np.float32)
+        _check(self.lib.mf_mlp_train(self.h, C.byref(batch), C.byref(params), losses.ctypes.data, stream),
+               "mf_mlp_train")
+        return losses[: params.epochs]
+
+    def mlp_gradient(self, batch: MfBatch, params: MfMlpTrainParams):
+        n = self.lib.mf_mlp_param_count()
+        B = params.batch
+        g = np.zeros(n, dtype=np.float32)
+        f = np.zeros((B, 16), dtype=np.uint16)
+        t = np.zeros((B, 20), dtype=np.float32)
+        loss = np.zeros(1, dtype=np.float32)
+        _check(self.lib.mf_mlp_gradient(self.h, C.byref(batch), C.byref(params), g.ctypes.data, f.ctypes.data,
+                                        t.ctypes.data, loss.ctypes.data), "mf_mlp_gradient")
+        feats = (f.astype(np.uint32) << 16).view(np.float32)
+        return g, feats, t, float(loss[0])
+
+    def mlp_get_weights(self):
+        w = np.zeros(self.lib.mf_mlp_param_count(), dtype=np.float32)
+        _check(self.lib.mf_mlp_get_weights(self.h, w.ctypes.data), "mf_mlp_get_weights")
+        return w
+
+    def mlp_set_weights(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        _check(self.lib.mf_mlp_set_weights(self.h, w.ctypes.data), "mf_mlp_set_weights")
+
+    def mlp_predict(self, batch: MfBatch, mask_ptr, amp_ptr, logits_ptr=None, stream=None):
+        _check(self.lib.mf_mlp_predict(self.h, C.byref(batch), mask_ptr, amp_ptr, logits_ptr, stream),
+               "mf_mlp_predict")
+
+    return dict(mlp_init=mlp_init, mlp_train=mlp_train, mlp_gradient=mlp_gradient, mlp_get_weights=mlp_get_weights,
+                mlp_set_weights=mlp_set_weights, mlp_predict=mlp_predict)
+
+
+for _k, _v in _mlp_engine_methods().items():
+    setattr(Engine, _k, _v)
+
+
+def save_mlp_weights(path: str, flat: np.ndarray, meta: dict | None = None):
+    """Checkpoint: a JSON header line then the little-endian float32 parameters."""
+    import json
+
+    hdr = {"format": "multifit-gb300-mlp", "version": 1, "layout": MLP_LAYOUT, "count": int(flat.size)}
+    hdr.update(meta or {})
+    with open(path, "wb") as f:
+        f.write((json.dumps(hdr) + "\n").encode())
+        f.write(np.ascontiguousarray(flat, dtype="<f4").tobytes())
+
+
+def load_mlp_weights(path: str):
+    import json
+
+    with open(path, "rb") as f:
+        hdr = json.loads(f.readline().decode())
+        flat = np.frombuffer(f.read(), dtype="<f4").copy()
+    if hdr.get("format") != "multifit-gb300-mlp" or flat.size != hdr["count"]:
+        raise ValueError(f"{path}: not an MLP checkpoint")
+    return flat, hdr
 
 
 def unpack_iters(iters: np.ndarray):

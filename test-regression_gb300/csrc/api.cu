@@ -6,6 +6,8 @@
 #include <new>
 
 #include "mf_internal.h"
+#include "mlp.h"
+#include "mlp_state.h"
 
 namespace mfgb {
 
@@ -61,6 +63,8 @@ struct mf_context {
   int* d_offset[MF_MAX_CTYPES] = {nullptr, nullptr};
   double* d_pinv64[MF_MAX_CTYPES] = {nullptr, nullptr};
   float* d_pinv32[MF_MAX_CTYPES] = {nullptr, nullptr};
+  MlpState mlp;
+  int sms = 152;
   // staging area for mf_fit_host
   int64_t cap = 0;
   int cap_ss = 0, cap_as = 0;
@@ -134,7 +138,9 @@ int fill_args(mf_context* ctx, const mf_batch* b, const mf_options* o, FitArgs* 
 void fill_dev_mixed(const mf_context* c, int t, DevMixed* m);
 
 int dispatch_mixed(const mf_context* c, const FitArgs& a, const mf_options* o, cudaStream_t s) {
-  if (o->compute_errors || o->schedule != MF_SCHED_GRID || o->warm_start != MF_WARM_NONE) return MF_EUNSUPPORTED;
+  if (o->compute_errors || o->schedule != MF_SCHED_GRID) return MF_EUNSUPPORTED;
+  const bool warm = o->warm_start == MF_WARM_MLP;
+  if (warm && (!c->mlp.trained || !c->tab_ok[c->mlp.set] || c->tab[c->mlp.set].N != 10)) return MF_ENOTRAINED;
   MixedArgs m;
   std::memset(&m, 0, sizeof(m));
   for (int t = 0; t < a.n_ctypes; ++t) {
@@ -158,10 +164,47 @@ int dispatch_mixed(const mf_context* c, const FitArgs& a, const mf_options* o, c
   m.active_mask = a.active_mask;
   m.status = a.status;
   m.iters = a.iters;
-  cudaError_t e = launch_fit_mixed(m, o->block_size, s);
-  if (e != cudaSuccess) {
-    set_last_error("fit_mixed launch", e);
-    return MF_ECUDA;
+  if (!warm) {
+    cudaError_t e = launch_fit_mixed(m, o->block_size, s);
+    if (e != cudaSuccess) {
+      set_last_error("fit_mixed launch", e);
+      return MF_ECUDA;
+    }
+    return MF_OK;
+  }
+  // learned warm start: predict a chunk into the workspace, then fit it
+  MlpInferArgs ia;
+  fill_infer_args(c->mlp, c->tab[c->mlp.set], 0, &ia);
+  ia.sample_stride = a.sample_stride;
+  ia.warm_mask = c->mlp.warm_mask;
+  ia.warm_amp = c->mlp.warm_amp;
+  ia.warm_stride = 10;
+  for (int64_t off = 0; off < a.n; off += c->mlp.ws_cap) {
+    const int64_t cnt = a.n - off < c->mlp.ws_cap ? a.n - off : c->mlp.ws_cap;
+    ia.n = cnt;
+    ia.samples = a.samples + off * a.sample_stride;
+    ia.pederr = a.pederr + off;
+    ia.ctype = a.ctype ? a.ctype + off : nullptr;
+    MixedArgs mc = m;
+    mc.n = cnt;
+    mc.samples = ia.samples;
+    mc.pederr = ia.pederr;
+    mc.ctype = ia.ctype;
+    mc.amplitudes = a.amplitudes + off * a.amp_stride;
+    mc.chi2 = a.chi2 + off;
+    mc.intime = a.intime ? a.intime + off : nullptr;
+    mc.active_mask = a.active_mask ? a.active_mask + off : nullptr;
+    mc.status = a.status ? a.status + off : nullptr;
+    mc.iters = a.iters ? a.iters + off : nullptr;
+    mc.warm_mask = c->mlp.warm_mask;
+    mc.warm_amp = c->mlp.warm_amp;
+    mc.warm_stride = 10;
+    cudaError_t e = launch_mlp_infer(ia, c->sms, s);
+    if (e == cudaSuccess) e = launch_fit_mixed(mc, o->block_size, s);
+    if (e != cudaSuccess) {
+      set_last_error("warm fit launch", e);
+      return MF_ECUDA;
+    }
   }
   return MF_OK;
 }
@@ -334,6 +377,7 @@ int mf_create(mf_context** out, int device) {
   mf_context* c = new (std::nothrow) mf_context();
   if (!c) return MF_ENOMEM;
   c->device = device;
+  cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
   e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     set_last_error("cudaStreamCreate", e);
@@ -348,6 +392,7 @@ void mf_destroy(mf_context* c) {
   if (!c) return;
   free_staging(c);
   for (int t = 0; t < MF_MAX_CTYPES; ++t) free_tables(c, t);
+  mlp_free(c->mlp);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -430,6 +475,71 @@ int mf_fit_host(mf_context* c, const mf_batch* hb, const mf_options* o) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) {
     set_last_error("mf_fit_host", e);
+    return MF_ECUDA;
+  }
+  return MF_OK;
+}
+
+int mf_mlp_param_count(void) { return P_COUNT; }
+
+int mf_mlp_init(mf_context* c, int ctype, uint64_t seed, int64_t chunk) {
+  if (!c || ctype < 0 || ctype >= MF_MAX_CTYPES || chunk < 0) return MF_EINVAL;
+  std::lock_guard<std::mutex> g(c->mu);
+  return mlp_init(c->mlp, c->device, ctype, seed, chunk ? chunk : (int64_t(1) << 20));
+}
+
+int mf_mlp_train(mf_context* c, const mf_batch* d, const mf_mlp_train_params* p, float* epoch_loss, void* stream) {
+  if (!c || !d || !p || !d->samples || !d->pederr || !d->amplitudes || p->epochs < 0) return MF_EINVAL;
+  if (!c->mlp.ready) return MF_ENOTRAINED;
+  const int t = c->mlp.set;
+  if (!c->tab_ok[t] || c->tab[t].N != 10) return MF_EUNSUPPORTED;
+  std::lock_guard<std::mutex> g(c->mu);
+  return mlp_train(c->mlp, c->tab[t], d->n, d->sample_stride, d->samples, d->pederr, d->ctype, d->amplitudes,
+                   d->amp_stride, *p, epoch_loss, (cudaStream_t)stream);
+}
+
+int mf_mlp_gradient(mf_context* c, const mf_batch* d, const mf_mlp_train_params* p, float* grads,
+                    uint16_t* features_bf16, float* targets, float* loss) {
+  if (!c || !d || !p || !grads || !features_bf16 || !targets || !loss || !d->amplitudes) return MF_EINVAL;
+  if (!c->mlp.ready) return MF_ENOTRAINED;
+  const int t = c->mlp.set;
+  if (!c->tab_ok[t] || c->tab[t].N != 10) return MF_EUNSUPPORTED;
+  std::lock_guard<std::mutex> g(c->mu);
+  MlpGradProbe probe{grads, reinterpret_cast<__nv_bfloat16*>(features_bf16), targets, loss};
+  return mlp_train(c->mlp, c->tab[t], d->n, d->sample_stride, d->samples, d->pederr, d->ctype, d->amplitudes,
+                   d->amp_stride, *p, nullptr, c->stream, &probe);
+}
+
+int mf_mlp_get_weights(mf_context* c, float* host) {
+  if (!c || !host) return MF_EINVAL;
+  return mlp_get_weights(c->mlp, host);
+}
+
+int mf_mlp_set_weights(mf_context* c, const float* host) {
+  if (!c || !host) return MF_EINVAL;
+  std::lock_guard<std::mutex> g(c->mu);
+  return mlp_set_weights(c->mlp, host);
+}
+
+int mf_mlp_predict(mf_context* c, const mf_batch* b, uint16_t* mask, float* amp, float* logits, void* stream) {
+  if (!c || !b || !mask || !amp || b->n < 0 || (b->n > 0 && (!b->samples || !b->pederr))) return MF_EINVAL;
+  if (!c->mlp.ready) return MF_ENOTRAINED;
+  const int t = c->mlp.set;
+  if (!c->tab_ok[t] || c->tab[t].N != 10) return MF_EUNSUPPORTED;
+  MlpInferArgs ia;
+  fill_infer_args(c->mlp, c->tab[t], 0, &ia);
+  ia.n = b->n;
+  ia.sample_stride = b->sample_stride;
+  ia.samples = b->samples;
+  ia.pederr = b->pederr;
+  ia.ctype = b->ctype;
+  ia.warm_mask = mask;
+  ia.warm_amp = amp;
+  ia.warm_stride = 10;
+  ia.logits = logits;
+  cudaError_t e = launch_mlp_infer(ia, c->sms, (cudaStream_t)stream);
+  if (e != cudaSuccess) {
+    set_last_error("mlp_infer launch", e);
     return MF_ECUDA;
   }
   return MF_OK;

@@ -1,0 +1,443 @@
+// Learned warm start: a small MLP that predicts, from the whitened samples and
+// the noise scale, the passive set and the amplitudes of a channel's fit.
+//
+// Network: 16 inputs (10 normalised whitened samples, log SNR, pederr, zero
+// padding) -> 128 -> GELU -> 128 -> GELU -> 32 outputs (10 passive-set logits,
+// 10 amplitude outputs, padding). BF16 weights and activations on the tensor
+// cores (mma.sync m16n8k16, FP32 accumulate); FP32 master weights, Adam.
+//
+// Kernels:
+//   mlp_features_kernel   channel -> feature row (bf16) + per-channel scale
+//   gemm_kernel<EPI,..>   C = A * B^T for every training GEMM (forward layers,
+//                         input gradients, split-K weight gradients)
+//   loss_kernel           BCE on the logits + MSE on softplus(amplitude outputs)
+//   gelu_backward_kernel, bias_grad_kernel, adam_kernel, pack_weights_kernel
+//   mlp_infer_kernel      fused features->3 layers->warm-start outputs, the
+//                         weights and the activations of a 64-channel tile in
+//                         shared memory (the path inside a timed fit)
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <cstring>
+
+#include "mf_internal.h"
+#include "mlp.h"
+
+namespace mfgb {
+namespace {
+
+typedef __nv_bfloat16 bf16;
+
+constexpr int BM = 64, BN = 64, BK = 32, PAD = 8;
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__device__ __forceinline__ uint32_t ld32(const bf16* p) { return *reinterpret_cast<const uint32_t*>(p); }
+
+__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float x) {
+  const float cdf = 0.5f * (1.f + erff(x * 0.70710678118654752f));
+  const float pdf = 0.39894228040143268f * expf(-0.5f * x * x);
+  return cdf + x * pdf;
+}
+__device__ __forceinline__ float softplusf(float x) { return x > 20.f ? x : log1pf(expf(x)); }
+__device__ __forceinline__ float sigmoidf(float x) { return 1.f / (1.f + expf(-x)); }
+
+// Warp-level 32x32 tile product over one BK slice held in shared memory
+// (row-major [rows][BK+PAD], k contiguous), accumulating into acc[2][4][4].
+__device__ __forceinline__ void warp_tile_mma(const bf16 (*As)[BK + PAD], const bf16 (*Bs)[BK + PAD], int wm, int wn,
+                                              float (&acc)[2][4][4]) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll
+  for (int kk = 0; kk < BK; kk += 16) {
+    uint32_t a[2][4], b[4][2];
+#pragma unroll
+    for (int mi = 0; mi < 2; ++mi) {
+      const int r = wm + mi * 16 + g;
+      a[mi][0] = ld32(&As[r][kk + 2 * t]);
+      a[mi][1] = ld32(&As[r + 8][kk + 2 * t]);
+      a[mi][2] = ld32(&As[r][kk + 8 + 2 * t]);
+      a[mi][3] = ld32(&As[r + 8][kk + 8 + 2 * t]);
+    }
+#pragma unroll
+    for (int ni = 0; ni < 4; ++ni) {
+      const int c = wn + ni * 8 + g;
+      b[ni][0] = ld32(&Bs[c][kk + 2 * t]);
+      b[ni][1] = ld32(&Bs[c][kk + 8 + 2 * t]);
+    }
+#pragma unroll
+    for (int mi = 0; mi < 2; ++mi)
+#pragma unroll
+      for (int ni = 0; ni < 4; ++ni) mma_bf16(acc[mi][ni], a[mi], b[ni]);
+  }
+}
+
+// Loads a BM x BK (or BN x BK) tile of op(X) into shared memory. Element
+// (i, k) of op(X) is X[i*si + k*sk]; KC selects the coalescing direction
+// (k contiguous or i contiguous). Out-of-range elements are zero.
+template <bool KC, int ROWS>
+__device__ __forceinline__ void load_tile(bf16 (*S)[BK + PAD], const bf16* X, int64_t si, int64_t sk, int i0, int k0,
+                                          int I, int Kend) {
+  const int tid = threadIdx.x;
+#pragma unroll
+  for (int e = tid; e < ROWS * BK; e += 128) {
+    int i, k;
+    if (KC) {
+      i = e / BK;
+      k = e % BK;
+    } else {
+      k = e / ROWS;
+      i = e % ROWS;
+    }
+    const int gi = i0 + i, gk = k0 + k;
+    bf16 v = __float2bfloat16(0.f);
+    if (gi < I && gk < Kend) v = X[gi * si + gk * sk];
+    S[i][k] = v;
+  }
+}
+
+template <int EPI, bool AKC, bool BKC>
+__global__ void __launch_bounds__(128) gemm_kernel(const GemmArgs p) {
+  __shared__ __align__(16) bf16 As[BM][BK + PAD];
+  __shared__ __align__(16) bf16 Bs[BN][BK + PAD];
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  const int kbeg = blockIdx.z * p.k_split;
+  const int kend = min(p.K, kbeg + p.k_split);
+  const int warp = threadIdx.x >> 5;
+  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+  float acc[2][4][4] = {};
+  for (int k0 = kbeg; k0 < kend; k0 += BK) {
+    load_tile<AKC, BM>(As, p.A, p.a_si, p.a_sk, m0, k0, p.M, kend);
+    load_tile<BKC, BN>(Bs, p.B, p.b_sj, p.b_sk, n0, k0, p.N, kend);
+    __syncthreads();
+    warp_tile_mma(As, Bs, wm, wn, acc);
+    __syncthreads();
+  }
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll
+  for (int mi = 0; mi < 2; ++mi)
+#pragma unroll
+    for (int ni = 0; ni < 4; ++ni)
+#pragma unroll
+      for (int h = 0; h < 4; ++h) {
+        const int r = m0 + wm + mi * 16 + g + (h >= 2 ? 8 : 0);
+        const int c = n0 + wn + ni * 8 + 2 * t + (h & 1);
+        if (r >= p.M || c >= p.N) continue;
+        const float v = acc[mi][ni][h];
+        if (EPI == EPI_BIAS_GELU) {
+          const float z = v + p.bias[c];
+          p.C[int64_t(r) * p.ldc + c] = z;
+          p.H[int64_t(r) * p.ldh + c] = __float2bfloat16(gelu(z));
+        } else if (EPI == EPI_BIAS) {
+          p.C[int64_t(r) * p.ldc + c] = v + p.bias[c];
+        } else if (EPI == EPI_STORE) {
+          p.C[int64_t(r) * p.ldc + c] = v;
+        } else {  // EPI_ATOMIC: split-K accumulation of a weight gradient
+          atomicAdd(&p.C[int64_t(r) * p.ldc + c], v);
+        }
+      }
+}
+
+}  // namespace
+
+// --------------------------------------------------------------------------
+// element-wise kernels
+// --------------------------------------------------------------------------
+
+// Features of channel i: y = L_R^-1 s (FP64), f = [y/|y|, log(|y|/sigma)/10,
+// sigma, 0...]; scale[i] = |y| (the amplitude outputs are in units of
+// |y| / |G_k|). Channels of a set without tables (HCAL here) get f = 0.
+__global__ void mlp_features_kernel(const MlpFeatArgs a) {
+  const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= a.n) return;
+  float f[MLP_IN];
+  for (int j = 0; j < MLP_IN; ++j) f[j] = 0.f;
+  float scale = 0.f;
+  const int t = a.ctype ? int(a.ctype[i]) : 0;
+  if (t == a.set && a.N == 10) {
+    const double* s = a.samples + i * a.sample_stride;
+    double y[10], n2 = 0.;
+    int w = 0;
+    for (int r = 0; r < 10; ++r) {
+      double acc = 0.;
+      for (int c = 0; c <= r; ++c) acc = fma(a.W64[w + c], s[c], acc);
+      w += r + 1;
+      y[r] = acc;
+      n2 = fma(acc, acc, n2);
+    }
+    const double nrm = sqrt(n2);
+    const double sig = a.pederr[i];
+    const double inv = nrm > 0 ? 1.0 / nrm : 0.0;
+    for (int r = 0; r < 10; ++r) f[r] = float(y[r] * inv);
+    f[10] = float(log(fmax(nrm / sig, 1e-30)) * 0.1);
+    f[11] = float(sig);
+    scale = float(nrm);
+  }
+  bf16* out = a.X + i * MLP_IN;
+  for (int j = 0; j < MLP_IN; ++j) out[j] = __float2bfloat16(f[j]);
+  if (a.scale) a.scale[i] = scale;
+}
+
+// Targets from a converged fit: support bit and t_k = x_k |G_k| / |y|.
+__global__ void mlp_targets_kernel(int64_t n, const double* amp, int amp_stride, const float* scale,
+                                   const float* gnorm, float* T) {
+  const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= n) return;
+  const float sc = scale[i];
+  for (int k = 0; k < 10; ++k) {
+    const double x = amp[i * amp_stride + k];
+    T[i * 20 + k] = x > 0. ? 1.f : 0.f;
+    T[i * 20 + 10 + k] = sc > 0.f ? float(x * gnorm[k] / sc) : 0.f;
+  }
+}
+
+// Loss of a batch and its gradient dO (bf16, already divided by the batch).
+__global__ void mlp_loss_kernel(int B, const float* O, const float* T, float amp_weight, bf16* dO,
+                                float* loss_sum) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= B) return;
+  float l = 0.f;
+  const float invB = 1.f / float(B);
+  for (int k = 0; k < 10; ++k) {
+    const float z = O[i * MLP_OUT + k], y = T[i * 20 + k];
+    l += fmaxf(z, 0.f) - z * y + log1pf(expf(-fabsf(z)));
+    dO[i * MLP_OUT + k] = __float2bfloat16((sigmoidf(z) - y) * invB);
+    const float o = O[i * MLP_OUT + 10 + k], tt = T[i * 20 + 10 + k];
+    const float sp = softplusf(o), d = sp - tt;
+    l += amp_weight * d * d;
+    dO[i * MLP_OUT + 10 + k] = __float2bfloat16(2.f * amp_weight * d * sigmoidf(o) * invB);
+  }
+  for (int k = 20; k < MLP_OUT; ++k) dO[i * MLP_OUT + k] = __float2bfloat16(0.f);
+  if (loss_sum) atomicAdd(loss_sum, l * invB);
+}
+
+__global__ void gelu_backward_kernel(int64_t count, const float* dH, const float* Z, bf16* dZ) {
+  const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= count) return;
+  dZ[i] = __float2bfloat16(dH[i] * gelu_grad(Z[i]));
+}
+
+// db[c] += sum_b dZ[b][c] over a chunk of rows (float atomics).
+__global__ void bias_grad_kernel(int B, int C, const bf16* dZ, float* db) {
+  const int c = threadIdx.x;
+  if (c >= C) return;
+  const int rows = (B + gridDim.x - 1) / gridDim.x;
+  const int r0 = blockIdx.x * rows, r1 = min(B, r0 + rows);
+  float s = 0.f;
+  for (int r = r0; r < r1; ++r) s += __bfloat162float(dZ[int64_t(r) * C + c]);
+  atomicAdd(&db[c], s);
+}
+
+__global__ void adam_kernel(int count, float* w, const float* g, float* m, float* v, float lr, float b1, float b2,
+                            float eps, float c1, float c2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gi;
+  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+// FP32 master weights -> BF16 copies (row-major [out][in]) and their transposes.
+__global__ void pack_weights_kernel(const float* w, bf16* wh, bf16* wt, int out, int in) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= out * in) return;
+  const int o = i / in, c = i % in;
+  const bf16 v = __float2bfloat16(w[i]);
+  wh[i] = v;
+  if (wt) wt[c * out + o] = v;
+}
+
+// --------------------------------------------------------------------------
+// fused inference: one block = 64 channels; weights in shared memory
+// --------------------------------------------------------------------------
+constexpr int IT = 64;  // channels per tile
+struct InferSmem {
+  bf16 W1[MLP_H][MLP_IN + PAD];
+  bf16 W2[MLP_H][MLP_H + PAD];
+  bf16 W3[MLP_OUT][MLP_H + PAD];
+  float b1[MLP_H], b2[MLP_H], b3[MLP_OUT];
+  bf16 X[IT][MLP_IN + PAD];
+  bf16 H1[IT][MLP_H + PAD];
+  bf16 H2[IT][MLP_H + PAD];
+  float O[IT][MLP_OUT + 1];
+  float scale[IT];
+};
+
+// out[r][c] for r in [0,64), c in [0,NOUT): A (64 x KD) times W^T (NOUT x KD),
+// four warps each owning 16 rows.
+template <int KD, int NOUT, int LDA, int LDW>
+__device__ __forceinline__ void tile_layer(const bf16 (*A)[LDA], const bf16 (*W)[LDW], float (&acc)[NOUT / 8][4]) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const int r = (threadIdx.x >> 5) * 16 + g;
+#pragma unroll
+  for (int ni = 0; ni < NOUT / 8; ++ni)
+#pragma unroll
+    for (int h = 0; h < 4; ++h) acc[ni][h] = 0.f;
+#pragma unroll
+  for (int kk = 0; kk < KD; kk += 16) {
+    uint32_t a[4];
+    a[0] = ld32(&A[r][kk + 2 * t]);
+    a[1] = ld32(&A[r + 8][kk + 2 * t]);
+    a[2] = ld32(&A[r][kk + 8 + 2 * t]);
+    a[3] = ld32(&A[r + 8][kk + 8 + 2 * t]);
+#pragma unroll
+    for (int ni = 0; ni < NOUT / 8; ++ni) {
+      uint32_t b[2];
+      b[0] = ld32(&W[ni * 8 + g][kk + 2 * t]);
+      b[1] = ld32(&W[ni * 8 + g][kk + 8 + 2 * t]);
+      mma_bf16(acc[ni], a, b);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(128) mlp_infer_kernel(const MlpInferArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
+  const int tid = threadIdx.x;
+  for (int e = tid; e < MLP_H * MLP_IN; e += 128) S.W1[e / MLP_IN][e % MLP_IN] = a.W1[e];
+  for (int e = tid; e < MLP_H * MLP_H; e += 128) S.W2[e / MLP_H][e % MLP_H] = a.W2[e];
+  for (int e = tid; e < MLP_OUT * MLP_H; e += 128) S.W3[e / MLP_H][e % MLP_H] = a.W3[e];
+  for (int e = tid; e < MLP_H; e += 128) {
+    S.b1[e] = a.b1[e];
+    S.b2[e] = a.b2[e];
+  }
+  for (int e = tid; e < MLP_OUT; e += 128) S.b3[e] = a.b3[e];
+  const int lane = tid & 31, g = lane >> 2, t = lane & 3;
+  const int wr = (tid >> 5) * 16;
+  for (int64_t base = int64_t(blockIdx.x) * IT; base < a.n; base += int64_t(gridDim.x) * IT) {
+    __syncthreads();
+    // features: threads 0..63 one channel each
+    if (tid < IT) {
+      const int64_t i = base + tid;
+      float f[MLP_IN];
+      for (int j = 0; j < MLP_IN; ++j) f[j] = 0.f;
+      float scale = 0.f;
+      if (i < a.n && (a.ctype ? int(a.ctype[i]) : 0) == a.set) {
+        const double* s = a.samples + i * a.sample_stride;
+        double y[10], n2 = 0.;
+        int w = 0;
+#pragma unroll
+        for (int r = 0; r < 10; ++r) {
+          double acc = 0.;
+#pragma unroll
+          for (int c = 0; c <= r; ++c) acc = fma(a.W64[w + c], s[c], acc);
+          w += r + 1;
+          y[r] = acc;
+          n2 = fma(acc, acc, n2);
+        }
+        const double nrm = sqrt(n2);
+        const double sig = a.pederr[i];
+        const double inv = nrm > 0 ? 1.0 / nrm : 0.0;
+#pragma unroll
+        for (int r = 0; r < 10; ++r) f[r] = float(y[r] * inv);
+        f[10] = float(log(fmax(nrm / sig, 1e-30)) * 0.1);
+        f[11] = float(sig);
+        scale = float(nrm);
+      }
+#pragma unroll
+      for (int j = 0; j < MLP_IN; ++j) S.X[tid][j] = __float2bfloat16(f[j]);
+      S.scale[tid] = scale;
+    }
+    __syncthreads();
+    {
+      float acc[MLP_H / 8][4];
+      tile_layer<MLP_IN, MLP_H, MLP_IN + PAD, MLP_IN + PAD>(S.X, S.W1, acc);
+#pragma unroll
+      for (int ni = 0; ni < MLP_H / 8; ++ni)
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          const int r = wr + g + (h >= 2 ? 8 : 0), c = ni * 8 + 2 * t + (h & 1);
+          S.H1[r][c] = __float2bfloat16(gelu(acc[ni][h] + S.b1[c]));
+        }
+    }
+    __syncthreads();
+    {
+      float acc[MLP_H / 8][4];
+      tile_layer<MLP_H, MLP_H, MLP_H + PAD, MLP_H + PAD>(S.H1, S.W2, acc);
+#pragma unroll
+      for (int ni = 0; ni < MLP_H / 8; ++ni)
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          const int r = wr + g + (h >= 2 ? 8 : 0), c = ni * 8 + 2 * t + (h & 1);
+          S.H2[r][c] = __float2bfloat16(gelu(acc[ni][h] + S.b2[c]));
+        }
+    }
+    __syncthreads();
+    {
+      float acc[MLP_OUT / 8][4];
+      tile_layer<MLP_H, MLP_OUT, MLP_H + PAD, MLP_H + PAD>(S.H2, S.W3, acc);
+#pragma unroll
+      for (int ni = 0; ni < MLP_OUT / 8; ++ni)
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          const int r = wr + g + (h >= 2 ? 8 : 0), c = ni * 8 + 2 * t + (h & 1);
+          S.O[r][c] = acc[ni][h] + S.b3[c];
+        }
+    }
+    __syncthreads();
+    if (tid < IT) {
+      const int64_t i = base + tid;
+      if (i < a.n) {
+        uint16_t m = 0;
+        const float sc = S.scale[tid];
+        float* wa = a.warm_amp + i * a.warm_stride;
+#pragma unroll
+        for (int k = 0; k < 10; ++k) {
+          if (S.O[tid][k] > 0.f && sc > 0.f) m |= uint16_t(1u << k);
+          wa[k] = softplusf(S.O[tid][10 + k]) * sc * a.inv_gnorm[k];
+        }
+        a.warm_mask[i] = m;
+        if (a.logits) {
+          for (int k = 0; k < MLP_OUT; ++k) a.logits[i * MLP_OUT + k] = S.O[tid][k];
+        }
+      }
+    }
+  }
+}
+
+// --------------------------------------------------------------------------
+// launchers
+// --------------------------------------------------------------------------
+cudaError_t launch_gemm(int epi, bool akc, bool bkc, const GemmArgs& p, int splits, cudaStream_t s) {
+  dim3 grid((p.N + BN - 1) / BN, (p.M + BM - 1) / BM, splits);
+#define MF_GEMM_CASE(E, A, B)                                          \
+  if (epi == E && akc == A && bkc == B) {                              \
+    gemm_kernel<E, A, B><<<grid, 128, 0, s>>>(p);                      \
+    return cudaGetLastError();                                         \
+  }
+  MF_GEMM_CASE(EPI_BIAS_GELU, true, true)
+  MF_GEMM_CASE(EPI_BIAS, true, true)
+  MF_GEMM_CASE(EPI_STORE, true, true)
+  MF_GEMM_CASE(EPI_ATOMIC, false, false)
+#undef MF_GEMM_CASE
+  return cudaErrorInvalidValue;
+}
+
+size_t infer_smem_bytes() { return sizeof(InferSmem); }
+
+cudaError_t launch_mlp_infer(const MlpInferArgs& a, int sms, cudaStream_t s) {
+  if (a.n == 0) return cudaSuccess;
+  static bool attr_set = false;
+  const size_t smem = sizeof(InferSmem);
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(mlp_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  const int64_t tiles = (a.n + IT - 1) / IT;
+  const int64_t cap = int64_t(sms) * 2;
+  const int grid = int(tiles < cap ? tiles : cap);
+  mlp_infer_kernel<<<grid, 128, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace mfgb

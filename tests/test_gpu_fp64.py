@@ -163,8 +163,10 @@ def test_bad_condition_index(mf, cuda):
     n = 4
     s = np.zeros((n, 10))
     ct = np.array([0, 1, 0, 7], dtype=np.uint8)
-    with pytest.raises(mf.MultifitError):  # set 1 was never given
-        eng.fit_host(s, np.full(n, 0.044), ctype=ct)
+    # the host cannot see device-side indices: a channel naming a set that was
+    # never given is flagged per channel
+    out = eng.fit_host(s, np.full(n, 0.044), ctype=ct)
+    assert list(out["status"]) == [0, mf.CH_BADINPUT, 0, mf.CH_BADINPUT]
     mixed_engine(mf, eng)
     out = eng.fit_host(s, np.full(n, 0.044), ctype=ct)
     assert out["status"][3] == mf.CH_BADINPUT
@@ -190,4 +192,5 @@ def test_pulsechisq_mirror_matches_oracle(mf, oracle, cuda):
         assert f.DoFit(data["samples"][c], R, data["pederr"][c], bxs, fullpulse, np.zeros((19, 19)))
         assert np.array_equal(f.X(), ref["amplitudes"][c])
         assert f.ChiSq() == ref["chi2"][c]
-        assert f.Errors()[5] == ref["errors"][c]
+        e, r = f.Errors()[5], ref["errors"][c]
+        assert e == r or (np.isnan(e) and np.isnan(r))  # the reference start can leave NaN errors

@@ -1,0 +1,109 @@
+"""Learned warm start on the GPU: the hand-written MLP kernels against the
+CPU FP64 checker (oracle/mlp_oracle.py), training, and the warm fit against
+the FP64 oracle.
+
+Tolerances: gradients of the BF16/FP32 kernels vs the FP64 checker with the
+same BF16 rounding points -- normwise relative error <= 2e-2 per parameter
+tensor (FP32 accumulation order and rare BF16 tie flips), cosine >= 0.999;
+against the exact FP64 gradient, cosine >= 0.99. The warm fit obeys the
+mixed form's bounds (<= 1e-4 normwise relative amplitude error and identical
+active sets on >= 99.9 % of channels vs the FP64 oracle at KKT convergence).
+"""
+import numpy as np
+import pytest
+
+from _helpers import DeviceBatch, oracle_fit_sets
+from oracle import mlp_oracle as mo
+
+pytestmark = pytest.mark.gpu
+
+
+def train_set(mf, cuda, eng, n, seed):
+    """Channels of the log-uniform pileup-4 generator plus their converged FP64 fits (the targets)."""
+    db = DeviceBatch(mf, cuda, n)
+    db.generate(mf, mf.synth_params(seed, n, intime_log=True, lo=0.1, hi=1000.0, pileup_mean=4.0))
+    eng.fit_device(db.batch, mf.default_options(max_iter_nnls=1000, nnls_start=mf.START_SUPPORT))
+    cuda.cuda.synchronize()
+    return db
+
+
+@pytest.fixture(scope="module")
+def mlp_engine(mf, cuda):
+    eng = mf.Engine(0)
+    eng.set_conditions(0, mf.synth_conditions(mf.SYNTH_ECAL)[0])
+    eng.mlp_init(0, seed=7)
+    yield eng
+    eng.close()
+
+
+def test_gradients_match_cpu_fp64(mf, cuda, mlp_engine):
+    eng = mlp_engine
+    B = 4096
+    db = train_set(mf, cuda, eng, B, seed=31)
+    p = mf.mlp_params(epochs=1, batch=B, amp_weight=1.0)
+    g, X, T, loss = eng.mlp_gradient(db.batch, p)
+    params = mo.unflatten(eng.mlp_get_weights())
+    X = X.astype(np.float64)
+    T = T.astype(np.float64)
+    # features: 10 unit-normalised whitened samples, log SNR, pederr
+    assert np.allclose(np.linalg.norm(X[:, :10], axis=1), 1.0, atol=2e-2)
+    assert (X[:, 12:] == 0).all()
+    lq, gq = mo.loss_and_grad(params, X, T, 1.0, quantized=True)
+    le, ge = mo.loss_and_grad(params, X, T, 1.0, quantized=False)
+    assert abs(loss - lq) <= 1e-4 * abs(lq)
+    gg = mo.unflatten(g)
+    for name, _ in mo.LAYOUT:
+        a, r, ex = gg[name].ravel(), gq[name].ravel(), ge[name].ravel()
+        if name in ("W3", "b3"):
+            a, r, ex = gg[name][:20].ravel(), gq[name][:20].ravel(), ge[name][:20].ravel()
+            assert (gg[name][20:] == 0).all()
+        rel = np.linalg.norm(a - r) / np.linalg.norm(r)
+        cos = a @ r / (np.linalg.norm(a) * np.linalg.norm(r))
+        cos_exact = a @ ex / (np.linalg.norm(a) * np.linalg.norm(ex))
+        assert rel <= 2e-2, (name, rel)
+        assert cos >= 0.999, (name, cos)
+        assert cos_exact >= 0.99, (name, cos_exact)
+
+
+def test_training_reduces_loss_and_warm_fit_parity(mf, oracle, cuda, mlp_engine):
+    eng = mlp_engine
+    n = 262_144
+    db = train_set(mf, cuda, eng, n, seed=5)
+    losses = eng.mlp_train(db.batch, mf.mlp_params(epochs=4, batch=4096, lr=2e-3))
+    assert np.isfinite(losses).all()
+    assert losses[-1] < 0.6 * losses[0], losses
+    # fresh evaluation channels (seed 6)
+    m = 20_000
+    ev = DeviceBatch(mf, cuda, m)
+    ev.generate(mf, mf.synth_params(6, m, intime_log=True, lo=0.1, hi=1000.0, pileup_mean=4.0))
+    eng.fit_device(ev.batch, mf.default_options(precision=mf.PREC_MIXED, warm_start=mf.WARM_MLP, max_iter_nnls=1000))
+    warm = ev.outputs_host()
+    eng.fit_device(ev.batch, mf.default_options(precision=mf.PREC_MIXED, max_iter_nnls=1000))
+    cold = ev.outputs_host()
+    ref = oracle_fit_sets(mf, oracle, eng, ev.inputs_host(), max_iter_nnls=1000, start=1)
+    scale = np.maximum(np.abs(ref["amplitudes"]).max(axis=1), 1e-300)
+    err = np.abs(warm["amplitudes"] - ref["amplitudes"]).max(axis=1) / scale
+    assert (err <= 1e-4).mean() >= 0.999
+    assert (warm["active_mask"] == ref["active_mask"]).mean() >= 0.999
+    assert (warm["status"] == 0).all()
+    # what the trained network gains: fewer FNNLS additions and solves than the cold start
+    _, adds_w, solves_w = mf.unpack_iters(warm["iters"])
+    _, adds_c, solves_c = mf.unpack_iters(cold["iters"])
+    assert adds_w.mean() < 0.5 * adds_c.mean(), (adds_w.mean(), adds_c.mean())
+    # predicted passive sets: exact on a majority of channels
+    mask = cuda.zeros(m, dtype=cuda.int16, device="cuda")
+    amp = cuda.zeros((m, 10), dtype=cuda.float32, device="cuda")
+    eng.mlp_predict(ev.batch, mask.data_ptr(), amp.data_ptr())
+    pred = mask.cpu().numpy().view(np.uint16)
+    assert (pred == ref["active_mask"]).mean() > 0.5
+
+
+def test_weights_roundtrip(mf, cuda, mlp_engine, tmp_path):
+    eng = mlp_engine
+    w = eng.mlp_get_weights()
+    path = tmp_path / "mlp.bin"
+    mf.save_mlp_weights(str(path), w, {"trained_on": "test"})
+    w2, hdr = mf.load_mlp_weights(str(path))
+    assert np.array_equal(w, w2) and hdr["trained_on"] == "test"
+    eng.mlp_set_weights(w2)
+    assert np.array_equal(eng.mlp_get_weights(), w)
