@@ -166,8 +166,9 @@ int mf_fit(mf_context* ctx, const mf_batch* batch, const mf_options* opt, void* 
 
 /* Same fit as mf_fit, additionally writing the executed floating-point
  * operation count of every channel to flops[n] (device pointer; an FMA counts
- * 2, add/sub/mul/div/sqrt 1). An instrumented, slower build of the kernel:
- * it measures a workload's algorithmic work and is never the timed path. */
+ * 2, add/sub/mul/div/sqrt 1): every FP64 and no other operation for the plain
+ * FP64 precision (an instrumented, slower build, never the timed path), the
+ * FP64 operations (the bound of that kernel) for the mixed precision. */
 int mf_fit_count_flops(mf_context* ctx, const mf_batch* batch, const mf_options* opt, double* flops, void* stream);
 
 /* Same fit with HOST buffers: copies inputs to the context's device staging
@@ -198,9 +199,8 @@ typedef struct mf_mlp_train_params {
 } mf_mlp_train_params;
 
 int mf_mlp_param_count(void);
-/* Allocates the network (He-normal init from `seed`) for condition set `ctype`,
- * plus an inference workspace of `chunk` channels (0 = 1,048,576). */
-int mf_mlp_init(mf_context* ctx, int ctype, uint64_t seed, int64_t chunk);
+/* Allocates the network (He-normal init from `seed`) for condition set `ctype`. */
+int mf_mlp_init(mf_context* ctx, int ctype, uint64_t seed);
 /* Trains on device data: batch.samples/pederr/ctype are the inputs and
  * batch.amplitudes holds their converged fits (the targets). Writes the mean
  * loss of each epoch to epoch_loss (host, may be NULL). Synchronous. */

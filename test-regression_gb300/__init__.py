@@ -118,7 +118,7 @@ SIGNATURES = [
     ("mf_build_pulse_matrix", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
     ("mf_table_operator", C.c_int, [C.POINTER(MfConditions), C.c_uint32, C.c_void_p, C.c_void_p]),
     ("mf_mlp_param_count", C.c_int, []),
-    ("mf_mlp_init", C.c_int, [C.c_void_p, C.c_int, C.c_uint64, C.c_int64]),
+    ("mf_mlp_init", C.c_int, [C.c_void_p, C.c_int, C.c_uint64]),
     ("mf_mlp_train", C.c_int, [C.c_void_p, C.POINTER(MfBatch), C.POINTER(MfMlpTrainParams), C.c_void_p, C.c_void_p]),
     ("mf_mlp_gradient", C.c_int, [C.c_void_p, C.POINTER(MfBatch), C.POINTER(MfMlpTrainParams), C.c_void_p,
                                   C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -376,8 +376,8 @@ def mlp_unflatten(flat: np.ndarray) -> dict:
 
 
 def _mlp_engine_methods():
-    def mlp_init(self, ctype=0, seed=1, chunk=0):
-        _check(self.lib.mf_mlp_init(self.h, ctype, seed, chunk), "mf_mlp_init")
+    def mlp_init(self, ctype=0, seed=1):
+        _check(self.lib.mf_mlp_init(self.h, ctype, seed), "mf_mlp_init")
 
     def mlp_train(self, batch: MfBatch, params: MfMlpTrainParams, stream=None):
         losses = np.zeros(max(params.epochs, 1), dtype=np.float32)

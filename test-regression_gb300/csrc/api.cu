@@ -164,6 +164,7 @@ int dispatch_mixed(const mf_context* c, const FitArgs& a, const mf_options* o, c
   m.active_mask = a.active_mask;
   m.status = a.status;
   m.iters = a.iters;
+  m.flops = a.flops;
   if (!warm) {
     cudaError_t e = launch_fit_mixed(m, o->block_size, s);
     if (e != cudaSuccess) {
@@ -172,45 +173,28 @@ int dispatch_mixed(const mf_context* c, const FitArgs& a, const mf_options* o, c
     }
     return MF_OK;
   }
-  // learned warm start: predict a chunk into the workspace, then fit it
-  MlpInferArgs ia;
-  fill_infer_args(c->mlp, c->tab[c->mlp.set], 0, &ia);
-  ia.sample_stride = a.sample_stride;
-  ia.warm_mask = c->mlp.warm_mask;
-  ia.warm_amp = c->mlp.warm_amp;
-  ia.warm_stride = 10;
-  for (int64_t off = 0; off < a.n; off += c->mlp.ws_cap) {
-    const int64_t cnt = a.n - off < c->mlp.ws_cap ? a.n - off : c->mlp.ws_cap;
-    ia.n = cnt;
-    ia.samples = a.samples + off * a.sample_stride;
-    ia.pederr = a.pederr + off;
-    ia.ctype = a.ctype ? a.ctype + off : nullptr;
-    MixedArgs mc = m;
-    mc.n = cnt;
-    mc.samples = ia.samples;
-    mc.pederr = ia.pederr;
-    mc.ctype = ia.ctype;
-    mc.amplitudes = a.amplitudes + off * a.amp_stride;
-    mc.chi2 = a.chi2 + off;
-    mc.intime = a.intime ? a.intime + off : nullptr;
-    mc.active_mask = a.active_mask ? a.active_mask + off : nullptr;
-    mc.status = a.status ? a.status + off : nullptr;
-    mc.iters = a.iters ? a.iters + off : nullptr;
-    mc.warm_mask = c->mlp.warm_mask;
-    mc.warm_amp = c->mlp.warm_amp;
-    mc.warm_stride = 10;
-    cudaError_t e = launch_mlp_infer(ia, c->sms, s);
-    if (e == cudaSuccess) e = launch_fit_mixed(mc, o->block_size, s);
-    if (e != cudaSuccess) {
-      set_last_error("warm fit launch", e);
-      return MF_ECUDA;
-    }
+  // learned warm start: one fused launch (whitening -> MLP -> warm fit)
+  FusedMlp w;
+  std::memset(&w, 0, sizeof(w));
+  w.W1 = c->mlp.W1h;
+  w.W2 = c->mlp.W2h;
+  w.W3 = c->mlp.W3h;
+  w.b1 = c->mlp.params + P_B1;
+  w.b2 = c->mlp.params + P_B2;
+  w.b3 = c->mlp.params + P_B3;
+  w.set = c->mlp.set;
+  const HostTables& ht = c->tab[c->mlp.set];
+  for (int k = 0; k < KMAX; ++k) w.inv_gnorm[k] = ht.gnorm2[k] > 0 ? float(1.0 / std::sqrt(ht.gnorm2[k])) : 0.f;
+  cudaError_t e = launch_fit_warm_fused(m, w, c->sms, s);
+  if (e != cudaSuccess) {
+    set_last_error("fit_warm_fused launch", e);
+    return MF_ECUDA;
   }
   return MF_OK;
 }
 
 int dispatch(const mf_context* c, const FitArgs& a, const mf_options* o, cudaStream_t s, bool instrumented) {
-  if (o->precision == MF_PREC_MIXED && !instrumented) return dispatch_mixed(c, a, o, s);
+  if (o->precision == MF_PREC_MIXED) return dispatch_mixed(c, a, o, s);
   if (o->precision != MF_PREC_FP64 || o->schedule != MF_SCHED_GRID || o->warm_start != MF_WARM_NONE)
     return MF_EUNSUPPORTED;
   cudaError_t e = launch_fit_fp64(a, o->block_size, s, instrumented);
@@ -482,10 +466,10 @@ int mf_fit_host(mf_context* c, const mf_batch* hb, const mf_options* o) {
 
 int mf_mlp_param_count(void) { return P_COUNT; }
 
-int mf_mlp_init(mf_context* c, int ctype, uint64_t seed, int64_t chunk) {
-  if (!c || ctype < 0 || ctype >= MF_MAX_CTYPES || chunk < 0) return MF_EINVAL;
+int mf_mlp_init(mf_context* c, int ctype, uint64_t seed) {
+  if (!c || ctype < 0 || ctype >= MF_MAX_CTYPES) return MF_EINVAL;
   std::lock_guard<std::mutex> g(c->mu);
-  return mlp_init(c->mlp, c->device, ctype, seed, chunk ? chunk : (int64_t(1) << 20));
+  return mlp_init(c->mlp, c->device, ctype, seed);
 }
 
 int mf_mlp_train(mf_context* c, const mf_batch* d, const mf_mlp_train_params* p, float* epoch_loss, void* stream) {

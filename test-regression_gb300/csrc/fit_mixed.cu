@@ -20,6 +20,8 @@
 #include <cfloat>
 
 #include "mf_internal.h"
+#include "mlp.h"
+#include "mlp_common.cuh"
 
 namespace mfgb {
 namespace {
@@ -109,43 +111,60 @@ __device__ __forceinline__ int inner_loop(unsigned& m, F* x, Solve solve) {
   return solves;
 }
 
-template <int N, int K, bool WARM>
-__device__ void fit_channel(const MixedArgs& a, const DevMixed& T, int64_t ch) {
+// Loads a channel and whitens it with the shared inverse factor: y = L_R^-1 s
+// in FP64 (packed rows, 55 FMA for N = 10, no division). Returns true for a
+// non-finite or non-positive input.
+template <int N>
+__device__ __forceinline__ bool whiten(const MixedArgs& a, const DevMixed& T, int64_t ch, double* y, double& sig) {
   const double* in = a.samples + ch * a.sample_stride;
-  const double sig = a.pederr[ch];
-  double s[N];
+  sig = a.pederr[ch];
   bool bad = !isfinite(sig) || !(sig > 0.);
+  double s[N];
 #pragma unroll
   for (int i = 0; i < N; ++i) {
     s[i] = in[i];
     bad = bad || !isfinite(s[i]);
   }
-  // 1. whitening with the shared inverse factor
-  double y[N];
+  int w = 0;
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    double acc = 0.;
+#pragma unroll
+    for (int j = 0; j <= i; ++j) acc = fma(T.W64[w + j], s[j], acc);
+    w += i + 1;
+    y[i] = acc;
+  }
+  return bad;
+}
+
+// The fit of one whitened channel (steps 2-4), optionally from a predicted
+// passive set warm_m with amplitudes warm_x.
+template <int N, int K>
+__device__ void fit_from_y(const MixedArgs& a, const DevMixed& T, int64_t ch, const double* y, double sig, bool bad,
+                           bool warm, unsigned warm_m, const float* warm_x) {
+  // executed FP64 flops (FMA = 2): whitening, FP64 solves, residuals, FP64
+  // gradients and chi2 -- the work on the FP64 pipe, the bound of this kernel
+  int f64 = N * (N + 1);
   float y32[N];
   float ynorm2 = 0.f;
-  {
-    int w = 0;
 #pragma unroll
-    for (int i = 0; i < N; ++i) {
-      double acc = 0.;
-#pragma unroll
-      for (int j = 0; j <= i; ++j) acc = fma(T.W64[w + j], s[j], acc);
-      w += i + 1;
-      y[i] = acc;
-      y32[i] = float(acc);
-      ynorm2 = fmaf(y32[i], y32[i], ynorm2);
-    }
+  for (int i = 0; i < N; ++i) {
+    y32[i] = float(y[i]);
+    ynorm2 = fmaf(y32[i], y32[i], ynorm2);
   }
   // 2. FP32 active-set search
-  float c32[K];
+  float c32[K], cmag[K];  // c = G^T y and sum |G_ik y_i| (its FP32 error scale)
 #pragma unroll
   for (int k = 0; k < K; ++k) {
-    float acc = 0.f;
+    float acc = 0.f, mag = 0.f;
 #pragma unroll
     for (int i = 0; i < N; ++i)
-      if (i >= T.gfz[k]) acc = fmaf(T.G32[k * N + i], y32[i], acc);
+      if (i >= T.gfz[k]) {
+        acc = fmaf(T.G32[k * N + i], y32[i], acc);
+        mag = fmaf(fabsf(T.G32[k * N + i]), fabsf(y32[i]), mag);
+      }
     c32[k] = acc;
+    cmag[k] = mag;
   }
   const float ynorm = sqrtf(ynorm2);
   const unsigned full = (1u << K) - 1u;
@@ -155,12 +174,11 @@ __device__ void fit_channel(const MixedArgs& a, const DevMixed& T, int64_t ch) {
   for (int k = 0; k < K; ++k) x32[k] = 0.f;
   int adds = 0, solves = 0;
   auto s32 = [&](unsigned mm, float* out) { solve32<N, K>(T, mm, y32, out); };
-  if (WARM) {
-    m = unsigned(a.warm_mask[ch]) & full;
-    const float* wa = a.warm_amp + ch * a.warm_stride;
+  if (warm) {
+    m = warm_m & full;
 #pragma unroll
     for (int k = 0; k < K; ++k)
-      if (m & (1u << k)) x32[k] = fmaxf(wa[k], 1e-30f);
+      if (m & (1u << k)) x32[k] = fmaxf(warm_x[k], 1e-30f);
     if (m) solves += inner_loop<K>(m, x32, s32);
   }
   for (int it = 0; it < a.max_iter32; ++it) {
@@ -184,36 +202,73 @@ __device__ void fit_channel(const MixedArgs& a, const DevMixed& T, int64_t ch) {
     ++adds;
     solves += inner_loop<K>(m, x32, s32);
   }
-  // 3. FP64 judge: continue the same loop in FP64 from the FP32 passive set
+  // 3. FP64 judge: the FP64 solve on the FP32 passive set, then the KKT test
+  //    in FP64 where FP32 cannot decide; a failed test continues the loop in FP64.
   double x[K];
+  auto s64 = [&](unsigned mm, double* out) {
+    solve64<N, K>(T, mm, y, out);
+    f64 += 2 * N * __popc(mm);
+  };
+  {
+    double sv[K];
+    bool allpos = true;
+    if (m) {
+      s64(m, sv);
+      ++solves;
 #pragma unroll
-  for (int k = 0; k < K; ++k) x[k] = double(x32[k]);
-  auto s64 = [&](unsigned mm, double* out) { solve64<N, K>(T, mm, y, out); };
-  if (m) solves += inner_loop<K>(m, x, s64);
-  double c64[K];
+      for (int k = 0; k < K; ++k)
+        if ((m & (1u << k)) && !(sv[k] > 0.)) allpos = false;
+    }
 #pragma unroll
-  for (int k = 0; k < K; ++k) {
-    double acc = 0.;
+    for (int k = 0; k < K; ++k) x[k] = (m & (1u << k)) ? sv[k] : 0.;
+    if (!allpos) {  // rare: step back from the feasible FP32 point in FP64
 #pragma unroll
-    for (int i = 0; i < N; ++i)
-      if (i >= T.gfz[k]) acc = fma(T.G64[k * N + i], y[i], acc);
-    c64[k] = acc;
+      for (int k = 0; k < K; ++k) x[k] = double(x32[k]);
+      solves += inner_loop<K>(m, x, s64);
+    }
   }
   const double tol64 = a.eps * sig * sig;
   bool converged = false;
   int adds64 = 0;
-  for (int it = 0; it < a.max_iter64; ++it) {
+  double r[N];
+  for (int it = 0;; ++it) {
+    // FP64 residual r = y - G_S x over the passive columns
+#pragma unroll
+    for (int i = 0; i < N; ++i) r[i] = y[i];
+    for (unsigned mm = m; mm; mm &= mm - 1) {
+      const int k = __ffs(mm) - 1;
+      const double xk = x[k];
+      f64 += 2 * (N - T.gfz[k]);
+#pragma unroll
+      for (int i = 0; i < N; ++i)
+        if (i >= T.gfz[k]) r[i] = fma(-T.G64[k * N + i], xk, r[i]);
+    }
+    if (it >= a.max_iter64) break;
+    // gradient w_k = G_k^T r: screened in FP32 (c - H x), exact in FP64 only
+    // where the FP32 value is within its error bound of the threshold
+    float xf[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) xf[k] = float(x[k]);
     double wmax = 0.;
     int imax = -1;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
       if (m & (1u << k)) continue;
-      double acc = c64[k];
+      float acc = c32[k], mag = cmag[k];
 #pragma unroll
-      for (int j = 0; j < K; ++j)
-        if (m & (1u << j)) acc = fma(-T.H64[k * KMAX + j], x[j], acc);
-      if (imax < 0 || acc > wmax) {
-        wmax = acc;
+      for (int j = 0; j < K; ++j) {
+        const float hx = T.H32[k * KMAX + j] * xf[j];
+        acc -= hx;
+        mag += fabsf(hx);
+      }
+      if (acc < -4e-6f * mag) continue;  // certainly below the threshold
+      double w = 0.;
+      f64 += 2 * (N - T.gfz[k]);
+#pragma unroll
+      for (int i = 0; i < N; ++i)
+        if (i >= T.gfz[k]) w = fma(T.G64[k * N + i], r[i], w);
+      if (imax < 0 || w > wmax) {
+        wmax = w;
         imax = k;
       }
     }
@@ -225,17 +280,13 @@ __device__ void fit_channel(const MixedArgs& a, const DevMixed& T, int64_t ch) {
     ++adds64;
     solves += inner_loop<K>(m, x, s64);
   }
-  // 4. chi2 in FP64
+  // 4. chi2 in FP64 from the residual
   double chi2 = 0.;
 #pragma unroll
-  for (int i = 0; i < N; ++i) {
-    double acc = y[i];
-#pragma unroll
-    for (int k = 0; k < K; ++k)
-      if (i >= T.gfz[k]) acc = fma(-T.G64[k * N + i], x[k], acc);
-    chi2 = fma(acc, acc, chi2);
-  }
+  for (int i = 0; i < N; ++i) chi2 = fma(r[i], r[i], chi2);
   chi2 = chi2 / (sig * sig);
+  f64 += 2 * N + 2;
+  if (a.flops) a.flops[ch] = double(f64);
 
   double* out = a.amplitudes + ch * a.amp_stride;
   bool finite = isfinite(chi2);
@@ -264,6 +315,21 @@ __device__ void fit_channel(const MixedArgs& a, const DevMixed& T, int64_t ch) {
   }
 }
 
+template <int N, int K, bool WARM>
+__device__ __forceinline__ void fit_channel(const MixedArgs& a, const DevMixed& T, int64_t ch) {
+  double y[N], sig;
+  const bool bad = whiten<N>(a, T, ch, y, sig);
+  unsigned m = 0;
+  float xw[K];
+  if (WARM) {
+    m = a.warm_mask[ch];
+    const float* wa = a.warm_amp + ch * a.warm_stride;
+#pragma unroll
+    for (int k = 0; k < K; ++k) xw[k] = wa[k];
+  }
+  fit_from_y<N, K>(a, T, ch, y, sig, bad, WARM, m, xw);
+}
+
 template <bool WARM>
 __global__ void __launch_bounds__(128) fit_mixed_kernel(const MixedArgs a) {
   const int64_t ch = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
@@ -280,7 +346,169 @@ __global__ void __launch_bounds__(128) fit_mixed_kernel(const MixedArgs a) {
   else if (a.status) a.status[ch] = CH_BADINPUT;  // shapes without a mixed build (rejected on the host)
 }
 
+// --------------------------------------------------------------------------
+// Fused learned warm start: whitening -> MLP on the tensor cores -> warm fit
+// --------------------------------------------------------------------------
+struct FusedSmem {
+  __nv_bfloat16 W1[MLP_H][MLP_IN + 8];
+  __nv_bfloat16 W2[MLP_H][MLP_H + 8];
+  __nv_bfloat16 W3[MLP_OUT][MLP_H + 8];
+  float b1[MLP_H], b2[MLP_H], b3[MLP_OUT];
+  __nv_bfloat16 X[128][MLP_IN + 8];
+  float O[128][MLP_OUT + 1];
+};
+
+// Two adjacent n8 accumulator tiles (columns c0.. and c0+8..) after bias and
+// GELU, packed as the BF16 A fragment of the next layer's k16 slice.
+__device__ __forceinline__ void gelu_pack(const float (&c0)[4], const float (&c1)[4], const float* bias, int col0,
+                                          uint32_t (&h)[4]) {
+  h[0] = pack_bf16(gelu(c0[0] + bias[col0]), gelu(c0[1] + bias[col0 + 1]));
+  h[1] = pack_bf16(gelu(c0[2] + bias[col0]), gelu(c0[3] + bias[col0 + 1]));
+  h[2] = pack_bf16(gelu(c1[0] + bias[col0 + 8]), gelu(c1[1] + bias[col0 + 9]));
+  h[3] = pack_bf16(gelu(c1[2] + bias[col0 + 8]), gelu(c1[3] + bias[col0 + 9]));
+}
+
+// The MLP of the warp's 32 channels (rows 32*warp.. of S.X) into S.O. The
+// hidden activations stay in registers: the m16n8 accumulators of one layer,
+// two n8 tiles at a time, are exactly the m16n8k16 A fragments of the next.
+__device__ __forceinline__ void warp_mlp(FusedSmem& S, int warp) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll 1
+  for (int mt = 0; mt < 2; ++mt) {
+    const int r = warp * 32 + mt * 16 + g;
+    uint32_t a0[4];
+    a0[0] = ld32(&S.X[r][2 * t]);
+    a0[1] = ld32(&S.X[r + 8][2 * t]);
+    a0[2] = ld32(&S.X[r][8 + 2 * t]);
+    a0[3] = ld32(&S.X[r + 8][8 + 2 * t]);
+    uint32_t h1[8][4];
+#pragma unroll
+    for (int kt = 0; kt < 8; ++kt) {
+      float c0[4] = {0.f, 0.f, 0.f, 0.f}, c1[4] = {0.f, 0.f, 0.f, 0.f};
+      const uint32_t b0[2] = {ld32(&S.W1[16 * kt + g][2 * t]), ld32(&S.W1[16 * kt + g][8 + 2 * t])};
+      const uint32_t b1[2] = {ld32(&S.W1[16 * kt + 8 + g][2 * t]), ld32(&S.W1[16 * kt + 8 + g][8 + 2 * t])};
+      mma_bf16(c0, a0, b0);
+      mma_bf16(c1, a0, b1);
+      gelu_pack(c0, c1, S.b1, 16 * kt + 2 * t, h1[kt]);
+    }
+    uint32_t h2[8][4];
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+      float c0[4] = {0.f, 0.f, 0.f, 0.f}, c1[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int kt = 0; kt < 8; ++kt) {
+        const uint32_t b0[2] = {ld32(&S.W2[16 * nt + g][16 * kt + 2 * t]),
+                                ld32(&S.W2[16 * nt + g][16 * kt + 8 + 2 * t])};
+        const uint32_t b1[2] = {ld32(&S.W2[16 * nt + 8 + g][16 * kt + 2 * t]),
+                                ld32(&S.W2[16 * nt + 8 + g][16 * kt + 8 + 2 * t])};
+        mma_bf16(c0, h1[kt], b0);
+        mma_bf16(c1, h1[kt], b1);
+      }
+      gelu_pack(c0, c1, S.b2, 16 * nt + 2 * t, h2[nt]);
+    }
+#pragma unroll
+    for (int nt = 0; nt < 2; ++nt) {
+      float c0[4] = {0.f, 0.f, 0.f, 0.f}, c1[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int kt = 0; kt < 8; ++kt) {
+        const uint32_t b0[2] = {ld32(&S.W3[16 * nt + g][16 * kt + 2 * t]),
+                                ld32(&S.W3[16 * nt + g][16 * kt + 8 + 2 * t])};
+        const uint32_t b1[2] = {ld32(&S.W3[16 * nt + 8 + g][16 * kt + 2 * t]),
+                                ld32(&S.W3[16 * nt + 8 + g][16 * kt + 8 + 2 * t])};
+        mma_bf16(c0, h2[kt], b0);
+        mma_bf16(c1, h2[kt], b1);
+      }
+      const int col0 = 16 * nt + 2 * t, col1 = col0 + 8;
+      S.O[r][col0] = c0[0] + S.b3[col0];
+      S.O[r][col0 + 1] = c0[1] + S.b3[col0 + 1];
+      S.O[r + 8][col0] = c0[2] + S.b3[col0];
+      S.O[r + 8][col0 + 1] = c0[3] + S.b3[col0 + 1];
+      S.O[r][col1] = c1[0] + S.b3[col1];
+      S.O[r][col1 + 1] = c1[1] + S.b3[col1 + 1];
+      S.O[r + 8][col1] = c1[2] + S.b3[col1];
+      S.O[r + 8][col1 + 1] = c1[3] + S.b3[col1 + 1];
+    }
+  }
+}
+
+__global__ void __launch_bounds__(128) fit_warm_fused_kernel(const MixedArgs a, const FusedMlp w) {
+  extern __shared__ __align__(16) unsigned char fused_smem[];
+  FusedSmem& S = *reinterpret_cast<FusedSmem*>(fused_smem);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const __nv_bfloat16* W1 = reinterpret_cast<const __nv_bfloat16*>(w.W1);
+  const __nv_bfloat16* W2 = reinterpret_cast<const __nv_bfloat16*>(w.W2);
+  const __nv_bfloat16* W3 = reinterpret_cast<const __nv_bfloat16*>(w.W3);
+  for (int e = tid; e < MLP_H * MLP_IN; e += 128) S.W1[e / MLP_IN][e % MLP_IN] = W1[e];
+  for (int e = tid; e < MLP_H * MLP_H; e += 128) S.W2[e / MLP_H][e % MLP_H] = W2[e];
+  for (int e = tid; e < MLP_OUT * MLP_H; e += 128) S.W3[e / MLP_H][e % MLP_H] = W3[e];
+  for (int e = tid; e < MLP_H; e += 128) {
+    S.b1[e] = w.b1[e];
+    S.b2[e] = w.b2[e];
+  }
+  for (int e = tid; e < MLP_OUT; e += 128) S.b3[e] = w.b3[e];
+  __syncthreads();
+  for (int64_t base = int64_t(blockIdx.x) * 128; base < a.n; base += int64_t(gridDim.x) * 128) {
+    const int64_t ch = base + tid;
+    const bool active = ch < a.n;
+    const int ct = active ? (a.ctype ? int(a.ctype[ch]) : 0) : -1;
+    const bool learned = active && ct == w.set;
+    double y[10], sig = 1.;
+    bool bad = false;
+    float f[MLP_IN], scale = 0.f;
+#pragma unroll
+    for (int j = 0; j < MLP_IN; ++j) f[j] = 0.f;
+    if (learned) {
+      bad = whiten<10>(a, a.tab[ct], ch, y, sig);
+      mlp_features(y, sig, f, &scale);
+    }
+#pragma unroll
+    for (int j = 0; j < MLP_IN; j += 2)
+      *reinterpret_cast<uint32_t*>(&S.X[tid][j]) = pack_bf16(f[j], f[j + 1]);
+    __syncwarp();
+    warp_mlp(S, warp);
+    __syncwarp();
+    if (learned) {
+      unsigned m = 0;
+      float xw[10];
+#pragma unroll
+      for (int k = 0; k < 10; ++k) {
+        if (S.O[tid][k] > 0.f && scale > 0.f) m |= 1u << k;
+        xw[k] = softplusf(S.O[tid][10 + k]) * scale * w.inv_gnorm[k];
+      }
+      fit_from_y<10, 10>(a, a.tab[ct], ch, y, sig, bad, true, m, xw);
+    } else if (active) {
+      if (ct >= a.n_ctypes) {
+        if (a.status) a.status[ch] = CH_BADINPUT;
+        a.chi2[ch] = 0.;
+      } else if (a.tab[ct].N == 10 && a.tab[ct].K == 10) {
+        fit_channel<10, 10, false>(a, a.tab[ct], ch);
+      } else if (a.tab[ct].N == 8 && a.tab[ct].K == 8) {
+        fit_channel<8, 8, false>(a, a.tab[ct], ch);
+      } else if (a.status) {
+        a.status[ch] = CH_BADINPUT;
+      }
+    }
+    __syncwarp();
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_fit_warm_fused(const MixedArgs& a, const FusedMlp& w, int sms, cudaStream_t s) {
+  if (a.n == 0) return cudaSuccess;
+  static bool attr_set = false;
+  const size_t smem = sizeof(FusedSmem);
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(fit_warm_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  const int64_t tiles = (a.n + 127) / 128;
+  const int64_t cap = int64_t(sms) * 3;
+  const int grid = int(tiles < cap ? tiles : cap);
+  fit_warm_fused_kernel<<<grid, 128, smem, s>>>(a, w);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_fit_mixed(const MixedArgs& a, int block, cudaStream_t s) {
   if (a.n == 0) return cudaSuccess;

@@ -112,8 +112,22 @@ struct MixedArgs {
   uint16_t* active_mask;
   uint8_t* status;
   int32_t* iters;
+  double* flops;  // optional per-channel executed FP64 flops
 };
 cudaError_t launch_fit_mixed(const MixedArgs& a, int block, cudaStream_t s);
+
+// Weights of the warm-start MLP for the fused warm fit (device pointers).
+struct FusedMlp {
+  const void* W1;  // bf16 [128][16]
+  const void* W2;  // bf16 [128][128]
+  const void* W3;  // bf16 [32][128]
+  const float* b1;
+  const float* b2;
+  const float* b3;
+  float inv_gnorm[KMAX];
+  int set;
+};
+cudaError_t launch_fit_warm_fused(const MixedArgs& a, const FusedMlp& w, int sms, cudaStream_t s);
 
 // Synthetic generator (synth.cu).
 int synth_conditions(int kind, mf_conditions* cond, double* sigma);

@@ -22,6 +22,7 @@
 
 #include "mf_internal.h"
 #include "mlp.h"
+#include "mlp_common.cuh"
 
 namespace mfgb {
 namespace {
@@ -29,25 +30,6 @@ namespace {
 typedef __nv_bfloat16 bf16;
 
 constexpr int BM = 64, BN = 64, BK = 32, PAD = 8;
-
-__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-__device__ __forceinline__ uint32_t ld32(const bf16* p) { return *reinterpret_cast<const uint32_t*>(p); }
-
-__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.f + erff(x * 0.70710678118654752f)); }
-__device__ __forceinline__ float gelu_grad(float x) {
-  const float cdf = 0.5f * (1.f + erff(x * 0.70710678118654752f));
-  const float pdf = 0.39894228040143268f * expf(-0.5f * x * x);
-  return cdf + x * pdf;
-}
-__device__ __forceinline__ float softplusf(float x) { return x > 20.f ? x : log1pf(expf(x)); }
-__device__ __forceinline__ float sigmoidf(float x) { return 1.f / (1.f + expf(-x)); }
 
 // Warp-level 32x32 tile product over one BK slice held in shared memory
 // (row-major [rows][BK+PAD], k contiguous), accumulating into acc[2][4][4].
@@ -162,22 +144,15 @@ __global__ void mlp_features_kernel(const MlpFeatArgs a) {
   const int t = a.ctype ? int(a.ctype[i]) : 0;
   if (t == a.set && a.N == 10) {
     const double* s = a.samples + i * a.sample_stride;
-    double y[10], n2 = 0.;
+    double y[10];
     int w = 0;
     for (int r = 0; r < 10; ++r) {
       double acc = 0.;
       for (int c = 0; c <= r; ++c) acc = fma(a.W64[w + c], s[c], acc);
       w += r + 1;
       y[r] = acc;
-      n2 = fma(acc, acc, n2);
     }
-    const double nrm = sqrt(n2);
-    const double sig = a.pederr[i];
-    const double inv = nrm > 0 ? 1.0 / nrm : 0.0;
-    for (int r = 0; r < 10; ++r) f[r] = float(y[r] * inv);
-    f[10] = float(log(fmax(nrm / sig, 1e-30)) * 0.1);
-    f[11] = float(sig);
-    scale = float(nrm);
+    mlp_features(y, a.pederr[i], f, &scale);
   }
   bf16* out = a.X + i * MLP_IN;
   for (int j = 0; j < MLP_IN; ++j) out[j] = __float2bfloat16(f[j]);
@@ -323,7 +298,7 @@ __global__ void __launch_bounds__(128) mlp_infer_kernel(const MlpInferArgs a) {
       float scale = 0.f;
       if (i < a.n && (a.ctype ? int(a.ctype[i]) : 0) == a.set) {
         const double* s = a.samples + i * a.sample_stride;
-        double y[10], n2 = 0.;
+        double y[10];
         int w = 0;
 #pragma unroll
         for (int r = 0; r < 10; ++r) {
@@ -332,16 +307,8 @@ __global__ void __launch_bounds__(128) mlp_infer_kernel(const MlpInferArgs a) {
           for (int c = 0; c <= r; ++c) acc = fma(a.W64[w + c], s[c], acc);
           w += r + 1;
           y[r] = acc;
-          n2 = fma(acc, acc, n2);
         }
-        const double nrm = sqrt(n2);
-        const double sig = a.pederr[i];
-        const double inv = nrm > 0 ? 1.0 / nrm : 0.0;
-#pragma unroll
-        for (int r = 0; r < 10; ++r) f[r] = float(y[r] * inv);
-        f[10] = float(log(fmax(nrm / sig, 1e-30)) * 0.1);
-        f[11] = float(sig);
-        scale = float(nrm);
+        mlp_features(y, a.pederr[i], f, &scale);
       }
 #pragma unroll
       for (int j = 0; j < MLP_IN; ++j) S.X[tid][j] = __float2bfloat16(f[j]);

@@ -1,0 +1,57 @@
+// Device helpers shared by the MLP kernels (training, inference, fused warm fit).
+#pragma once
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+namespace mfgb {
+
+// D += A * B on the tensor cores: m16n8k16, BF16 operands, FP32 accumulate.
+// A fragment (row-major 16x16): a[0] = rows g, k 2t..2t+1; a[1] = rows g+8;
+// a[2] = rows g, k 8+2t..; a[3] = rows g+8, k 8+2t... B fragment (16x8,
+// "col"): b[0] = k 2t..2t+1 of column g, b[1] = k 8+2t... D: d[0..1] = row g,
+// columns 2t, 2t+1; d[2..3] = row g+8. (g = lane / 4, t = lane % 4.)
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__device__ __forceinline__ uint32_t ld32(const __nv_bfloat16* p) { return *reinterpret_cast<const uint32_t*>(p); }
+
+// Two floats -> one register holding two BF16 (first in the low half).
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float x) {
+  const float cdf = 0.5f * (1.f + erff(x * 0.70710678118654752f));
+  const float pdf = 0.39894228040143268f * expf(-0.5f * x * x);
+  return cdf + x * pdf;
+}
+__device__ __forceinline__ float softplusf(float x) { return x > 20.f ? x : log1pf(expf(x)); }
+__device__ __forceinline__ float sigmoidf(float x) { return 1.f / (1.f + expf(-x)); }
+
+// MLP input of a channel from its whitened samples y = L_R^-1 s (N = 10) and
+// noise scale: f[0..9] = y / |y|, f[10] = log(|y| / pederr) / 10,
+// f[11] = pederr, f[12..15] = 0; *scale = |y| (amplitude outputs are in units
+// of |y| / |G_k|). The one definition used by training and inference.
+__device__ __forceinline__ void mlp_features(const double* y, double pederr, float* f, float* scale) {
+  double n2 = 0.;
+#pragma unroll
+  for (int r = 0; r < 10; ++r) n2 = fma(y[r], y[r], n2);
+  const double nrm = sqrt(n2);
+  const double inv = nrm > 0. ? 1.0 / nrm : 0.;
+#pragma unroll
+  for (int r = 0; r < 10; ++r) f[r] = float(y[r] * inv);
+  f[10] = logf(fmaxf(float(nrm / pederr), 1e-30f)) * 0.1f;
+  f[11] = float(pederr);
+#pragma unroll
+  for (int r = 12; r < 16; ++r) f[r] = 0.f;
+  *scale = float(nrm);
+}
+
+}  // namespace mfgb

@@ -30,10 +30,6 @@ struct MlpState {
   __nv_bfloat16* W3h = nullptr;
   __nv_bfloat16* W2t = nullptr;
   __nv_bfloat16* W3t = nullptr;
-  // inference workspace of a warm fit (channels per chunk)
-  int64_t ws_cap = 0;
-  uint16_t* warm_mask = nullptr;
-  float* warm_amp = nullptr;
 };
 
 // Host buffers of a gradient check (one forward/backward on the first batch).
@@ -45,7 +41,7 @@ struct MlpGradProbe {
 };
 
 void mlp_free(MlpState& s);
-int mlp_init(MlpState& s, int device, int set, uint64_t seed, int64_t ws_cap);
+int mlp_init(MlpState& s, int device, int set, uint64_t seed);
 int mlp_set_weights(MlpState& s, const float* host);
 int mlp_get_weights(const MlpState& s, float* host);
 void fill_infer_args(const MlpState& s, const HostTables& tab, int unused, MlpInferArgs* a);

@@ -31,12 +31,12 @@ cudaError_t alloc(T** p, size_t count) {
 }  // namespace
 
 void mlp_free(MlpState& s) {
-  void* ps[] = {s.params, s.grads, s.m, s.v, s.W1h, s.W2h, s.W3h, s.W2t, s.W3t, s.warm_mask, s.warm_amp};
+  void* ps[] = {s.params, s.grads, s.m, s.v, s.W1h, s.W2h, s.W3h, s.W2t, s.W3t};
   for (void* p : ps) cudaFree(p);
   s = MlpState();
 }
 
-int mlp_init(MlpState& s, int device, int set, uint64_t seed, int64_t ws_cap) {
+int mlp_init(MlpState& s, int device, int set, uint64_t seed) {
   mlp_free(s);
   cudaError_t e = cudaSetDevice(device);
   if (e == cudaSuccess) e = alloc(&s.params, P_COUNT);
@@ -48,14 +48,11 @@ int mlp_init(MlpState& s, int device, int set, uint64_t seed, int64_t ws_cap) {
   if (e == cudaSuccess) e = alloc(&s.W3h, MLP_OUT * MLP_H);
   if (e == cudaSuccess) e = alloc(&s.W2t, MLP_H * MLP_H);
   if (e == cudaSuccess) e = alloc(&s.W3t, MLP_OUT * MLP_H);
-  if (e == cudaSuccess) e = alloc(&s.warm_mask, ws_cap);
-  if (e == cudaSuccess) e = alloc(&s.warm_amp, ws_cap * 10);
   if (e != cudaSuccess) {
     set_last_error("mlp_init cudaMalloc", e);
     mlp_free(s);
     return MF_ENOMEM;
   }
-  s.ws_cap = ws_cap;
   s.set = set;
   // He-normal weights (std sqrt(2/fan_in)), zero biases; unused outputs stay zero
   std::vector<float> h(P_COUNT, 0.f);

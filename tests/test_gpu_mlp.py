@@ -107,3 +107,49 @@ def test_weights_roundtrip(mf, cuda, mlp_engine, tmp_path):
     assert np.array_equal(w, w2) and hdr["trained_on"] == "test"
     eng.mlp_set_weights(w2)
     assert np.array_equal(eng.mlp_get_weights(), w)
+
+
+def test_warm_fused_mixed_batch(mf, oracle, cuda):
+    """The fused warm kernel on a batch mixing ECAL (learned start) and HCAL
+    (cold start) channels, against the FP64 oracle."""
+    eng = mf.Engine(0)
+    eng.set_conditions(0, mf.synth_conditions(mf.SYNTH_ECAL)[0])
+    eng.set_conditions(1, mf.synth_conditions(mf.SYNTH_HCAL)[0])
+    eng.mlp_init(0, seed=3)
+    tr = DeviceBatch(mf, cuda, 65_536)
+    tr.generate(mf, mf.synth_params(5, 65_536, intime_log=True, lo=0.1, hi=1000.0, pileup_mean=4.0))
+    eng.fit_device(tr.batch, mf.default_options(max_iter_nnls=1000, nnls_start=mf.START_SUPPORT))
+    eng.mlp_train(tr.batch, mf.mlp_params(epochs=2, batch=4096))
+    m = 30_000
+    db = DeviceBatch(mf, cuda, m, ctype=True)
+    db.generate(mf, mf.synth_params(4, m, pileup_mean=-8.0, hcal_fraction=0.4))
+    eng.fit_device(db.batch, mf.default_options(precision=mf.PREC_MIXED, warm_start=mf.WARM_MLP, max_iter_nnls=1000))
+    gpu = db.outputs_host()
+    inp = db.inputs_host()
+    ref = oracle_fit_sets(mf, oracle, eng, inp, max_iter_nnls=1000, start=1)
+    scale = np.maximum(np.abs(ref["amplitudes"]).max(axis=1), 1e-300)
+    err = np.abs(gpu["amplitudes"] - ref["amplitudes"]).max(axis=1) / scale
+    assert (err <= 1e-4).mean() >= 0.999
+    assert (gpu["active_mask"] == ref["active_mask"]).mean() >= 0.999
+    assert (gpu["status"] == 0).all()
+    eng.close()
+
+
+def test_mixed_fp64_flop_counter(mf, cuda):
+    """The instrumented mixed kernel reports its FP64 work; the outputs are unchanged by counting."""
+    eng = mf.Engine(0)
+    eng.set_conditions(0, mf.synth_conditions(mf.SYNTH_ECAL)[0])
+    n = 8192
+    db = DeviceBatch(mf, cuda, n)
+    db.generate(mf, mf.synth_params(3, n, intime_log=True, lo=0.1, hi=1000.0, pileup_mean=4.0))
+    opt = mf.default_options(precision=mf.PREC_MIXED, max_iter_nnls=1000)
+    eng.fit_device(db.batch, opt)
+    a = db.outputs_host()
+    flops = cuda.zeros(n, dtype=cuda.float64, device="cuda")
+    eng.fit_count_flops(db.batch, flops.data_ptr(), opt)
+    b = db.outputs_host()
+    assert np.array_equal(a["amplitudes"], b["amplitudes"])
+    f = flops.cpu().numpy()
+    # whitening 110 + one FP64 solve + residual + chi2 at least
+    assert (f >= 110 + 20 + 22).all() and f.mean() < 2000
+    eng.close()
