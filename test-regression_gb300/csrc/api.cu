@@ -148,6 +148,7 @@ int dispatch_mixed(const mf_context* c, const FitArgs& a, const mf_options* o, c
     fill_dev_mixed(c, t, &m.tab[t]);
   }
   m.n_ctypes = a.n_ctypes;
+  m.skip_set = -1;
   m.n = a.n;
   m.sample_stride = a.sample_stride;
   m.amp_stride = a.amp_stride;
@@ -544,9 +545,13 @@ int mf_table_operator(const mf_conditions* cond, uint32_t mask, double* whiten, 
     for (int i = 0; i < d.N; ++i)
       for (int j = 0; j < d.N; ++j) whiten[i * d.N + j] = j <= i ? h.W64[w++] : 0.;
   }
-  if (pinv) {
-    const int p = __builtin_popcount(mask);
-    std::memcpy(pinv, h.pinv64.data() + h.offset[mask], sizeof(double) * p * d.N);
+  if (pinv) {  // the rows of the set's columns, in ascending order
+    int r = 0;
+    for (int k = 0; k < d.K; ++k)
+      if (mask & (1u << k)) {
+        std::memcpy(pinv + r * d.N, h.pinv64.data() + h.offset[mask] + k * d.N, sizeof(double) * d.N);
+        ++r;
+      }
   }
   return MF_OK;
 }

@@ -26,47 +26,47 @@
 namespace mfgb {
 namespace {
 
-template <int N, int K>
-struct ChannelFP {
-  double y[N];
-  float y32[N];
-  float c32[K];
-  float x32[K];
-  double x64[K];
-};
-
+// Passive-set solves from the dense K x N operator blocks (tables.cu): the
+// same K*N products on every lane, read with 16-byte vector loads. Row k of
+// the block of mask m holds the coefficients of x_k (zero outside m).
 template <int N, int K>
 __device__ __forceinline__ void solve32(const DevMixed& T, unsigned m, const float* y32, float* s) {
-  const float* P = T.pinv32 + T.offset[m];
-  int r = 0;
+  static_assert((K * N) % 4 == 0, "operator blocks are read as float4");
+  const float4* P = reinterpret_cast<const float4*>(T.pinv32) + size_t(m) * (K * N / 4);
 #pragma unroll
-  for (int k = 0; k < K; ++k) {
-    s[k] = 0.f;
-    if (m & (1u << k)) {
-      float acc = 0.f;
+  for (int k = 0; k < K; ++k) s[k] = 0.f;
 #pragma unroll
-      for (int i = 0; i < N; ++i) acc = fmaf(__ldg(P + r * N + i), y32[i], acc);
-      s[k] = acc;
-      ++r;
+  for (int q = 0; q < K * N / 4; ++q) {
+    const float4 v = __ldg(P + q);
+    const float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int e = 4 * q + j;
+      s[e / N] = fmaf(vv[j], y32[e % N], s[e / N]);
     }
   }
 }
 
 template <int N, int K>
 __device__ __forceinline__ void solve64(const DevMixed& T, unsigned m, const double* y, double* s) {
-  const double* P = T.pinv64 + T.offset[m];
-  int r = 0;
+  static_assert((K * N) % 2 == 0, "operator blocks are read as double2");
+  const double2* P = reinterpret_cast<const double2*>(T.pinv64) + size_t(m) * (K * N / 2);
 #pragma unroll
-  for (int k = 0; k < K; ++k) {
-    s[k] = 0.;
-    if (m & (1u << k)) {
-      double acc = 0.;
+  for (int k = 0; k < K; ++k) s[k] = 0.;
 #pragma unroll
-      for (int i = 0; i < N; ++i) acc = fma(__ldg(P + r * N + i), y[i], acc);
-      s[k] = acc;
-      ++r;
-    }
+  for (int q = 0; q < K * N / 2; ++q) {
+    const double2 v = __ldg(P + q);
+    s[(2 * q) / N] = fma(v.x, y[(2 * q) % N], s[(2 * q) / N]);
+    s[(2 * q + 1) / N] = fma(v.y, y[(2 * q + 1) % N], s[(2 * q + 1) / N]);
   }
+}
+
+// x > 0 for a finite double, decided on its bit pattern (integer ops, which
+// keeps the compare off the FP64 pipe)
+__device__ __forceinline__ bool pos64(double v) {
+  const int hi = __double2hiint(v);
+  const unsigned lo = unsigned(__double2loint(v));
+  return (hi > 0 || (hi == 0 && lo != 0u)) && hi < 0x7ff00000;
 }
 
 // FNNLS inner loop (nnls/src/inplace_fnnls.cu:175-230) on a bit mask: solve
@@ -202,25 +202,27 @@ __device__ void fit_from_y(const MixedArgs& a, const DevMixed& T, int64_t ch, co
     ++adds;
     solves += inner_loop<K>(m, x32, s32);
   }
-  // 3. FP64 judge: the FP64 solve on the FP32 passive set, then the KKT test
-  //    in FP64 where FP32 cannot decide; a failed test continues the loop in FP64.
+  // 3. FP64 judge, written so that every lane issues the same FP64 work (on
+  //    this GPU an FP64 warp instruction costs the full pipe time whatever
+  //    the number of active lanes): the dense FP64 solve on the FP32 passive
+  //    set, the dense FP64 residual, and the KKT test screened in FP32 with an
+  //    FP64 gradient only when some lane of the warp is within the FP32 error
+  //    of the threshold. A failed test continues the loop in FP64.
   double x[K];
   auto s64 = [&](unsigned mm, double* out) {
     solve64<N, K>(T, mm, y, out);
-    f64 += 2 * N * __popc(mm);
+    f64 += 2 * N * K;
   };
   {
     double sv[K];
+    s64(m, sv);
+    ++solves;
     bool allpos = true;
-    if (m) {
-      s64(m, sv);
-      ++solves;
 #pragma unroll
-      for (int k = 0; k < K; ++k)
-        if ((m & (1u << k)) && !(sv[k] > 0.)) allpos = false;
+    for (int k = 0; k < K; ++k) {
+      x[k] = sv[k];
+      if ((m & (1u << k)) && !pos64(sv[k])) allpos = false;
     }
-#pragma unroll
-    for (int k = 0; k < K; ++k) x[k] = (m & (1u << k)) ? sv[k] : 0.;
     if (!allpos) {  // rare: step back from the feasible FP32 point in FP64
 #pragma unroll
       for (int k = 0; k < K; ++k) x[k] = double(x32[k]);
@@ -232,25 +234,19 @@ __device__ void fit_from_y(const MixedArgs& a, const DevMixed& T, int64_t ch, co
   int adds64 = 0;
   double r[N];
   for (int it = 0;; ++it) {
-    // FP64 residual r = y - G_S x over the passive columns
+    // FP64 residual r = y - G x (dense: x_k = 0 outside the passive set)
 #pragma unroll
     for (int i = 0; i < N; ++i) r[i] = y[i];
-    for (unsigned mm = m; mm; mm &= mm - 1) {
-      const int k = __ffs(mm) - 1;
-      const double xk = x[k];
-      f64 += 2 * (N - T.gfz[k]);
 #pragma unroll
-      for (int i = 0; i < N; ++i)
-        if (i >= T.gfz[k]) r[i] = fma(-T.G64[k * N + i], xk, r[i]);
-    }
+    for (int k = 0; k < K; ++k)
+#pragma unroll
+      for (int i = 0; i < N; ++i) r[i] = fma(-T.G64[k * N + i], x[k], r[i]);
+    f64 += 2 * N * K;
     if (it >= a.max_iter64) break;
-    // gradient w_k = G_k^T r: screened in FP32 (c - H x), exact in FP64 only
-    // where the FP32 value is within its error bound of the threshold
     float xf[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) xf[k] = float(x[k]);
-    double wmax = 0.;
-    int imax = -1;
+    unsigned flagged = 0;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
       if (m & (1u << k)) continue;
@@ -261,17 +257,25 @@ __device__ void fit_from_y(const MixedArgs& a, const DevMixed& T, int64_t ch, co
         acc -= hx;
         mag += fabsf(hx);
       }
-      if (acc < -4e-6f * mag) continue;  // certainly below the threshold
-      double w = 0.;
-      f64 += 2 * (N - T.gfz[k]);
+      if (acc >= -4e-6f * mag) flagged |= 1u << k;  // not certainly below the threshold
+    }
+    if (!__any_sync(__activemask(), flagged != 0u)) {
+      converged = true;
+      break;
+    }
+    double wmax = 0.;
+    int imax = -1;
 #pragma unroll
-      for (int i = 0; i < N; ++i)
-        if (i >= T.gfz[k]) w = fma(T.G64[k * N + i], r[i], w);
-      if (imax < 0 || w > wmax) {
+    for (int k = 0; k < K; ++k) {
+      double w = 0.;
+#pragma unroll
+      for (int i = 0; i < N; ++i) w = fma(T.G64[k * N + i], r[i], w);
+      if ((flagged & (1u << k)) && (imax < 0 || w > wmax)) {
         wmax = w;
         imax = k;
       }
     }
+    f64 += 2 * N * K;
     if (imax < 0 || !(wmax >= tol64)) {
       converged = true;
       break;
@@ -335,6 +339,7 @@ __global__ void __launch_bounds__(128) fit_mixed_kernel(const MixedArgs a) {
   const int64_t ch = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (ch >= a.n) return;
   const int t = a.ctype ? int(a.ctype[ch]) : 0;
+  if (t == a.skip_set) return;  // fitted by the fused warm kernel
   if (t >= a.n_ctypes) {
     if (a.status) a.status[ch] = CH_BADINPUT;
     a.chi2[ch] = 0.;
@@ -371,6 +376,8 @@ __device__ __forceinline__ void gelu_pack(const float (&c0)[4], const float (&c1
 // The MLP of the warp's 32 channels (rows 32*warp.. of S.X) into S.O. The
 // hidden activations stay in registers: the m16n8 accumulators of one layer,
 // two n8 tiles at a time, are exactly the m16n8k16 A fragments of the next.
+// Layer 2 is produced 16 columns at a time and each slice is folded into
+// layer 3 at once, so only H1 is held (32 registers) and the code stays small.
 __device__ __forceinline__ void warp_mlp(FusedSmem& S, int warp) {
   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
 #pragma unroll 1
@@ -391,8 +398,12 @@ __device__ __forceinline__ void warp_mlp(FusedSmem& S, int warp) {
       mma_bf16(c1, a0, b1);
       gelu_pack(c0, c1, S.b1, 16 * kt + 2 * t, h1[kt]);
     }
-    uint32_t h2[8][4];
+    float o[4][4];
 #pragma unroll
+    for (int n3 = 0; n3 < 4; ++n3)
+#pragma unroll
+      for (int h = 0; h < 4; ++h) o[n3][h] = 0.f;
+#pragma unroll 1
     for (int nt = 0; nt < 8; ++nt) {
       float c0[4] = {0.f, 0.f, 0.f, 0.f}, c1[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
@@ -404,29 +415,22 @@ __device__ __forceinline__ void warp_mlp(FusedSmem& S, int warp) {
         mma_bf16(c0, h1[kt], b0);
         mma_bf16(c1, h1[kt], b1);
       }
-      gelu_pack(c0, c1, S.b2, 16 * nt + 2 * t, h2[nt]);
+      uint32_t h2[4];
+      gelu_pack(c0, c1, S.b2, 16 * nt + 2 * t, h2);
+#pragma unroll
+      for (int n3 = 0; n3 < 4; ++n3) {
+        const uint32_t b3[2] = {ld32(&S.W3[8 * n3 + g][16 * nt + 2 * t]),
+                                ld32(&S.W3[8 * n3 + g][16 * nt + 8 + 2 * t])};
+        mma_bf16(o[n3], h2, b3);
+      }
     }
 #pragma unroll
-    for (int nt = 0; nt < 2; ++nt) {
-      float c0[4] = {0.f, 0.f, 0.f, 0.f}, c1[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-      for (int kt = 0; kt < 8; ++kt) {
-        const uint32_t b0[2] = {ld32(&S.W3[16 * nt + g][16 * kt + 2 * t]),
-                                ld32(&S.W3[16 * nt + g][16 * kt + 8 + 2 * t])};
-        const uint32_t b1[2] = {ld32(&S.W3[16 * nt + 8 + g][16 * kt + 2 * t]),
-                                ld32(&S.W3[16 * nt + 8 + g][16 * kt + 8 + 2 * t])};
-        mma_bf16(c0, h2[kt], b0);
-        mma_bf16(c1, h2[kt], b1);
-      }
-      const int col0 = 16 * nt + 2 * t, col1 = col0 + 8;
-      S.O[r][col0] = c0[0] + S.b3[col0];
-      S.O[r][col0 + 1] = c0[1] + S.b3[col0 + 1];
-      S.O[r + 8][col0] = c0[2] + S.b3[col0];
-      S.O[r + 8][col0 + 1] = c0[3] + S.b3[col0 + 1];
-      S.O[r][col1] = c1[0] + S.b3[col1];
-      S.O[r][col1 + 1] = c1[1] + S.b3[col1 + 1];
-      S.O[r + 8][col1] = c1[2] + S.b3[col1];
-      S.O[r + 8][col1 + 1] = c1[3] + S.b3[col1 + 1];
+    for (int n3 = 0; n3 < 4; ++n3) {
+      const int c = 8 * n3 + 2 * t;
+      S.O[r][c] = o[n3][0] + S.b3[c];
+      S.O[r][c + 1] = o[n3][1] + S.b3[c + 1];
+      S.O[r + 8][c] = o[n3][2] + S.b3[c];
+      S.O[r + 8][c + 1] = o[n3][3] + S.b3[c + 1];
     }
   }
 }
@@ -476,18 +480,8 @@ __global__ void __launch_bounds__(128) fit_warm_fused_kernel(const MixedArgs a, 
         xw[k] = softplusf(S.O[tid][10 + k]) * scale * w.inv_gnorm[k];
       }
       fit_from_y<10, 10>(a, a.tab[ct], ch, y, sig, bad, true, m, xw);
-    } else if (active) {
-      if (ct >= a.n_ctypes) {
-        if (a.status) a.status[ch] = CH_BADINPUT;
-        a.chi2[ch] = 0.;
-      } else if (a.tab[ct].N == 10 && a.tab[ct].K == 10) {
-        fit_channel<10, 10, false>(a, a.tab[ct], ch);
-      } else if (a.tab[ct].N == 8 && a.tab[ct].K == 8) {
-        fit_channel<8, 8, false>(a, a.tab[ct], ch);
-      } else if (a.status) {
-        a.status[ch] = CH_BADINPUT;
-      }
     }
+    // channels of other condition sets are fitted by a cold launch that skips this set
     __syncwarp();
   }
 }
@@ -507,6 +501,12 @@ cudaError_t launch_fit_warm_fused(const MixedArgs& a, const FusedMlp& w, int sms
   const int64_t cap = int64_t(sms) * 3;
   const int grid = int(tiles < cap ? tiles : cap);
   fit_warm_fused_kernel<<<grid, 128, smem, s>>>(a, w);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || a.n_ctypes == 1) return e;
+  MixedArgs rest = a;  // channels of the other condition sets: cold mixed fit
+  rest.skip_set = w.set;
+  const int64_t g2 = (a.n + 127) / 128;
+  fit_mixed_kernel<false><<<unsigned(g2), 128, 0, s>>>(rest);
   return cudaGetLastError();
 }
 

@@ -95,6 +95,7 @@ struct DevMixed {
 struct MixedArgs {
   DevMixed tab[MF_MAX_CTYPES];
   int n_ctypes;
+  int skip_set;  // condition set left to another launch (-1: none)
   int64_t n;
   int sample_stride, amp_stride;
   int max_iter32, max_iter64;
