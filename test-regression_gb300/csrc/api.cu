@@ -546,12 +546,8 @@ int mf_table_operator(const mf_conditions* cond, uint32_t mask, double* whiten, 
       for (int j = 0; j < d.N; ++j) whiten[i * d.N + j] = j <= i ? h.W64[w++] : 0.;
   }
   if (pinv) {  // the rows of the set's columns, in ascending order
-    int r = 0;
-    for (int k = 0; k < d.K; ++k)
-      if (mask & (1u << k)) {
-        std::memcpy(pinv + r * d.N, h.pinv64.data() + h.offset[mask] + k * d.N, sizeof(double) * d.N);
-        ++r;
-      }
+    const int p = __builtin_popcount(mask);
+    std::memcpy(pinv, h.pinv64.data() + h.offset[mask], sizeof(double) * p * d.N);
   }
   return MF_OK;
 }

@@ -352,24 +352,36 @@ __device__ double compute_chisq(int N, int K, const FitState& S, Counter<C>& f) 
   return c;
 }
 
-// NNLS + Minimize, multifit_cpu/src/PulseChiSqSNNLS.cpp:149-166, 219-273
+// NNLS + Minimize, multifit_cpu/src/PulseChiSqSNNLS.cpp:149-166, 219-273.
+// `lanes` = the lanes of the warp that run this call together. The outer
+// iterations are warp-uniform (a ballot at the loop head), and the lanes
+// reconverge after the divergent FNNLS: on this GPU an FP64 warp instruction
+// costs the full pipe time whatever the number of active lanes, so the
+// covariance factor, the whitening and chi2 must be issued once for all lanes
+// rather than once per group of lanes that left FNNLS together.
 template <int NT, int KT, bool C>
 __device__ void minimize(const DevConditions& c, const DevOptions& o, int N, int K, double pederr, FitState& S,
-                         Counter<C>& f) {
-  for (int it = 0; it < o.max_iter_outer; ++it) {
+                         Counter<C>& f, unsigned lanes) {
+  bool done = false;
+  for (int it = 0;; ++it) {
+    const bool run = !done && it < o.max_iter_outer;
+    const unsigned act = __ballot_sync(lanes, run);
+    if (act == 0u) break;
+    if (!run) continue;
     update_cov<NT, KT>(c, N, K, pederr, S, f);
     double A[KMAX * KMAX], b[KMAX];
     for (int k = 0; k < K; ++k) fwd(S.LC, KMAX, S.P + k * N, A + k * N, N, f);
     fwd(S.LC, KMAX, S.samp, b, N, f);
     fnnls<NT, KT>(A, b, S.amp, N, K, o.nnls_eps, o.max_iter_nnls, o.nnls_start, S.st, f);
+    __syncwarp(act);
     const double now = compute_chisq(N, K, S, f);
     const double delta = now - S.chisq;
     f.op(1);
     S.chisq = now;
     ++S.outer_iters;
-    if (fabs(delta) < o.dchi2_tol) return;
+    if (fabs(delta) < o.dchi2_tol) done = true;
   }
-  S.outer_maxed = 1;
+  if (!done) S.outer_maxed = 1;
 }
 
 // ComputeApproxUncertainty, multifit_cpu/src/PulseChiSqSNNLS.cpp:202-207
@@ -386,7 +398,7 @@ __device__ double approx_uncertainty(int N, const FitState& S, int k, Counter<C>
 
 // DoFit, multifit_cpu/src/PulseChiSqSNNLS.cpp:21-147
 template <int NT, int KT, bool C>
-__device__ void dofit(const FitArgs& a, const DevConditions& c, int64_t ch) {
+__device__ void dofit(const FitArgs& a, const DevConditions& c, int64_t ch, unsigned lanes) {
   const int N = NT > 0 ? NT : c.N;
   const int K = KT > 0 ? KT : c.K;
   Counter<C> f;
@@ -406,7 +418,7 @@ __device__ void dofit(const FitArgs& a, const DevConditions& c, int64_t ch) {
   S.outer_iters = 0;
   S.outer_maxed = 0;
 
-  minimize<NT, KT>(c, a.opt, N, K, pederr, S, f);
+  minimize<NT, KT>(c, a.opt, N, K, pederr, S, f, lanes);
   const FnnlsOut main_st = S.st;
   const int main_outer = S.outer_iters;
   const int main_maxed = S.outer_maxed;
@@ -427,14 +439,16 @@ __device__ void dofit(const FitArgs& a, const DevConditions& c, int64_t ch) {
     const double xplus = x0 + approxerr;
     S.amp[kin] = xplus;
     for (int i = 0; i < N; ++i) S.samp[i] = fma(-xplus, pulse_in[i], in[i]);
-    minimize<NT, KT>(c, a.opt, N, K, pederr, S, f);
+    minimize<NT, KT>(c, a.opt, N, K, pederr, S, f, lanes);
     const double chip = compute_chisq(N, K, S, f);
     const double sigmaplus = fabs(xplus - x0) / sqrt(chip - chisq0);
-    if (x0 / sigmaplus > 0.5) {
+    const bool lower = x0 / sigmaplus > 0.5;
+    const unsigned lanes2 = __ballot_sync(lanes, lower);
+    if (lower) {
       const double xminus = (x0 - approxerr) > 0. ? (x0 - approxerr) : 0.;
       S.amp[kin] = xminus;
       for (int i = 0; i < N; ++i) S.samp[i] = fma(-xminus, pulse_in[i], in[i]);
-      minimize<NT, KT>(c, a.opt, N, K, pederr, S, f);
+      minimize<NT, KT>(c, a.opt, N, K, pederr, S, f, lanes2);
       const double chim = compute_chisq(N, K, S, f);
       const double sigmaminus = fabs(xminus - x0) / sqrt(chim - chisq0);
       err = 0.5 * (sigmaplus + sigmaminus);
@@ -479,31 +493,48 @@ __device__ void dofit(const FitArgs& a, const DevConditions& c, int64_t ch) {
   if (C && a.flops) a.flops[ch] = f.f.v;
 }
 
-template <bool C>
-__global__ void __launch_bounds__(128) fit_fp64_kernel(const FitArgs a) {
+// One launch per condition set (lanes of other sets idle); out-of-range set
+// indices are flagged by the first launch.
+template <int NT, int KT, bool C>
+__global__ void __launch_bounds__(128) fit_fp64_kernel(const FitArgs a, int set, int flag_bad) {
   const int64_t ch = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (ch >= a.n) return;
-  int t = a.ctype ? int(a.ctype[ch]) : 0;
-  if (t >= a.n_ctypes) {
-    if (a.status) a.status[ch] = CH_BADINPUT;
-    a.chi2[ch] = 0.;
-    return;
+  bool mine = false;
+  if (ch < a.n) {
+    const int t = a.ctype ? int(a.ctype[ch]) : 0;
+    if (t >= a.n_ctypes) {
+      if (flag_bad) {
+        if (a.status) a.status[ch] = CH_BADINPUT;
+        a.chi2[ch] = 0.;
+      }
+    } else {
+      mine = t == set;
+    }
   }
-  const DevConditions& c = a.cond[t];
-  if (c.N == 10 && c.K == 10) dofit<10, 10, C>(a, c, ch);
-  else if (c.N == 8 && c.K == 8) dofit<8, 8, C>(a, c, ch);
-  else dofit<0, 0, C>(a, c, ch);
+  const unsigned lanes = __ballot_sync(0xffffffffu, mine);  // taken while the warp is converged
+  if (mine) dofit<NT, KT, C>(a, a.cond[set], ch, lanes);
 }
 
 }  // namespace
 
+template <bool C>
+cudaError_t launch_sets(const FitArgs& a, int block, cudaStream_t s) {
+  const unsigned grid = unsigned((a.n + block - 1) / block);
+  for (int t = 0; t < a.n_ctypes; ++t) {
+    const DevConditions& c = a.cond[t];
+    const int flag = t == 0;
+    if (c.N == 10 && c.K == 10) fit_fp64_kernel<10, 10, C><<<grid, block, 0, s>>>(a, t, flag);
+    else if (c.N == 8 && c.K == 8) fit_fp64_kernel<8, 8, C><<<grid, block, 0, s>>>(a, t, flag);
+    else fit_fp64_kernel<0, 0, C><<<grid, block, 0, s>>>(a, t, flag);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 cudaError_t launch_fit_fp64(const FitArgs& a, int block, cudaStream_t s, bool instrumented) {
   if (a.n == 0) return cudaSuccess;
   if (block <= 0) block = 128;
-  const int64_t grid = (a.n + block - 1) / block;
-  if (instrumented) fit_fp64_kernel<true><<<unsigned(grid), block, 0, s>>>(a);
-  else fit_fp64_kernel<false><<<unsigned(grid), block, 0, s>>>(a);
-  return cudaGetLastError();
+  return instrumented ? launch_sets<true>(a, block, s) : launch_sets<false>(a, block, s);
 }
 
 }  // namespace mfgb

@@ -26,38 +26,48 @@
 namespace mfgb {
 namespace {
 
-// Passive-set solves from the dense K x N operator blocks (tables.cu): the
-// same K*N products on every lane, read with 16-byte vector loads. Row k of
-// the block of mask m holds the coefficients of x_k (zero outside m).
+// Passive-set solves from the operator table (tables.cu): rows of the set's
+// columns, p x N packed at offset[m]. The loops are predicated on the mask, so
+// every lane issues the same instruction stream; only the addresses differ.
 template <int N, int K>
 __device__ __forceinline__ void solve32(const DevMixed& T, unsigned m, const float* y32, float* s) {
-  static_assert((K * N) % 4 == 0, "operator blocks are read as float4");
-  const float4* P = reinterpret_cast<const float4*>(T.pinv32) + size_t(m) * (K * N / 4);
+  const float* P = T.pinv32 + __ldg(T.offset + m);
+  int r = 0;
 #pragma unroll
-  for (int k = 0; k < K; ++k) s[k] = 0.f;
+  for (int k = 0; k < K; ++k) {
+    float acc = 0.f;
+    if (m & (1u << k)) {
+      const float2* row = reinterpret_cast<const float2*>(P + r * N);
 #pragma unroll
-  for (int q = 0; q < K * N / 4; ++q) {
-    const float4 v = __ldg(P + q);
-    const float vv[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int e = 4 * q + j;
-      s[e / N] = fmaf(vv[j], y32[e % N], s[e / N]);
+      for (int q = 0; q < N / 2; ++q) {
+        const float2 v = __ldg(row + q);
+        acc = fmaf(v.x, y32[2 * q], acc);
+        acc = fmaf(v.y, y32[2 * q + 1], acc);
+      }
+      ++r;
     }
+    s[k] = acc;
   }
 }
 
 template <int N, int K>
 __device__ __forceinline__ void solve64(const DevMixed& T, unsigned m, const double* y, double* s) {
-  static_assert((K * N) % 2 == 0, "operator blocks are read as double2");
-  const double2* P = reinterpret_cast<const double2*>(T.pinv64) + size_t(m) * (K * N / 2);
+  const double* P = T.pinv64 + __ldg(T.offset + m);
+  int r = 0;
 #pragma unroll
-  for (int k = 0; k < K; ++k) s[k] = 0.;
+  for (int k = 0; k < K; ++k) {
+    double acc = 0.;
+    if (m & (1u << k)) {
+      const double2* row = reinterpret_cast<const double2*>(P + r * N);
 #pragma unroll
-  for (int q = 0; q < K * N / 2; ++q) {
-    const double2 v = __ldg(P + q);
-    s[(2 * q) / N] = fma(v.x, y[(2 * q) % N], s[(2 * q) / N]);
-    s[(2 * q + 1) / N] = fma(v.y, y[(2 * q + 1) % N], s[(2 * q + 1) / N]);
+      for (int q = 0; q < N / 2; ++q) {
+        const double2 v = __ldg(row + q);
+        acc = fma(v.x, y[2 * q], acc);
+        acc = fma(v.y, y[2 * q + 1], acc);
+      }
+      ++r;
+    }
+    s[k] = acc;
   }
 }
 
@@ -139,9 +149,13 @@ __device__ __forceinline__ bool whiten(const MixedArgs& a, const DevMixed& T, in
 
 // The fit of one whitened channel (steps 2-4), optionally from a predicted
 // passive set warm_m with amplitudes warm_x.
+// `lanes` = the lanes of the warp that call this function for the same (N, K);
+// they reconverge before the FP64 judge, so its FP64 instructions are issued
+// once for all of them rather than once per group of lanes that left the
+// FP32 search together.
 template <int N, int K>
 __device__ void fit_from_y(const MixedArgs& a, const DevMixed& T, int64_t ch, const double* y, double sig, bool bad,
-                           bool warm, unsigned warm_m, const float* warm_x) {
+                           bool warm, unsigned warm_m, const float* warm_x, unsigned lanes) {
   // executed FP64 flops (FMA = 2): whitening, FP64 solves, residuals, FP64
   // gradients and chi2 -- the work on the FP64 pipe, the bound of this kernel
   int f64 = N * (N + 1);
@@ -202,6 +216,7 @@ __device__ void fit_from_y(const MixedArgs& a, const DevMixed& T, int64_t ch, co
     ++adds;
     solves += inner_loop<K>(m, x32, s32);
   }
+  __syncwarp(lanes);
   // 3. FP64 judge, written so that every lane issues the same FP64 work (on
   //    this GPU an FP64 warp instruction costs the full pipe time whatever
   //    the number of active lanes): the dense FP64 solve on the FP32 passive
@@ -259,7 +274,7 @@ __device__ void fit_from_y(const MixedArgs& a, const DevMixed& T, int64_t ch, co
       }
       if (acc >= -4e-6f * mag) flagged |= 1u << k;  // not certainly below the threshold
     }
-    if (!__any_sync(__activemask(), flagged != 0u)) {
+    if (!__any_sync(__activemask(), flagged != 0u)) {  // warp-uniform when converged
       converged = true;
       break;
     }
@@ -320,7 +335,7 @@ __device__ void fit_from_y(const MixedArgs& a, const DevMixed& T, int64_t ch, co
 }
 
 template <int N, int K, bool WARM>
-__device__ __forceinline__ void fit_channel(const MixedArgs& a, const DevMixed& T, int64_t ch) {
+__device__ __forceinline__ void fit_channel(const MixedArgs& a, const DevMixed& T, int64_t ch, unsigned lanes) {
   double y[N], sig;
   const bool bad = whiten<N>(a, T, ch, y, sig);
   unsigned m = 0;
@@ -331,24 +346,29 @@ __device__ __forceinline__ void fit_channel(const MixedArgs& a, const DevMixed& 
 #pragma unroll
     for (int k = 0; k < K; ++k) xw[k] = wa[k];
   }
-  fit_from_y<N, K>(a, T, ch, y, sig, bad, WARM, m, xw);
+  fit_from_y<N, K>(a, T, ch, y, sig, bad, WARM, m, xw, lanes);
 }
 
-template <bool WARM>
-__global__ void __launch_bounds__(128) fit_mixed_kernel(const MixedArgs a) {
+// One launch per condition set: lanes of other sets stay idle (the
+// persistent schedule groups channels by set instead). Out-of-range set
+// indices are flagged by the first launch.
+template <int N, int K>
+__global__ void __launch_bounds__(128) fit_mixed_kernel(const MixedArgs a, int set, int flag_bad) {
   const int64_t ch = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (ch >= a.n) return;
-  const int t = a.ctype ? int(a.ctype[ch]) : 0;
-  if (t == a.skip_set) return;  // fitted by the fused warm kernel
-  if (t >= a.n_ctypes) {
-    if (a.status) a.status[ch] = CH_BADINPUT;
-    a.chi2[ch] = 0.;
-    return;
+  bool mine = false;
+  if (ch < a.n) {
+    const int t = a.ctype ? int(a.ctype[ch]) : 0;
+    if (t >= a.n_ctypes) {
+      if (flag_bad) {
+        if (a.status) a.status[ch] = CH_BADINPUT;
+        a.chi2[ch] = 0.;
+      }
+    } else {
+      mine = t == set && t != a.skip_set;
+    }
   }
-  const DevMixed& T = a.tab[t];
-  if (T.N == 10 && T.K == 10) fit_channel<10, 10, WARM>(a, T, ch);
-  else if (T.N == 8 && T.K == 8) fit_channel<8, 8, WARM>(a, T, ch);
-  else if (a.status) a.status[ch] = CH_BADINPUT;  // shapes without a mixed build (rejected on the host)
+  const unsigned lanes = __ballot_sync(0xffffffffu, mine);  // taken while the warp is converged
+  if (mine) fit_channel<N, K, false>(a, a.tab[set], ch, lanes);
 }
 
 // --------------------------------------------------------------------------
@@ -435,7 +455,7 @@ __device__ __forceinline__ void warp_mlp(FusedSmem& S, int warp) {
   }
 }
 
-__global__ void __launch_bounds__(128) fit_warm_fused_kernel(const MixedArgs a, const FusedMlp w) {
+__global__ void __launch_bounds__(128, 3) fit_warm_fused_kernel(const MixedArgs a, const FusedMlp w) {
   extern __shared__ __align__(16) unsigned char fused_smem[];
   FusedSmem& S = *reinterpret_cast<FusedSmem*>(fused_smem);
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -456,6 +476,11 @@ __global__ void __launch_bounds__(128) fit_warm_fused_kernel(const MixedArgs a, 
     const bool active = ch < a.n;
     const int ct = active ? (a.ctype ? int(a.ctype[ch]) : 0) : -1;
     const bool learned = active && ct == w.set;
+    const unsigned lanes = __ballot_sync(0xffffffffu, learned);
+    if (active && ct >= a.n_ctypes) {
+      if (a.status) a.status[ch] = CH_BADINPUT;
+      a.chi2[ch] = 0.;
+    }
     double y[10], sig = 1.;
     bool bad = false;
     float f[MLP_IN], scale = 0.f;
@@ -479,7 +504,7 @@ __global__ void __launch_bounds__(128) fit_warm_fused_kernel(const MixedArgs a, 
         if (S.O[tid][k] > 0.f && scale > 0.f) m |= 1u << k;
         xw[k] = softplusf(S.O[tid][10 + k]) * scale * w.inv_gnorm[k];
       }
-      fit_from_y<10, 10>(a, a.tab[ct], ch, y, sig, bad, true, m, xw);
+      fit_from_y<10, 10>(a, a.tab[ct], ch, y, sig, bad, true, m, xw, lanes);
     }
     // channels of other condition sets are fitted by a cold launch that skips this set
     __syncwarp();
@@ -502,21 +527,28 @@ cudaError_t launch_fit_warm_fused(const MixedArgs& a, const FusedMlp& w, int sms
   const int grid = int(tiles < cap ? tiles : cap);
   fit_warm_fused_kernel<<<grid, 128, smem, s>>>(a, w);
   cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess || a.n_ctypes == 1) return e;
+  if (e != cudaSuccess || a.n_ctypes == 1 || !a.ctype) return e;
   MixedArgs rest = a;  // channels of the other condition sets: cold mixed fit
   rest.skip_set = w.set;
-  const int64_t g2 = (a.n + 127) / 128;
-  fit_mixed_kernel<false><<<unsigned(g2), 128, 0, s>>>(rest);
-  return cudaGetLastError();
+  return launch_fit_mixed(rest, 128, s);
 }
 
 cudaError_t launch_fit_mixed(const MixedArgs& a, int block, cudaStream_t s) {
   if (a.n == 0) return cudaSuccess;
   if (block <= 0) block = 128;
-  const int64_t grid = (a.n + block - 1) / block;
-  if (a.warm_mask) fit_mixed_kernel<true><<<unsigned(grid), block, 0, s>>>(a);
-  else fit_mixed_kernel<false><<<unsigned(grid), block, 0, s>>>(a);
-  return cudaGetLastError();
+  const unsigned grid = unsigned((a.n + block - 1) / block);
+  int flag_bad = 1;
+  for (int t = 0; t < a.n_ctypes; ++t) {
+    if (t == a.skip_set) continue;
+    const DevMixed& T = a.tab[t];
+    if (T.N == 10 && T.K == 10) fit_mixed_kernel<10, 10><<<grid, block, 0, s>>>(a, t, flag_bad);
+    else if (T.N == 8 && T.K == 8) fit_mixed_kernel<8, 8><<<grid, block, 0, s>>>(a, t, flag_bad);
+    else return cudaErrorInvalidValue;
+    flag_bad = 0;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 }  // namespace mfgb

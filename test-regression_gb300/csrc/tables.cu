@@ -10,9 +10,9 @@
 // pseudo-inverse G_S^+ = (G_S^T G_S)^-1 G_S^T, which depends on S only. The
 // engine therefore builds, once per condition set, the pseudo-inverse of
 // every non-empty S (columns in ascending order) by Householder QR in long
-// double, and stores it in FP64 and FP32 padded to a dense K x N block. A
-// passive-set solve on the device is then one K x N matrix-vector product read
-// from an L2-resident table (the same instructions on every lane);
+// double, and stores it in FP64 and FP32 (p x N rows per set, packed). A
+// passive-set solve on the device is then one small matrix-vector product read
+// from an L1/L2-resident table;
 // its error is ~cond(G_S) * eps (the QR-level bound), not cond(G_S)^2 * eps
 // as for normal equations -- which matters here, since cond(G) reaches 5e4
 // for the ECAL pulse and FP32 normal equations would break down.
@@ -134,30 +134,31 @@ int build_mixed_tables(const DevConditions& c, HostTables* t) {
       if (G[k * N + i] != 0) { fz = i; break; }
     t->gfz[k] = fz;
   }
-  // pseudo-inverses of every non-empty passive set, each padded to a dense
-  // K x N block (row k = the coefficients of x_k; zero for k outside the set)
-  // so that a device solve is the same K*N products on every lane
+  // pseudo-inverses of every non-empty passive set: the p rows of the set's
+  // columns (ascending), p x N row-major, packed back to back
   const int nmask = 1 << K;
-  const int block = K * N;
   t->offset.assign(nmask + 1, 0);
-  for (int m = 0; m <= nmask; ++m) t->offset[m] = m * block;
-  t->pinv64.assign(size_t(nmask) * block, 0.0);
-  t->pinv32.assign(size_t(nmask) * block, 0.0f);
+  int total = 0;
+  for (int m = 0; m < nmask; ++m) {
+    t->offset[m] = total;
+    total += __builtin_popcount(unsigned(m)) * N;
+  }
+  t->offset[nmask] = total;
+  t->pinv64.assign(total, 0.0);
+  t->pinv32.assign(total, 0.0f);
   std::vector<ld> A(N * KMAX), pinv(KMAX * N);
   for (int m = 1; m < nmask; ++m) {
-    int p = 0, cols[KMAX];
+    int p = 0;
     for (int k = 0; k < K; ++k)
       if (m & (1 << k)) {
         for (int i = 0; i < N; ++i) A[p * N + i] = G[k * N + i];
-        cols[p++] = k;
+        ++p;
       }
     if (!pinv_qr(A.data(), N, p, pinv.data())) return MF_EINVAL;  // a zero pulse column
-    for (int r = 0; r < p; ++r)
-      for (int i = 0; i < N; ++i) {
-        const size_t e = size_t(m) * block + size_t(cols[r]) * N + i;
-        t->pinv64[e] = double(pinv[r * N + i]);
-        t->pinv32[e] = float(pinv[r * N + i]);
-      }
+    for (int e = 0; e < p * N; ++e) {
+      t->pinv64[t->offset[m] + e] = double(pinv[e]);
+      t->pinv32[t->offset[m] + e] = float(pinv[e]);
+    }
   }
   return MF_OK;
 }
