@@ -65,6 +65,10 @@ struct mf_context {
   float* d_pinv32[MF_MAX_CTYPES] = {nullptr, nullptr};
   MlpState mlp;
   int sms = 152;
+  // mixed-form hand-off workspace (MIXED_CHUNK channels), allocated with the tables
+  uint16_t* ws_mask = nullptr;
+  uint16_t* ws_count = nullptr;
+  float* ws_x = nullptr;
   // staging area for mf_fit_host
   int64_t cap = 0;
   int cap_ss = 0, cap_as = 0;
@@ -149,6 +153,7 @@ int dispatch_mixed(const mf_context* c, const FitArgs& a, const mf_options* o, c
   }
   m.n_ctypes = a.n_ctypes;
   m.skip_set = -1;
+  m.warm_set = -1;
   m.n = a.n;
   m.sample_stride = a.sample_stride;
   m.amp_stride = a.amp_stride;
@@ -166,30 +171,51 @@ int dispatch_mixed(const mf_context* c, const FitArgs& a, const mf_options* o, c
   m.status = a.status;
   m.iters = a.iters;
   m.flops = a.flops;
-  if (!warm) {
-    cudaError_t e = launch_fit_mixed(m, o->block_size, s);
+  m.ws_mask = c->ws_mask;
+  m.ws_count = c->ws_count;
+  m.ws_x = c->ws_x;
+  if (!m.ws_mask) return MF_ENOMEM;
+  MlpInferArgs ia;
+  if (warm) {
+    fill_infer_args(c->mlp, c->tab[c->mlp.set], 0, &ia);
+    ia.sample_stride = a.sample_stride;
+    ia.warm_mask = c->mlp.warm_mask;
+    ia.warm_amp = c->mlp.warm_amp;
+    ia.warm_stride = 10;
+  }
+  const int64_t cap = warm && MlpState::kChunk < MIXED_CHUNK ? MlpState::kChunk : MIXED_CHUNK;
+  for (int64_t off = 0; off < a.n; off += cap) {
+    const int64_t cnt = a.n - off < cap ? a.n - off : cap;
+    MixedArgs mc = m;
+    mc.n = cnt;
+    mc.samples = a.samples + off * a.sample_stride;
+    mc.pederr = a.pederr + off;
+    mc.ctype = a.ctype ? a.ctype + off : nullptr;
+    mc.amplitudes = a.amplitudes + off * a.amp_stride;
+    mc.chi2 = a.chi2 + off;
+    mc.intime = a.intime ? a.intime + off : nullptr;
+    mc.active_mask = a.active_mask ? a.active_mask + off : nullptr;
+    mc.status = a.status ? a.status + off : nullptr;
+    mc.iters = a.iters ? a.iters + off : nullptr;
+    mc.flops = a.flops ? a.flops + off : nullptr;
+    cudaError_t e = cudaSuccess;
+    if (warm) {
+      // learned warm start: predictions of this chunk into the network's workspace
+      ia.n = cnt;
+      ia.samples = mc.samples;
+      ia.pederr = mc.pederr;
+      ia.ctype = mc.ctype;
+      mc.warm_mask = c->mlp.warm_mask;
+      mc.warm_amp = c->mlp.warm_amp;
+      mc.warm_stride = 10;
+      mc.warm_set = c->mlp.set;
+      e = launch_mlp_infer(ia, c->sms, s);
+    }
+    if (e == cudaSuccess) e = launch_fit_mixed(mc, o->block_size, s);
     if (e != cudaSuccess) {
-      set_last_error("fit_mixed launch", e);
+      set_last_error("mixed fit launch", e);
       return MF_ECUDA;
     }
-    return MF_OK;
-  }
-  // learned warm start: one fused launch (whitening -> MLP -> warm fit)
-  FusedMlp w;
-  std::memset(&w, 0, sizeof(w));
-  w.W1 = c->mlp.W1h;
-  w.W2 = c->mlp.W2h;
-  w.W3 = c->mlp.W3h;
-  w.b1 = c->mlp.params + P_B1;
-  w.b2 = c->mlp.params + P_B2;
-  w.b3 = c->mlp.params + P_B3;
-  w.set = c->mlp.set;
-  const HostTables& ht = c->tab[c->mlp.set];
-  for (int k = 0; k < KMAX; ++k) w.inv_gnorm[k] = ht.gnorm2[k] > 0 ? float(1.0 / std::sqrt(ht.gnorm2[k])) : 0.f;
-  cudaError_t e = launch_fit_warm_fused(m, w, c->sms, s);
-  if (e != cudaSuccess) {
-    set_last_error("fit_warm_fused launch", e);
-    return MF_ECUDA;
   }
   return MF_OK;
 }
@@ -256,6 +282,11 @@ int upload_tables(mf_context* c, int t) {
   if (e == cudaSuccess) e = cudaMemcpy(c->d_offset[t], h.offset.data(), sizeof(int) * no, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(c->d_pinv64[t], h.pinv64.data(), sizeof(double) * np, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(c->d_pinv32[t], h.pinv32.data(), sizeof(float) * np, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !c->ws_mask) {
+    e = cudaMalloc(&c->ws_mask, sizeof(uint16_t) * MIXED_CHUNK);
+    if (e == cudaSuccess) e = cudaMalloc(&c->ws_count, sizeof(uint16_t) * MIXED_CHUNK);
+    if (e == cudaSuccess) e = cudaMalloc(&c->ws_x, sizeof(float) * MIXED_CHUNK * KMAX);
+  }
   if (e != cudaSuccess) {
     set_last_error("table upload", e);
     free_tables(c, t);
@@ -273,6 +304,7 @@ void fill_dev_mixed(const mf_context* c, int t, DevMixed* m) {
   m->K = K;
   m->intime_col = c->cond[t].intime_col;
   std::memcpy(m->W64, h.W64, sizeof(h.W64));
+  std::memcpy(m->W32, h.W32, sizeof(h.W32));
   std::memcpy(m->G64, h.G64, sizeof(h.G64));
   std::memcpy(m->H64, h.H64, sizeof(h.H64));
   std::memcpy(m->G32, h.G32, sizeof(h.G32));
@@ -378,6 +410,9 @@ void mf_destroy(mf_context* c) {
   free_staging(c);
   for (int t = 0; t < MF_MAX_CTYPES; ++t) free_tables(c, t);
   mlp_free(c->mlp);
+  cudaFree(c->ws_mask);
+  cudaFree(c->ws_count);
+  cudaFree(c->ws_x);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }

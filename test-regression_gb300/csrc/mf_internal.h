@@ -81,6 +81,7 @@ int build_mixed_tables(const DevConditions& c, HostTables* t);
 struct DevMixed {
   int N, K, intime_col;
   double W64[KMAX * (KMAX + 1) / 2];
+  float W32[KMAX * (KMAX + 1) / 2];
   double G64[KMAX * KMAX];
   double H64[KMAX * KMAX];
   float G32[KMAX * KMAX];
@@ -105,6 +106,7 @@ struct MixedArgs {
   const double* pederr;
   const uint8_t* ctype;
   const uint16_t* warm_mask;  // learned warm start: predicted passive set, or null
+  int warm_set;               // condition set the predictions belong to
   const float* warm_amp;      // predicted amplitudes [n][warm_stride]
   int warm_stride;
   double* amplitudes;
@@ -114,21 +116,16 @@ struct MixedArgs {
   uint8_t* status;
   int32_t* iters;
   double* flops;  // optional per-channel executed FP64 flops
+  // hand-off from the FP32 search to the FP64 judge (context workspace)
+  uint16_t* ws_mask;
+  uint16_t* ws_count;
+  float* ws_x;
 };
+// Channels per chunk of a mixed fit (the size of the hand-off workspace).
+constexpr int64_t MIXED_CHUNK = int64_t(1) << 21;
 cudaError_t launch_fit_mixed(const MixedArgs& a, int block, cudaStream_t s);
 
-// Weights of the warm-start MLP for the fused warm fit (device pointers).
-struct FusedMlp {
-  const void* W1;  // bf16 [128][16]
-  const void* W2;  // bf16 [128][128]
-  const void* W3;  // bf16 [32][128]
-  const float* b1;
-  const float* b2;
-  const float* b3;
-  float inv_gnorm[KMAX];
-  int set;
-};
-cudaError_t launch_fit_warm_fused(const MixedArgs& a, const FusedMlp& w, int sms, cudaStream_t s);
+
 
 // Synthetic generator (synth.cu).
 int synth_conditions(int kind, mf_conditions* cond, double* sigma);

@@ -142,18 +142,7 @@ __global__ void mlp_features_kernel(const MlpFeatArgs a) {
   for (int j = 0; j < MLP_IN; ++j) f[j] = 0.f;
   float scale = 0.f;
   const int t = a.ctype ? int(a.ctype[i]) : 0;
-  if (t == a.set && a.N == 10) {
-    const double* s = a.samples + i * a.sample_stride;
-    double y[10];
-    int w = 0;
-    for (int r = 0; r < 10; ++r) {
-      double acc = 0.;
-      for (int c = 0; c <= r; ++c) acc = fma(a.W64[w + c], s[c], acc);
-      w += r + 1;
-      y[r] = acc;
-    }
-    mlp_features(y, a.pederr[i], f, &scale);
-  }
+  if (t == a.set && a.N == 10) mlp_features(a.W32, a.samples + i * a.sample_stride, a.pederr[i], f, &scale);
   bf16* out = a.X + i * MLP_IN;
   for (int j = 0; j < MLP_IN; ++j) out[j] = __float2bfloat16(f[j]);
   if (a.scale) a.scale[i] = scale;
@@ -232,44 +221,85 @@ __global__ void pack_weights_kernel(const float* w, bf16* wh, bf16* wt, int out,
 }
 
 // --------------------------------------------------------------------------
-// fused inference: one block = 64 channels; weights in shared memory
+// inference: one block = 128 channels (a warp's 32 rows each), weights in
+// shared memory, hidden activations chained through registers
 // --------------------------------------------------------------------------
-constexpr int IT = 64;  // channels per tile
 struct InferSmem {
   bf16 W1[MLP_H][MLP_IN + PAD];
   bf16 W2[MLP_H][MLP_H + PAD];
   bf16 W3[MLP_OUT][MLP_H + PAD];
   float b1[MLP_H], b2[MLP_H], b3[MLP_OUT];
-  bf16 X[IT][MLP_IN + PAD];
-  bf16 H1[IT][MLP_H + PAD];
-  bf16 H2[IT][MLP_H + PAD];
-  float O[IT][MLP_OUT + 1];
-  float scale[IT];
+  bf16 X[128][MLP_IN + PAD];
+  float O[128][MLP_OUT + 1];
 };
 
-// out[r][c] for r in [0,64), c in [0,NOUT): A (64 x KD) times W^T (NOUT x KD),
-// four warps each owning 16 rows.
-template <int KD, int NOUT, int LDA, int LDW>
-__device__ __forceinline__ void tile_layer(const bf16 (*A)[LDA], const bf16 (*W)[LDW], float (&acc)[NOUT / 8][4]) {
+// Two adjacent n8 accumulator tiles (columns c0.. and c0+8..) after bias and
+// GELU, packed as the BF16 A fragment of the next layer's k16 slice.
+__device__ __forceinline__ void gelu_pack(const float (&c0)[4], const float (&c1)[4], const float* bias, int col0,
+                                          uint32_t (&h)[4]) {
+  h[0] = pack_bf16(gelu(c0[0] + bias[col0]), gelu(c0[1] + bias[col0 + 1]));
+  h[1] = pack_bf16(gelu(c0[2] + bias[col0]), gelu(c0[3] + bias[col0 + 1]));
+  h[2] = pack_bf16(gelu(c1[0] + bias[col0 + 8]), gelu(c1[1] + bias[col0 + 9]));
+  h[3] = pack_bf16(gelu(c1[2] + bias[col0 + 8]), gelu(c1[3] + bias[col0 + 9]));
+}
+
+// The MLP of the warp's 32 rows of S.X into S.O. The m16n8 accumulators of a
+// layer, two n8 tiles at a time, are the m16n8k16 A fragments of the next
+// layer (rows g / g+8, k pairs 2t and 8+2t), so H1 stays in registers and each
+// 16-column slice of H2 is folded into layer 3 at once.
+__device__ __forceinline__ void warp_mlp(InferSmem& S, int warp) {
   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  const int r = (threadIdx.x >> 5) * 16 + g;
+#pragma unroll 1
+  for (int mt = 0; mt < 2; ++mt) {
+    const int r = warp * 32 + mt * 16 + g;
+    uint32_t a0[4];
+    a0[0] = ld32(&S.X[r][2 * t]);
+    a0[1] = ld32(&S.X[r + 8][2 * t]);
+    a0[2] = ld32(&S.X[r][8 + 2 * t]);
+    a0[3] = ld32(&S.X[r + 8][8 + 2 * t]);
+    uint32_t h1[8][4];
 #pragma unroll
-  for (int ni = 0; ni < NOUT / 8; ++ni)
+    for (int kt = 0; kt < 8; ++kt) {
+      float c0[4] = {0.f, 0.f, 0.f, 0.f}, c1[4] = {0.f, 0.f, 0.f, 0.f};
+      const uint32_t b0[2] = {ld32(&S.W1[16 * kt + g][2 * t]), ld32(&S.W1[16 * kt + g][8 + 2 * t])};
+      const uint32_t b1[2] = {ld32(&S.W1[16 * kt + 8 + g][2 * t]), ld32(&S.W1[16 * kt + 8 + g][8 + 2 * t])};
+      mma_bf16(c0, a0, b0);
+      mma_bf16(c1, a0, b1);
+      gelu_pack(c0, c1, S.b1, 16 * kt + 2 * t, h1[kt]);
+    }
+    float o[4][4];
 #pragma unroll
-    for (int h = 0; h < 4; ++h) acc[ni][h] = 0.f;
+    for (int n3 = 0; n3 < 4; ++n3)
 #pragma unroll
-  for (int kk = 0; kk < KD; kk += 16) {
-    uint32_t a[4];
-    a[0] = ld32(&A[r][kk + 2 * t]);
-    a[1] = ld32(&A[r + 8][kk + 2 * t]);
-    a[2] = ld32(&A[r][kk + 8 + 2 * t]);
-    a[3] = ld32(&A[r + 8][kk + 8 + 2 * t]);
+      for (int h = 0; h < 4; ++h) o[n3][h] = 0.f;
+#pragma unroll 1
+    for (int nt = 0; nt < 8; ++nt) {
+      float c0[4] = {0.f, 0.f, 0.f, 0.f}, c1[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-    for (int ni = 0; ni < NOUT / 8; ++ni) {
-      uint32_t b[2];
-      b[0] = ld32(&W[ni * 8 + g][kk + 2 * t]);
-      b[1] = ld32(&W[ni * 8 + g][kk + 8 + 2 * t]);
-      mma_bf16(acc[ni], a, b);
+      for (int kt = 0; kt < 8; ++kt) {
+        const uint32_t b0[2] = {ld32(&S.W2[16 * nt + g][16 * kt + 2 * t]),
+                                ld32(&S.W2[16 * nt + g][16 * kt + 8 + 2 * t])};
+        const uint32_t b1[2] = {ld32(&S.W2[16 * nt + 8 + g][16 * kt + 2 * t]),
+                                ld32(&S.W2[16 * nt + 8 + g][16 * kt + 8 + 2 * t])};
+        mma_bf16(c0, h1[kt], b0);
+        mma_bf16(c1, h1[kt], b1);
+      }
+      uint32_t h2[4];
+      gelu_pack(c0, c1, S.b2, 16 * nt + 2 * t, h2);
+#pragma unroll
+      for (int n3 = 0; n3 < 4; ++n3) {
+        const uint32_t b3[2] = {ld32(&S.W3[8 * n3 + g][16 * nt + 2 * t]),
+                                ld32(&S.W3[8 * n3 + g][16 * nt + 8 + 2 * t])};
+        mma_bf16(o[n3], h2, b3);
+      }
+    }
+#pragma unroll
+    for (int n3 = 0; n3 < 4; ++n3) {
+      const int c = 8 * n3 + 2 * t;
+      S.O[r][c] = o[n3][0] + S.b3[c];
+      S.O[r][c + 1] = o[n3][1] + S.b3[c + 1];
+      S.O[r + 8][c] = o[n3][2] + S.b3[c];
+      S.O[r + 8][c + 1] = o[n3][3] + S.b3[c + 1];
     }
   }
 }
@@ -277,7 +307,7 @@ __device__ __forceinline__ void tile_layer(const bf16 (*A)[LDA], const bf16 (*W)
 __global__ void __launch_bounds__(128) mlp_infer_kernel(const MlpInferArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, warp = tid >> 5;
   for (int e = tid; e < MLP_H * MLP_IN; e += 128) S.W1[e / MLP_IN][e % MLP_IN] = a.W1[e];
   for (int e = tid; e < MLP_H * MLP_H; e += 128) S.W2[e / MLP_H][e % MLP_H] = a.W2[e];
   for (int e = tid; e < MLP_OUT * MLP_H; e += 128) S.W3[e / MLP_H][e % MLP_H] = a.W3[e];
@@ -286,88 +316,33 @@ __global__ void __launch_bounds__(128) mlp_infer_kernel(const MlpInferArgs a) {
     S.b2[e] = a.b2[e];
   }
   for (int e = tid; e < MLP_OUT; e += 128) S.b3[e] = a.b3[e];
-  const int lane = tid & 31, g = lane >> 2, t = lane & 3;
-  const int wr = (tid >> 5) * 16;
-  for (int64_t base = int64_t(blockIdx.x) * IT; base < a.n; base += int64_t(gridDim.x) * IT) {
-    __syncthreads();
-    // features: threads 0..63 one channel each
-    if (tid < IT) {
-      const int64_t i = base + tid;
-      float f[MLP_IN];
-      for (int j = 0; j < MLP_IN; ++j) f[j] = 0.f;
-      float scale = 0.f;
-      if (i < a.n && (a.ctype ? int(a.ctype[i]) : 0) == a.set) {
-        const double* s = a.samples + i * a.sample_stride;
-        double y[10];
-        int w = 0;
+  __syncthreads();
+  for (int64_t base = int64_t(blockIdx.x) * 128; base < a.n; base += int64_t(gridDim.x) * 128) {
+    const int64_t i = base + tid;
+    float f[MLP_IN], scale = 0.f;
 #pragma unroll
-        for (int r = 0; r < 10; ++r) {
-          double acc = 0.;
+    for (int j = 0; j < MLP_IN; ++j) f[j] = 0.f;
+    const bool mine = i < a.n && (a.ctype ? int(a.ctype[i]) : 0) == a.set;
+    if (mine) mlp_features(a.W32, a.samples + i * a.sample_stride, a.pederr[i], f, &scale);
 #pragma unroll
-          for (int c = 0; c <= r; ++c) acc = fma(a.W64[w + c], s[c], acc);
-          w += r + 1;
-          y[r] = acc;
-        }
-        mlp_features(y, a.pederr[i], f, &scale);
+    for (int j = 0; j < MLP_IN; j += 2) *reinterpret_cast<uint32_t*>(&S.X[tid][j]) = pack_bf16(f[j], f[j + 1]);
+    __syncwarp();
+    warp_mlp(S, warp);
+    __syncwarp();
+    if (i < a.n) {
+      uint16_t m = 0;
+      float* wa = a.warm_amp + i * a.warm_stride;
+#pragma unroll
+      for (int k = 0; k < 10; ++k) {
+        if (S.O[tid][k] > 0.f && scale > 0.f) m |= uint16_t(1u << k);
+        wa[k] = softplusf(S.O[tid][10 + k]) * scale * a.inv_gnorm[k];
       }
-#pragma unroll
-      for (int j = 0; j < MLP_IN; ++j) S.X[tid][j] = __float2bfloat16(f[j]);
-      S.scale[tid] = scale;
-    }
-    __syncthreads();
-    {
-      float acc[MLP_H / 8][4];
-      tile_layer<MLP_IN, MLP_H, MLP_IN + PAD, MLP_IN + PAD>(S.X, S.W1, acc);
-#pragma unroll
-      for (int ni = 0; ni < MLP_H / 8; ++ni)
-#pragma unroll
-        for (int h = 0; h < 4; ++h) {
-          const int r = wr + g + (h >= 2 ? 8 : 0), c = ni * 8 + 2 * t + (h & 1);
-          S.H1[r][c] = __float2bfloat16(gelu(acc[ni][h] + S.b1[c]));
-        }
-    }
-    __syncthreads();
-    {
-      float acc[MLP_H / 8][4];
-      tile_layer<MLP_H, MLP_H, MLP_H + PAD, MLP_H + PAD>(S.H1, S.W2, acc);
-#pragma unroll
-      for (int ni = 0; ni < MLP_H / 8; ++ni)
-#pragma unroll
-        for (int h = 0; h < 4; ++h) {
-          const int r = wr + g + (h >= 2 ? 8 : 0), c = ni * 8 + 2 * t + (h & 1);
-          S.H2[r][c] = __float2bfloat16(gelu(acc[ni][h] + S.b2[c]));
-        }
-    }
-    __syncthreads();
-    {
-      float acc[MLP_OUT / 8][4];
-      tile_layer<MLP_H, MLP_OUT, MLP_H + PAD, MLP_H + PAD>(S.H2, S.W3, acc);
-#pragma unroll
-      for (int ni = 0; ni < MLP_OUT / 8; ++ni)
-#pragma unroll
-        for (int h = 0; h < 4; ++h) {
-          const int r = wr + g + (h >= 2 ? 8 : 0), c = ni * 8 + 2 * t + (h & 1);
-          S.O[r][c] = acc[ni][h] + S.b3[c];
-        }
-    }
-    __syncthreads();
-    if (tid < IT) {
-      const int64_t i = base + tid;
-      if (i < a.n) {
-        uint16_t m = 0;
-        const float sc = S.scale[tid];
-        float* wa = a.warm_amp + i * a.warm_stride;
-#pragma unroll
-        for (int k = 0; k < 10; ++k) {
-          if (S.O[tid][k] > 0.f && sc > 0.f) m |= uint16_t(1u << k);
-          wa[k] = softplusf(S.O[tid][10 + k]) * sc * a.inv_gnorm[k];
-        }
-        a.warm_mask[i] = m;
-        if (a.logits) {
-          for (int k = 0; k < MLP_OUT; ++k) a.logits[i * MLP_OUT + k] = S.O[tid][k];
-        }
+      a.warm_mask[i] = mine ? m : uint16_t(0);
+      if (a.logits) {
+        for (int k = 0; k < MLP_OUT; ++k) a.logits[i * MLP_OUT + k] = S.O[tid][k];
       }
     }
+    __syncwarp();
   }
 }
 
@@ -400,8 +375,8 @@ cudaError_t launch_mlp_infer(const MlpInferArgs& a, int sms, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
-  const int64_t tiles = (a.n + IT - 1) / IT;
-  const int64_t cap = int64_t(sms) * 2;
+  const int64_t tiles = (a.n + 127) / 128;
+  const int64_t cap = int64_t(sms) * 3;
   const int grid = int(tiles < cap ? tiles : cap);
   mlp_infer_kernel<<<grid, 128, smem, s>>>(a);
   return cudaGetLastError();

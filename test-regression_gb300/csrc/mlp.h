@@ -36,7 +36,7 @@ struct MlpFeatArgs {
   const uint8_t* ctype;
   int set;  // condition set served by the MLP
   int N;
-  double W64[55];
+  float W32[55];
   __nv_bfloat16* X;  // [n][MLP_IN]
   float* scale;      // [n] |y|
 };
@@ -48,7 +48,7 @@ struct MlpInferArgs {
   const double* pederr;
   const uint8_t* ctype;
   int set;
-  double W64[55];
+  float W32[55];
   float inv_gnorm[10];
   const __nv_bfloat16* W1;  // [MLP_H][MLP_IN]
   const __nv_bfloat16* W2;  // [MLP_H][MLP_H]

@@ -35,23 +35,34 @@ __device__ __forceinline__ float gelu_grad(float x) {
 __device__ __forceinline__ float softplusf(float x) { return x > 20.f ? x : log1pf(expf(x)); }
 __device__ __forceinline__ float sigmoidf(float x) { return 1.f / (1.f + expf(-x)); }
 
-// MLP input of a channel from its whitened samples y = L_R^-1 s (N = 10) and
-// noise scale: f[0..9] = y / |y|, f[10] = log(|y| / pederr) / 10,
-// f[11] = pederr, f[12..15] = 0; *scale = |y| (amplitude outputs are in units
-// of |y| / |G_k|). The one definition used by training and inference.
-__device__ __forceinline__ void mlp_features(const double* y, double pederr, float* f, float* scale) {
-  double n2 = 0.;
+// MLP input of a channel, in FP32 (the network reads BF16): y = L_R^-1 s from
+// the FP32 inverse factor (packed rows, N = 10), f[0..9] = y / |y|,
+// f[10] = log(|y| / pederr) / 10, f[11] = pederr, f[12..15] = 0; *scale = |y|
+// (the amplitude outputs are in units of |y| / |G_k|). The one definition used
+// by training and inference.
+__device__ __forceinline__ void mlp_features(const float* W32, const double* s, double pederr, float* f,
+                                             float* scale) {
+  float y[10], n2 = 0.f;
+  int w = 0;
 #pragma unroll
-  for (int r = 0; r < 10; ++r) n2 = fma(y[r], y[r], n2);
-  const double nrm = sqrt(n2);
-  const double inv = nrm > 0. ? 1.0 / nrm : 0.;
+  for (int r = 0; r < 10; ++r) {
+    float acc = 0.f;
 #pragma unroll
-  for (int r = 0; r < 10; ++r) f[r] = float(y[r] * inv);
-  f[10] = logf(fmaxf(float(nrm / pederr), 1e-30f)) * 0.1f;
-  f[11] = float(pederr);
+    for (int c = 0; c <= r; ++c) acc = fmaf(W32[w + c], float(s[c]), acc);
+    w += r + 1;
+    y[r] = acc;
+    n2 = fmaf(acc, acc, n2);
+  }
+  const float nrm = sqrtf(n2);
+  const float inv = nrm > 0.f ? 1.f / nrm : 0.f;
+  const float sig = float(pederr);
+#pragma unroll
+  for (int r = 0; r < 10; ++r) f[r] = y[r] * inv;
+  f[10] = logf(fmaxf(nrm / sig, 1e-30f)) * 0.1f;
+  f[11] = sig;
 #pragma unroll
   for (int r = 12; r < 16; ++r) f[r] = 0.f;
-  *scale = float(nrm);
+  *scale = nrm;
 }
 
 }  // namespace mfgb

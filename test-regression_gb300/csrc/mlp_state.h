@@ -30,6 +30,11 @@ struct MlpState {
   __nv_bfloat16* W3h = nullptr;
   __nv_bfloat16* W2t = nullptr;
   __nv_bfloat16* W3t = nullptr;
+  // predictions of one chunk of a warm fit (allocated with the network, so a
+  // warm fit allocates nothing)
+  static constexpr int64_t kChunk = int64_t(1) << 21;
+  uint16_t* warm_mask = nullptr;
+  float* warm_amp = nullptr;
 };
 
 // Host buffers of a gradient check (one forward/backward on the first batch).

@@ -31,7 +31,7 @@ cudaError_t alloc(T** p, size_t count) {
 }  // namespace
 
 void mlp_free(MlpState& s) {
-  void* ps[] = {s.params, s.grads, s.m, s.v, s.W1h, s.W2h, s.W3h, s.W2t, s.W3t};
+  void* ps[] = {s.params, s.grads, s.m, s.v, s.W1h, s.W2h, s.W3h, s.W2t, s.W3t, s.warm_mask, s.warm_amp};
   for (void* p : ps) cudaFree(p);
   s = MlpState();
 }
@@ -48,6 +48,8 @@ int mlp_init(MlpState& s, int device, int set, uint64_t seed) {
   if (e == cudaSuccess) e = alloc(&s.W3h, MLP_OUT * MLP_H);
   if (e == cudaSuccess) e = alloc(&s.W2t, MLP_H * MLP_H);
   if (e == cudaSuccess) e = alloc(&s.W3t, MLP_OUT * MLP_H);
+  if (e == cudaSuccess) e = alloc(&s.warm_mask, MlpState::kChunk);
+  if (e == cudaSuccess) e = alloc(&s.warm_amp, MlpState::kChunk * 10);
   if (e != cudaSuccess) {
     set_last_error("mlp_init cudaMalloc", e);
     mlp_free(s);
@@ -104,7 +106,7 @@ void fill_infer_args(const MlpState& s, const HostTables& tab, int intime_unused
   (void)intime_unused;
   std::memset(a, 0, sizeof(*a));
   a->set = s.set;
-  std::memcpy(a->W64, tab.W64, sizeof(a->W64));
+  std::memcpy(a->W32, tab.W32, sizeof(a->W32));
   for (int k = 0; k < 10; ++k) a->inv_gnorm[k] = tab.gnorm2[k] > 0 ? float(1.0 / std::sqrt(tab.gnorm2[k])) : 0.f;
   a->W1 = s.W1h;
   a->W2 = s.W2h;
@@ -157,7 +159,7 @@ int mlp_train(MlpState& s, const HostTables& tab, int64_t n, int sample_stride, 
     fa.ctype = ctype;
     fa.set = s.set;
     fa.N = tab.N;
-    std::memcpy(fa.W64, tab.W64, sizeof(fa.W64));
+    std::memcpy(fa.W32, tab.W32, sizeof(fa.W32));
     fa.X = X;
     fa.scale = scale;
     mlp_features_kernel<<<blocks(n, 256), 256, 0, st>>>(fa);
