@@ -313,6 +313,7 @@ void fill_dev_mixed(const mf_context* c, int t, DevMixed* m) {
     m->gnorm32[k] = float(std::sqrt(h.gnorm2[k]));
     m->gfz[k] = int8_t(h.gfz[k]);
   }
+  m->zero_row = h.offset[size_t(1) << K];
   m->offset = c->d_offset[t];
   m->pinv64 = c->d_pinv64[t];
   m->pinv32 = c->d_pinv32[t];

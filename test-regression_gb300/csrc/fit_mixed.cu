@@ -12,11 +12,11 @@
 //     gradient w = G^T y - H x, solve the passive set, step back and drop
 //     columns that go non-positive -- from an empty set or the predicted one;
 //     writes the passive mask and the FP32 amplitudes of each channel.
-//   judge_kernel   (FP64, lean, every thread the same work): y in FP64, the
-//     FP64 solve on the FP32 passive set, the FP64 residual, the KKT test
-//     max w < eps * pederr^2 (the reference's absolute eps on the pederr-scaled
-//     gradient, PulseChiSqSNNLS.cpp:242) screened in FP32 with an FP64
-//     gradient where FP32 cannot decide, and chi2 = ||y - G x||^2 / pederr^2.
+//   judge_kernel   (FP64, lean, branch-free: every lane the same FP64
+//     instructions): y in FP64, the FP64 solve on the FP32 passive set, the
+//     FP64 residual and gradient, the KKT test max w < eps * pederr^2 (the
+//     reference's absolute eps on the pederr-scaled gradient,
+//     PulseChiSqSNNLS.cpp:242), and chi2 = ||y - G x||^2 / pederr^2.
 //     A failed test continues the loop in FP64, so the result is the FP64 KKT
 //     point whatever the FP32 search found.
 //
@@ -79,6 +79,31 @@ __device__ __forceinline__ void solve64(const DevMixed& T, unsigned m, const dou
         acc = fma(v.y, y[2 * q + 1], acc);
       }
       ++r;
+    }
+    s[k] = acc;
+  }
+}
+
+// The same solve without branches: every lane computes all K rows, rows of
+// columns outside the set read the table's zero row. On this GPU an FP64 warp
+// instruction costs the full pipe time whatever the number of active lanes, so
+// the FP64 judge keeps all 32 lanes busy on every instruction.
+template <int N, int K>
+__device__ __forceinline__ void solve64_dense(const DevMixed& T, unsigned m, const double* y, double* s) {
+  const double* P = T.pinv64 + __ldg(T.offset + m);
+  const double* Z = T.pinv64 + T.zero_row;
+  int r = 0;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const bool in = (m >> k) & 1u;
+    const double2* row = reinterpret_cast<const double2*>(in ? P + r * N : Z);
+    r += in ? 1 : 0;
+    double acc = 0.;
+#pragma unroll
+    for (int q = 0; q < N / 2; ++q) {
+      const double2 v = __ldg(row + q);
+      acc = fma(v.x, y[2 * q], acc);
+      acc = fma(v.y, y[2 * q + 1], acc);
     }
     s[k] = acc;
   }
@@ -266,8 +291,8 @@ __global__ void __launch_bounds__(128, 6) judge_kernel(const MixedArgs a, int se
   const unsigned cnt = a.ws_count[ch];
   int adds = int(cnt & 255u), solves = int(cnt >> 8);
   auto s64 = [&](unsigned mm, double* out) {
-    solve64<N, K>(T, mm, y, out);
-    f64 += 2 * N * __popc(mm);
+    solve64_dense<N, K>(T, mm, y, out);
+    f64 += 2 * N * K;
   };
   // the FP64 solve on the FP32 passive set
   double x[K];
@@ -288,13 +313,8 @@ __global__ void __launch_bounds__(128, 6) judge_kernel(const MixedArgs a, int se
       solves += inner_loop<K>(m, x, s64);
     }
   }
-  // the KKT test: FP32 screen of w = G^T y - H x, FP64 gradient G^T r where
-  // FP32 cannot decide; a violation continues the loop in FP64
-  float y32[N];
-#pragma unroll
-  for (int i = 0; i < N; ++i) y32[i] = float(y[i]);
-  float c32[K], cmag[K];
-  gram_rhs32<N, K>(T, y32, c32, cmag);
+  // the KKT test in FP64: the residual r = y - G x and the gradient G^T r of
+  // every column, both dense; a violation continues the loop in FP64
   const double tol64 = a.eps * sig * sig;
   bool converged = false;
   double r[N];
@@ -308,38 +328,19 @@ __global__ void __launch_bounds__(128, 6) judge_kernel(const MixedArgs a, int se
         if (i >= T.gfz[k]) r[i] = fma(-T.G64[k * N + i], x[k], r[i]);
     f64 += 2 * N * K;
     if (it >= a.max_iter64) break;
-    unsigned flagged = 0;
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      if (m & (1u << k)) continue;
-      float acc = c32[k], mag = cmag[k];
-#pragma unroll
-      for (int j = 0; j < K; ++j) {
-        const float hx = T.H32[k * KMAX + j] * float(x[j]);
-        acc -= hx;
-        mag += fabsf(hx);
-      }
-      if (acc >= -4e-6f * mag) flagged |= 1u << k;  // not certainly below the threshold
-    }
-    if (flagged == 0u) {
-      converged = true;
-      break;
-    }
     double wmax = 0.;
     int imax = -1;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-      if (!(flagged & (1u << k))) continue;
       double w = 0.;
 #pragma unroll
       for (int i = 0; i < N; ++i)
         if (i >= T.gfz[k]) w = fma(T.G64[k * N + i], r[i], w);
-      f64 += 2 * N;
-      if (imax < 0 || w > wmax) {
-        wmax = w;
-        imax = k;
-      }
+      const bool cand = !(m & (1u << k)) && (imax < 0 || w > wmax);
+      wmax = cand ? w : wmax;
+      imax = cand ? k : imax;
     }
+    f64 += 2 * N * K;
     if (imax < 0 || !(wmax >= tol64)) {
       converged = true;
       break;

@@ -88,6 +88,7 @@ struct DevMixed {
   float H32[KMAX * KMAX];
   float gnorm32[KMAX];
   int8_t gfz[KMAX];
+  int zero_row;  // offset of an all-zero row after the last operator
   const int* offset;
   const double* pinv64;
   const float* pinv32;

@@ -143,9 +143,9 @@ int build_mixed_tables(const DevConditions& c, HostTables* t) {
     t->offset[m] = total;
     total += __builtin_popcount(unsigned(m)) * N;
   }
-  t->offset[nmask] = total;
-  t->pinv64.assign(total, 0.0);
-  t->pinv32.assign(total, 0.0f);
+  t->offset[nmask] = total;  // followed by one zero row (the branch-free solves read it)
+  t->pinv64.assign(total + N, 0.0);
+  t->pinv32.assign(total + N, 0.0f);
   std::vector<ld> A(N * KMAX), pinv(KMAX * N);
   for (int m = 1; m < nmask; ++m) {
     int p = 0;
