@@ -250,111 +250,70 @@ __global__ void __launch_bounds__(128) search_kernel(const MixedArgs a, int set)
 // ---------------------------------------------------------------------------
 // FP64 judge
 // ---------------------------------------------------------------------------
+
+// FP64 residual r = y - G x (dense; G's structural zeros are skipped
+// uniformly) and the index and value of the largest gradient w = G^T r over
+// the columns outside the passive set m.
 template <int N, int K>
-__global__ void __launch_bounds__(128, 6) judge_kernel(const MixedArgs a, int set, int flag_bad) {
-  const int64_t ch = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (ch >= a.n) return;
-  const int t = a.ctype ? int(a.ctype[ch]) : 0;
-  if (t >= a.n_ctypes) {
-    if (flag_bad) {
-      if (a.status) a.status[ch] = CH_BADINPUT;
-      a.chi2[ch] = 0.;
-    }
-    return;
+__device__ __forceinline__ void residual_gradient(const DevMixed& T, const double* y, const double* x, unsigned m,
+                                                  double* r, double& wmax, int& imax) {
+#pragma unroll
+  for (int i = 0; i < N; ++i) r[i] = y[i];
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      if (i >= T.gfz[k]) r[i] = fma(-T.G64[k * N + i], x[k], r[i]);
+  wmax = 0.;
+  imax = -1;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    double w = 0.;
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      if (i >= T.gfz[k]) w = fma(T.G64[k * N + i], r[i], w);
+    const bool cand = !(m & (1u << k)) && (imax < 0 || w > wmax);
+    wmax = cand ? w : wmax;
+    imax = cand ? k : imax;
   }
-  if (t != set) return;
-  const DevMixed& T = a.tab[set];
-  // y = L_R^-1 s in FP64 (packed rows, no division)
+}
+
+// y = L_R^-1 s in FP64 (packed rows, no division); returns true for a
+// non-finite or non-positive input.
+template <int N>
+__device__ __forceinline__ bool whiten64(const MixedArgs& a, const DevMixed& T, int64_t ch, double* y, double& sig) {
   const double* in = a.samples + ch * a.sample_stride;
-  const double sig = a.pederr[ch];
+  sig = a.pederr[ch];
   bool bad = !isfinite(sig) || !(sig > 0.);
-  double y[N];
-  {
-    double s[N];
+  double s[N];
 #pragma unroll
-    for (int i = 0; i < N; ++i) {
-      s[i] = in[i];
-      bad = bad || !isfinite(s[i]);
-    }
-    int w = 0;
-#pragma unroll
-    for (int i = 0; i < N; ++i) {
-      double acc = 0.;
-#pragma unroll
-      for (int j = 0; j <= i; ++j) acc = fma(T.W64[w + j], s[j], acc);
-      w += i + 1;
-      y[i] = acc;
-    }
+  for (int i = 0; i < N; ++i) {
+    s[i] = in[i];
+    bad = bad || !isfinite(s[i]);
   }
-  int f64 = N * (N + 1);  // executed FP64 flops (FMA = 2)
-  unsigned m = a.ws_mask[ch];
-  const unsigned cnt = a.ws_count[ch];
-  int adds = int(cnt & 255u), solves = int(cnt >> 8);
-  auto s64 = [&](unsigned mm, double* out) {
-    solve64_dense<N, K>(T, mm, y, out);
-    f64 += 2 * N * K;
-  };
-  // the FP64 solve on the FP32 passive set
-  double x[K];
-  {
-    double sv[K];
-    s64(m, sv);
-    ++solves;
-    bool allpos = true;
+  int w = 0;
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-      x[k] = sv[k];
-      if ((m & (1u << k)) && !pos64(sv[k])) allpos = false;
-    }
-    if (!allpos) {  // rare: step back from the feasible FP32 point in FP64
-      const float* wx = a.ws_x + ch * K;
+  for (int i = 0; i < N; ++i) {
+    double acc = 0.;
 #pragma unroll
-      for (int k = 0; k < K; ++k) x[k] = double(wx[k]);
-      solves += inner_loop<K>(m, x, s64);
-    }
+    for (int j = 0; j <= i; ++j) acc = fma(T.W64[w + j], s[j], acc);
+    w += i + 1;
+    y[i] = acc;
   }
-  // the KKT test in FP64: the residual r = y - G x and the gradient G^T r of
-  // every column, both dense; a violation continues the loop in FP64
-  const double tol64 = a.eps * sig * sig;
-  bool converged = false;
-  double r[N];
-  for (int it = 0;; ++it) {
-#pragma unroll
-    for (int i = 0; i < N; ++i) r[i] = y[i];
-#pragma unroll
-    for (int k = 0; k < K; ++k)
-#pragma unroll
-      for (int i = 0; i < N; ++i)
-        if (i >= T.gfz[k]) r[i] = fma(-T.G64[k * N + i], x[k], r[i]);
-    f64 += 2 * N * K;
-    if (it >= a.max_iter64) break;
-    double wmax = 0.;
-    int imax = -1;
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      double w = 0.;
-#pragma unroll
-      for (int i = 0; i < N; ++i)
-        if (i >= T.gfz[k]) w = fma(T.G64[k * N + i], r[i], w);
-      const bool cand = !(m & (1u << k)) && (imax < 0 || w > wmax);
-      wmax = cand ? w : wmax;
-      imax = cand ? k : imax;
-    }
-    f64 += 2 * N * K;
-    if (imax < 0 || !(wmax >= tol64)) {
-      converged = true;
-      break;
-    }
-    m |= 1u << imax;
-    ++adds;
-    solves += inner_loop<K>(m, x, s64);
-  }
+  return bad;
+}
+
+// Outputs of a judged channel: amplitudes, chi2 from the residual, in-time
+// amplitude, active mask (support of x), status, counters, FP64 flops.
+template <int N, int K>
+__device__ __forceinline__ void write_outputs(const MixedArgs& a, const DevMixed& T, int64_t ch, const double* x,
+                                              const double* r, double sig, bool bad, bool converged, int adds,
+                                              int solves, int f64) {
   double chi2 = 0.;
 #pragma unroll
   for (int i = 0; i < N; ++i) chi2 = fma(r[i], r[i], chi2);
   chi2 = chi2 / (sig * sig);
   f64 += 2 * N + 2;
-
   double* out = a.amplitudes + ch * a.amp_stride;
   bool finite = isfinite(chi2);
   uint16_t support = 0;
@@ -381,6 +340,87 @@ __global__ void __launch_bounds__(128, 6) judge_kernel(const MixedArgs a, int se
     a.iters[ch] = 1 | (fo << 8) | (fi << 20);
   }
   if (a.flops) a.flops[ch] = double(f64);
+}
+
+// The rare repair path (the FP64 solve on the FP32 set has a non-positive
+// component, or the FP64 KKT test fails), out of line and self-contained so
+// that the common path keeps its state in registers: the FNNLS loop in FP64
+// from the FP32 passive set and the feasible FP32 amplitudes, to the FP64 KKT
+// point; writes the channel's outputs.
+template <int N, int K>
+__device__ __noinline__ void judge_repair(const MixedArgs& a, const DevMixed& T, int64_t ch) {
+  double y[N], sig;
+  const bool bad = whiten64<N>(a, T, ch, y, sig);
+  unsigned m = a.ws_mask[ch];
+  const unsigned cnt = a.ws_count[ch];
+  int adds = int(cnt & 255u), solves = int(cnt >> 8) + 1;
+  int f64 = N * (N + 1) + 6 * N * K;
+  auto s64 = [&](unsigned mm, double* out) {
+    solve64_dense<N, K>(T, mm, y, out);
+    f64 += 2 * N * K;
+  };
+  double x[K], r[N];
+  const float* wx = a.ws_x + ch * K;
+#pragma unroll
+  for (int k = 0; k < K; ++k) x[k] = double(wx[k]);
+  solves += inner_loop<K>(m, x, s64);
+  const double tol64 = a.eps * sig * sig;
+  bool converged = false;
+  double wmax;
+  int imax;
+  for (int it = 0; it < a.max_iter64; ++it) {
+    residual_gradient<N, K>(T, y, x, m, r, wmax, imax);
+    f64 += 4 * N * K;
+    if (imax < 0 || !(wmax >= tol64)) {
+      converged = true;
+      break;
+    }
+    m |= 1u << imax;
+    ++adds;
+    solves += inner_loop<K>(m, x, s64);
+  }
+  if (!converged) residual_gradient<N, K>(T, y, x, m, r, wmax, imax);  // residual of the last state
+  write_outputs<N, K>(a, T, ch, x, r, sig, bad, converged, adds, solves, f64);
+}
+
+template <int N, int K>
+__global__ void __launch_bounds__(128, 6) judge_kernel(const MixedArgs a, int set, int flag_bad) {
+  const int64_t ch = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (ch >= a.n) return;
+  const int t = a.ctype ? int(a.ctype[ch]) : 0;
+  if (t >= a.n_ctypes) {
+    if (flag_bad) {
+      if (a.status) a.status[ch] = CH_BADINPUT;
+      a.chi2[ch] = 0.;
+    }
+    return;
+  }
+  if (t != set) return;
+  const DevMixed& T = a.tab[set];
+  double y[N], sig;
+  const bool bad = whiten64<N>(a, T, ch, y, sig);
+  const unsigned m = a.ws_mask[ch];
+  const unsigned cnt = a.ws_count[ch];
+  // common path, straight-line: the FP64 solve on the FP32 passive set, the
+  // residual and gradient, the KKT test max w < eps * pederr^2
+  double x[K], r[N];
+  solve64_dense<N, K>(T, m, y, x);
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+    if ((m & (1u << k)) && !pos64(x[k])) ok = false;
+  if (ok) {
+    double wmax;
+    int imax;
+    residual_gradient<N, K>(T, y, x, m, r, wmax, imax);
+    ok = imax < 0 || !(wmax >= a.eps * sig * sig);
+  }
+  if (!ok) {
+    judge_repair<N, K>(a, T, ch);
+    return;
+  }
+  write_outputs<N, K>(a, T, ch, x, r, sig, bad, true, int(cnt & 255u), int(cnt >> 8) + 1,
+                      N * (N + 1) + 6 * N * K);
 }
 
 }  // namespace
