@@ -240,6 +240,32 @@ __global__ void __launch_bounds__(128) search_kernel(const MixedArgs a, int set)
     ++adds;
     solves += inner_loop<K>(m, x32, s32);
   }
+  // Columns whose gradient FP32 cannot prove negative (within its rounding
+  // error of zero) may still carry a positive FP64 gradient, which the FP64
+  // judge's absolute threshold eps * pederr^2 would add one at a time. Add
+  // them here as a batch; the inner loop drops those that come out negative.
+  {
+    float cmag[K], cc[K];
+    gram_rhs32<N, K>(T, y32, cc, cmag);
+    unsigned amb = 0;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      if (m & (1u << k)) continue;
+      float acc = c32[k], mag = cmag[k];
+#pragma unroll
+      for (int j = 0; j < K; ++j) {
+        const float hx = T.H32[k * KMAX + j] * x32[j];
+        acc -= hx;
+        mag += fabsf(hx);
+      }
+      if (acc >= -4e-6f * mag) amb |= 1u << k;
+    }
+    if (amb) {
+      m |= amb;
+      adds += __popc(amb);
+      solves += inner_loop<K>(m, x32, s32);
+    }
+  }
   a.ws_mask[ch] = uint16_t(m);
   a.ws_count[ch] = uint16_t((adds < 255 ? adds : 255) | ((solves < 255 ? solves : 255) << 8));
   float* wx = a.ws_x + ch * K;
@@ -253,10 +279,12 @@ __global__ void __launch_bounds__(128) search_kernel(const MixedArgs a, int set)
 
 // FP64 residual r = y - G x (dense; G's structural zeros are skipped
 // uniformly) and the index and value of the largest gradient w = G^T r over
-// the columns outside the passive set m.
+// the columns outside the passive set m (and, with viol, the mask of those at
+// or above tol).
 template <int N, int K>
 __device__ __forceinline__ void residual_gradient(const DevMixed& T, const double* y, const double* x, unsigned m,
-                                                  double* r, double& wmax, int& imax) {
+                                                  double* r, double& wmax, int& imax, double tol = 0.,
+                                                  unsigned* viol = nullptr) {
 #pragma unroll
   for (int i = 0; i < N; ++i) r[i] = y[i];
 #pragma unroll
@@ -275,6 +303,7 @@ __device__ __forceinline__ void residual_gradient(const DevMixed& T, const doubl
     const bool cand = !(m & (1u << k)) && (imax < 0 || w > wmax);
     wmax = cand ? w : wmax;
     imax = cand ? k : imax;
+    if (viol && !(m & (1u << k)) && w >= tol) *viol |= 1u << k;
   }
 }
 
@@ -369,14 +398,17 @@ __device__ __noinline__ void judge_repair(const MixedArgs& a, const DevMixed& T,
   double wmax;
   int imax;
   for (int it = 0; it < a.max_iter64; ++it) {
-    residual_gradient<N, K>(T, y, x, m, r, wmax, imax);
+    unsigned viol = 0;
+    residual_gradient<N, K>(T, y, x, m, r, wmax, imax, tol64, &viol);
     f64 += 4 * N * K;
-    if (imax < 0 || !(wmax >= tol64)) {
+    if (viol == 0u) {
       converged = true;
       break;
     }
-    m |= 1u << imax;
-    ++adds;
+    // add every violating column at once (the KKT point of this strictly
+    // convex problem is unique, so the order of additions does not matter)
+    m |= viol;
+    adds += __popc(viol);
     solves += inner_loop<K>(m, x, s64);
   }
   if (!converged) residual_gradient<N, K>(T, y, x, m, r, wmax, imax);  // residual of the last state
