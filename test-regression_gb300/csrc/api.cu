@@ -69,6 +69,8 @@ struct mf_context {
   uint16_t* ws_mask = nullptr;
   uint16_t* ws_count = nullptr;
   float* ws_x = nullptr;
+  int* ws_queue = nullptr;
+  unsigned* ws_qcount = nullptr;
   // staging area for mf_fit_host
   int64_t cap = 0;
   int cap_ss = 0, cap_as = 0;
@@ -174,6 +176,9 @@ int dispatch_mixed(const mf_context* c, const FitArgs& a, const mf_options* o, c
   m.ws_mask = c->ws_mask;
   m.ws_count = c->ws_count;
   m.ws_x = c->ws_x;
+  m.ws_queue = c->ws_queue;
+  m.ws_qcount = c->ws_qcount;
+  m.sms = c->sms;
   if (!m.ws_mask) return MF_ENOMEM;
   MlpInferArgs ia;
   if (warm) {
@@ -286,6 +291,8 @@ int upload_tables(mf_context* c, int t) {
     e = cudaMalloc(&c->ws_mask, sizeof(uint16_t) * MIXED_CHUNK);
     if (e == cudaSuccess) e = cudaMalloc(&c->ws_count, sizeof(uint16_t) * MIXED_CHUNK);
     if (e == cudaSuccess) e = cudaMalloc(&c->ws_x, sizeof(float) * MIXED_CHUNK * KMAX);
+    if (e == cudaSuccess) e = cudaMalloc(&c->ws_queue, sizeof(int) * MIXED_CHUNK);
+    if (e == cudaSuccess) e = cudaMalloc(&c->ws_qcount, sizeof(unsigned));
   }
   if (e != cudaSuccess) {
     set_last_error("table upload", e);
@@ -414,6 +421,8 @@ void mf_destroy(mf_context* c) {
   cudaFree(c->ws_mask);
   cudaFree(c->ws_count);
   cudaFree(c->ws_x);
+  cudaFree(c->ws_queue);
+  cudaFree(c->ws_qcount);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }

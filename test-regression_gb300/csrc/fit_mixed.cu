@@ -181,6 +181,7 @@ __device__ __forceinline__ void gram_rhs32(const DevMixed& T, const float* y32, 
 template <int N, int K, bool WARM>
 __global__ void __launch_bounds__(128) search_kernel(const MixedArgs a, int set) {
   const int64_t ch = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (ch == 0) *a.ws_qcount = 0u;  // the judge launch that follows fills the repair queue
   if (ch >= a.n) return;
   const int t = a.ctype ? int(a.ctype[ch]) : 0;
   if (t != set) return;
@@ -371,13 +372,12 @@ __device__ __forceinline__ void write_outputs(const MixedArgs& a, const DevMixed
   if (a.flops) a.flops[ch] = double(f64);
 }
 
-// The rare repair path (the FP64 solve on the FP32 set has a non-positive
-// component, or the FP64 KKT test fails), out of line and self-contained so
-// that the common path keeps its state in registers: the FNNLS loop in FP64
-// from the FP32 passive set and the feasible FP32 amplitudes, to the FP64 KKT
-// point; writes the channel's outputs.
+// The repair path (the FP64 solve on the FP32 set has a non-positive
+// component, or the FP64 KKT test fails), self-contained: the FNNLS loop in
+// FP64 from the FP32 passive set and the feasible FP32 amplitudes, to the FP64
+// KKT point; writes the channel's outputs.
 template <int N, int K>
-__device__ __noinline__ void judge_repair(const MixedArgs& a, const DevMixed& T, int64_t ch) {
+__device__ __forceinline__ void judge_repair(const MixedArgs& a, const DevMixed& T, int64_t ch) {
   double y[N], sig;
   const bool bad = whiten64<N>(a, T, ch, y, sig);
   unsigned m = a.ws_mask[ch];
@@ -448,22 +448,43 @@ __global__ void __launch_bounds__(128, 6) judge_kernel(const MixedArgs a, int se
     ok = imax < 0 || !(wmax >= a.eps * sig * sig);
   }
   if (!ok) {
-    judge_repair<N, K>(a, T, ch);
+    // compaction: append the channel to the repair queue (one atomic per warp)
+    const unsigned act = __activemask();
+    const int lane = threadIdx.x & 31, leader = __ffs(act) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(a.ws_qcount, unsigned(__popc(act)));
+    base = __shfl_sync(act, base, leader);
+    a.ws_queue[base + __popc(act & ((1u << lane) - 1u))] = int(ch);
     return;
   }
   write_outputs<N, K>(a, T, ch, x, r, sig, bad, true, int(cnt & 255u), int(cnt >> 8) + 1,
                       N * (N + 1) + 6 * N * K);
 }
 
+// Channels the judge queued, in full warps: an FP64 warp instruction costs the
+// same with one active lane as with 32, so a repair left inside the judge
+// would cost its whole warp the repair's FP64 time.
+template <int N, int K>
+__global__ void __launch_bounds__(128) repair_kernel(const MixedArgs a, int set) {
+  const DevMixed& T = a.tab[set];
+  const unsigned cnt = *a.ws_qcount;
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x)
+    judge_repair<N, K>(a, T, int64_t(a.ws_queue[i]));
+}
+
 }  // namespace
 
-// One pair of launches per condition set (lanes of other sets return at
+// One search, judge and repair launch per condition set (lanes of other sets return at
 // once); out-of-range set indices are flagged by the first judge launch.
 cudaError_t launch_fit_mixed(const MixedArgs& a, int block, cudaStream_t s) {
   if (a.n == 0) return cudaSuccess;
   if (block <= 0) block = 128;
   const unsigned grid = unsigned((a.n + block - 1) / block);
   const unsigned jgrid = unsigned((a.n + 127) / 128);
+  // the repair grid covers the queue's worst case (every channel) with at most
+  // eight 128-thread blocks per SM, striding when the queue is longer
+  const int64_t rmax = int64_t(a.sms > 0 ? a.sms : 1) * 8;
+  const unsigned rgrid = unsigned(jgrid < rmax ? jgrid : rmax);
   int flag_bad = 1;
   for (int t = 0; t < a.n_ctypes; ++t) {
     const DevMixed& T = a.tab[t];
@@ -472,9 +493,11 @@ cudaError_t launch_fit_mixed(const MixedArgs& a, int block, cudaStream_t s) {
       if (warm) search_kernel<10, 10, true><<<grid, block, 0, s>>>(a, t);
       else search_kernel<10, 10, false><<<grid, block, 0, s>>>(a, t);
       judge_kernel<10, 10><<<jgrid, 128, 0, s>>>(a, t, flag_bad);
+      repair_kernel<10, 10><<<rgrid, 128, 0, s>>>(a, t);
     } else if (T.N == 8 && T.K == 8) {
       search_kernel<8, 8, false><<<grid, block, 0, s>>>(a, t);
       judge_kernel<8, 8><<<jgrid, 128, 0, s>>>(a, t, flag_bad);
+      repair_kernel<8, 8><<<rgrid, 128, 0, s>>>(a, t);
     } else {
       return cudaErrorInvalidValue;
     }

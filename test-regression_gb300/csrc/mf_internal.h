@@ -121,6 +121,9 @@ struct MixedArgs {
   uint16_t* ws_mask;
   uint16_t* ws_count;
   float* ws_x;
+  int* ws_queue;           // channels the FP64 judge hands to the repair kernel
+  unsigned* ws_qcount;     // their number (zeroed by the search launch)
+  int sms;
 };
 // Channels per chunk of a mixed fit (the size of the hand-off workspace).
 constexpr int64_t MIXED_CHUNK = int64_t(1) << 21;
