@@ -171,6 +171,25 @@ int mf_fit(mf_context* ctx, const mf_batch* batch, const mf_options* opt, void* 
  * FP64 operations (the bound of that kernel) for the mixed precision. */
 int mf_fit_count_flops(mf_context* ctx, const mf_batch* batch, const mf_options* opt, double* flops, void* stream);
 
+/* Same fit as mf_fit with the mixed precision (cold start, grid schedule, no
+ * errors), for callers that may not allocate device memory per call: a module
+ * of a multi-threaded event-processing framework whose caching allocator owns
+ * the device memory, where cudaMalloc/cudaFree would synchronise the device
+ * under every other event in flight. The search-to-judge hand-off lives in a
+ * static device array (about 6 MB per device) instead of the context's
+ * workspace; the call allocates nothing. No counterpart in the reference
+ * (multifit_cpu allocates nothing on the device).
+ *  - n > MF_NOALLOC_MAX_CHANNELS: MF_EINVAL, mf_last_error says why.
+ *  - The context's device must be current. The first call on a device
+ *    resolves the scratch address (cudaGetSymbolAddress): make it before any
+ *    stream capture on that device begins.
+ *  - One scratch per device: calls that overlap on a device (other streams,
+ *    threads or contexts) race on it; serialise them.
+ *  - The only scratch word that must start at zero (the repair-queue counter)
+ *    is written by the call itself before it is read. */
+#define MF_NOALLOC_MAX_CHANNELS 131072
+int mf_fit_noalloc(mf_context* ctx, const mf_batch* batch, const mf_options* opt, void* stream);
+
 /* Same fit with HOST buffers: copies inputs to the context's device staging
  * area, fits, copies results back and synchronises. Grows the staging area
  * when the batch is larger than any before it. */

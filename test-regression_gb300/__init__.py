@@ -104,6 +104,8 @@ class MfMlpTrainParams(C.Structure):
 
 
 # Exported symbols and their signatures: (name, restype, argtypes).
+NOALLOC_MAX_CHANNELS = 131072  # MF_NOALLOC_MAX_CHANNELS
+
 SIGNATURES = [
     ("mf_abi_version", C.c_int, []),
     ("mf_rc_string", C.c_char_p, [C.c_int]),
@@ -115,6 +117,7 @@ SIGNATURES = [
     ("mf_fit", C.c_int, [C.c_void_p, C.POINTER(MfBatch), C.POINTER(MfOptions), C.c_void_p]),
     ("mf_fit_count_flops", C.c_int, [C.c_void_p, C.POINTER(MfBatch), C.POINTER(MfOptions), C.c_void_p, C.c_void_p]),
     ("mf_fit_host", C.c_int, [C.c_void_p, C.POINTER(MfBatch), C.POINTER(MfOptions)]),
+    ("mf_fit_noalloc", C.c_int, [C.c_void_p, C.POINTER(MfBatch), C.POINTER(MfOptions), C.c_void_p]),
     ("mf_build_pulse_matrix", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
     ("mf_table_operator", C.c_int, [C.POINTER(MfConditions), C.c_uint32, C.c_void_p, C.c_void_p]),
     ("mf_mlp_param_count", C.c_int, []),
@@ -322,6 +325,11 @@ class Engine:
     def fit_device(self, batch: MfBatch, options: MfOptions | None = None, stream: int | None = None):
         """mf_fit on device pointers (asynchronous on `stream`)."""
         _check(self.lib.mf_fit(self.h, C.byref(batch), C.byref(options or default_options()), stream), "mf_fit")
+
+    def fit_noalloc(self, batch: MfBatch, options: MfOptions, stream: int | None = None) -> int:
+        """mf_fit_noalloc on device pointers; returns the return code (the
+        caller checks it: oversize batches are an expected MF_EINVAL)."""
+        return int(self.lib.mf_fit_noalloc(self.h, C.byref(batch), C.byref(options), stream))
 
     def fit_count_flops(self, batch: MfBatch, flops_ptr: int, options: MfOptions | None = None,
                         stream: int | None = None):

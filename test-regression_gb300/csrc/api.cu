@@ -618,3 +618,133 @@ int mf_build_pulse_matrix(const double* fullpulse, const int8_t* bxs, int N, int
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// mf_fit_noalloc: the mixed-precision fit with its search -> judge hand-off in
+// a fixed static device array instead of the context's cudaMalloc'd workspace.
+//
+// Who needs it: a module of a multi-threaded event-processing framework that
+// owns the device memory through its own caching allocator. There cudaMalloc
+// and cudaFree are not allowed on the per-event path: they synchronise the
+// whole device (stalling the streams of every other event in flight) and take
+// memory behind the pool's back. Such a caller allocates its channel buffers
+// from its pool, sets the context up once at job start, and then calls this
+// entry point, which allocates nothing.
+//
+// Limits: at most MF_NOALLOC_MAX_CHANNELS channels per call (larger batches
+// are rejected with MF_EINVAL, never split or truncated); cold start only (no
+// MLP warm start), no MINOS errors. The scratch is one array per device, so
+// calls whose work overlaps on one device (two streams, two host threads, two
+// contexts) race on it: serialise them, e.g. one stream per device.
+// What must start at zero: only the repair-queue counter, and the search
+// launch of every call writes it before the judge launch reads it; the other
+// scratch words are written before they are read within a call.
+// ---------------------------------------------------------------------------
+
+namespace {
+
+constexpr int64_t kNoallocMax = MF_NOALLOC_MAX_CHANNELS;
+constexpr size_t kAlignUp(size_t b) { return (b + 255) & ~size_t(255); }
+// byte offsets of the hand-off arrays inside the scratch (each 256-byte aligned)
+constexpr size_t kOffX = 0;                                                     // float [max][KMAX]
+constexpr size_t kOffQueue = kOffX + kAlignUp(sizeof(float) * kNoallocMax * KMAX);  // int [max]
+constexpr size_t kOffMask = kOffQueue + kAlignUp(sizeof(int) * kNoallocMax);       // uint16 [max]
+constexpr size_t kOffCount = kOffMask + kAlignUp(sizeof(uint16_t) * kNoallocMax);  // uint16 [max]
+constexpr size_t kOffQcount = kOffCount + kAlignUp(sizeof(uint16_t) * kNoallocMax);  // unsigned
+constexpr size_t kNoallocBytes = kOffQcount + 256;  // 6,291,712 bytes for 131,072 channels
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned char* g_noalloc_ptr[kMaxDevices] = {};
+
+// Address of this device's scratch, resolved once per device (the device must
+// be current). The first call on a device resolves it; make that call before
+// any stream capture on the device begins.
+int noalloc_scratch(int device, unsigned char** out) {
+  if (device < 0 || device >= kMaxDevices) return MF_EINVAL;
+  std::lock_guard<std::mutex> g(g_noalloc_mu);
+  if (!g_noalloc_ptr[device]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) {
+      set_last_error("mf_fit_noalloc: cudaGetSymbolAddress of the static scratch", e);
+      return MF_ECUDA;
+    }
+    g_noalloc_ptr[device] = static_cast<unsigned char*>(p);
+  }
+  *out = g_noalloc_ptr[device];
+  return MF_OK;
+}
+
+}  // namespace
+
+extern "C" int mf_fit_noalloc(mf_context* c, const mf_batch* b, const mf_options* o, void* stream) {
+  FitArgs a;
+  int rc = fill_args(c, b, o, &a);
+  if (rc) return rc;
+  if (o->precision != MF_PREC_MIXED || o->warm_start != MF_WARM_NONE || o->compute_errors ||
+      o->schedule != MF_SCHED_GRID) {
+    std::snprintf(g_last_error, sizeof(g_last_error),
+                  "mf_fit_noalloc: only the mixed precision, cold start, grid schedule, no errors");
+    return MF_EUNSUPPORTED;
+  }
+  if (b->n > kNoallocMax) {
+    std::snprintf(g_last_error, sizeof(g_last_error),
+                  "mf_fit_noalloc: batch of %lld channels exceeds MF_NOALLOC_MAX_CHANNELS = %lld; split it",
+                  (long long)b->n, (long long)kNoallocMax);
+    return MF_EINVAL;
+  }
+  for (int t = 0; t < a.n_ctypes; ++t)
+    if (!c->tab_ok[t]) return MF_EUNSUPPORTED;
+  int cur = -1;
+  cudaError_t e = cudaGetDevice(&cur);
+  if (e != cudaSuccess) {
+    set_last_error("mf_fit_noalloc: cudaGetDevice", e);
+    return MF_ECUDA;
+  }
+  if (cur != c->device) {
+    std::snprintf(g_last_error, sizeof(g_last_error),
+                  "mf_fit_noalloc: the context's device %d is not the current device %d", c->device, cur);
+    return MF_EINVAL;
+  }
+  unsigned char* scratch = nullptr;
+  rc = noalloc_scratch(cur, &scratch);
+  if (rc) return rc;
+  if (b->n == 0) return MF_OK;
+  MixedArgs m;
+  std::memset(&m, 0, sizeof(m));
+  for (int t = 0; t < a.n_ctypes; ++t) fill_dev_mixed(c, t, &m.tab[t]);
+  m.n_ctypes = a.n_ctypes;
+  m.skip_set = -1;
+  m.warm_set = -1;
+  m.n = a.n;
+  m.sample_stride = a.sample_stride;
+  m.amp_stride = a.amp_stride;
+  m.max_iter32 = 3 * KMAX;  // the search and repair limits of mf_fit's mixed precision
+  m.max_iter64 = o->max_iter_nnls > 0 ? o->max_iter_nnls : 1;
+  m.tol32 = 1e-5f;
+  m.eps = o->nnls_eps;
+  m.samples = a.samples;
+  m.pederr = a.pederr;
+  m.ctype = a.ctype;
+  m.amplitudes = a.amplitudes;
+  m.chi2 = a.chi2;
+  m.intime = a.intime;
+  m.active_mask = a.active_mask;
+  m.status = a.status;
+  m.iters = a.iters;
+  m.ws_x = reinterpret_cast<float*>(scratch + kOffX);
+  m.ws_queue = reinterpret_cast<int*>(scratch + kOffQueue);
+  m.ws_mask = reinterpret_cast<uint16_t*>(scratch + kOffMask);
+  m.ws_count = reinterpret_cast<uint16_t*>(scratch + kOffCount);
+  m.ws_qcount = reinterpret_cast<unsigned*>(scratch + kOffQcount);
+  m.sms = c->sms;
+  e = launch_fit_mixed(m, o->block_size, (cudaStream_t)stream);
+  if (e != cudaSuccess) {
+    set_last_error("mf_fit_noalloc launch", e);
+    return MF_ECUDA;
+  }
+  return MF_OK;
+}
