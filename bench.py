@@ -161,7 +161,9 @@ FORM_DESC = {
     "mixed": "mixed precision: FP32 active-set search + FP64 judge/solve/chi2, KKT-converged",
     "warm": "learned warm start: BF16 tensor-core MLP + mixed-precision FNNLS to KKT",
 }
-LAUNCHES_PER_STEP = {"fp64": 1, "mixed": 1, "warm": 2}
+# useful FLOPs of one warm-start prediction: 12 inputs -> 128 -> 128 -> 20
+# outputs, 2 per multiply-add (the network pads to 16 inputs and 32 outputs)
+MLP_FLOPS_PER_CHANNEL = 2 * (12 * 128 + 128 * 128 + 128 * 20)
 
 
 def form_options(mf, args):
@@ -293,10 +295,15 @@ def run_ours(args, world, rank, local):
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
     clocks.start()
+    eng.profile(True)  # per-kernel CUDA events on the launch stream, inside the timed region
+    torch.cuda.nvtx.range_push("timed_region")  # lets ncu --nvtx-include select exactly these launches
     evs = [step() for _ in range(args.steps)]
+    torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     barrier(world)
     clk = clocks.stop()
+    kernels = eng.profile_read()
+    eng.profile(False)
     times = [e0.elapsed_time(e1) for e0, e1 in evs]
     step_ms = sum(times) / len(times)
     step_ms_max = max_over_ranks(step_ms, world, device=dev)
@@ -413,9 +420,13 @@ def run_ours(args, world, rank, local):
 
     peaks, peak_src = measured_peaks()
     fp64_peak = fp64_peak_tflops(torch)
-    achieved = form_fp64_flops / (step_ms * 1e-3) / 1e12
     bytes_per_launch = n * (10 * 8 + 8) + n * (10 * 8 + 8 + 8 + 2 + 1)
     hbm_gbs = bytes_per_launch / (step_ms * 1e-3) / 1e9
+    kernel_table = kernel_rooflines(mf, eng, kernels, args, n, ctype, flops_per_launch, form_fp64_flops,
+                                    fp64_peak, peaks, peak_src, step_ms)
+    dominant = max(kernel_table, key=lambda k: kernel_table[k]["ms_per_step"])
+    roof = dict(kernel_table[dominant])
+    roof["kernel"] = dominant
 
     out = None
     if rank == 0:
@@ -447,23 +458,8 @@ def run_ours(args, world, rank, local):
             },
             "e2e": {"value": n * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "entry": "mf_fit_host (pinned host buffers)"},
-            "roofline": {
-                "bound": "fp64",
-                "achieved": achieved,
-                "peak": fp64_peak,
-                "unit": "TFLOP/s",
-                "frac": achieved / fp64_peak,
-                "traffic": None,
-                "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (MEASURED_PEAKS.json has no FP64 figure)",
-                "algorithmic_flops_per_launch": form_fp64_flops,
-                "flops_per_channel": form_fp64_flops / n,
-                "plain_algorithm_flops_per_channel": flops_per_launch / n,
-                "kernel": {"fp64": "fit_fp64_kernel", "mixed": "fit_mixed_kernel",
-                           "warm": "fit_mixed_kernel<warm> + mlp_infer_kernel"}[args.form],
-                "flops_note": ("executed FP64 flops of the timed kernel (FMA = 2, div/sqrt = 1), counted by its "
-                               "instrumented run; plain_algorithm_flops_per_channel is the plain FP64 fit's work "
-                               "on the same channels"),
-            },
+            "roofline": roof,
+            "kernels": kernel_table,
             "roofline_hbm": {"bound": "hbm", "achieved": hbm_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                              "frac": hbm_gbs / peaks["hbm_gbs"], "peak_source": peak_src,
                              "algorithmic_bytes_per_launch": bytes_per_launch},
@@ -471,12 +467,64 @@ def run_ours(args, world, rank, local):
             "plain_fp64_same_inputs": baseline,
             "accuracy": accuracy,
             "mlp_training": training,
-            "gpu_launches": args.steps * LAUNCHES_PER_STEP[args.form] * (-(-n // (1 << 21)) if args.form == "warm" else 1),
+            "gpu_launches": sum(v[0] for v in kernels.values()),
             "clocks": clk,
             "parity": parity,
         }
         print(json.dumps(out), flush=True)
     eng.close()
+    return out
+
+
+def kernel_rooflines(mf, eng, kernels, args, n, ctype, plain_flops, form_fp64_flops, fp64_peak, peaks, peak_src,
+                     step_ms):
+    """Roofline of every kernel launched in the timed region: its algorithmic
+    work per launch over its mean launch time (CUDA events from mf_profile).
+
+    fit_fp64_kernel: the plain fit's executed FP64 flops (instrumented count).
+    judge_kernel: N(N+1) + 6NK FP64 flops per channel of its set (whitening,
+      dense passive-set solve, residual, gradient; FMA = 2).
+    repair_kernel: the rest of the form's counted FP64 flops.
+    mlp_infer_kernel: MLP_FLOPS_PER_CHANNEL on the tensor cores (BF16).
+    search_kernel: FP32 and latency-bound; its HBM bytes (samples, pederr,
+      warm start in; hand-off out) against the copy bandwidth."""
+    import numpy as np
+
+    counts = {0: n}
+    if ctype is not None:
+        ct = np.bincount(ctype.cpu().numpy(), minlength=2)
+        counts = {0: int(ct[0]), 1: int(ct[1])}
+    judge = 0.0
+    for t, m in counts.items():
+        c = eng.conditions.get(t)
+        if c is None:
+            continue
+        N, K = c.nsamples, c.npulses
+        judge += m * (N * (N + 1) + 6 * N * K)
+    warm = args.form == "warm"
+    out = {}
+    for name, (launches, total) in kernels.items():
+        per_step = launches / args.steps
+        ms = total / args.steps
+        mean_s = total / launches * 1e-3
+        if name == "fit_fp64_kernel":
+            work, bound, peak, unit = plain_flops / per_step, "fp64", fp64_peak, "TFLOP/s"
+        elif name == "judge_kernel":
+            work, bound, peak, unit = judge / per_step, "fp64", fp64_peak, "TFLOP/s"
+        elif name == "repair_kernel":
+            work, bound, peak, unit = max(form_fp64_flops - judge, 0.0) / per_step, "fp64", fp64_peak, "TFLOP/s"
+        elif name == "mlp_infer_kernel":
+            work = n * MLP_FLOPS_PER_CHANNEL / per_step
+            bound, peak, unit = "tensor", peaks["bf16_tflops"], "TFLOP/s"
+        else:  # search_kernel
+            work = n * (10 * 8 + 8 + (2 + 40 if warm else 0) + 2 + 2 + 40) / per_step
+            bound, peak, unit = "hbm", peaks["hbm_gbs"], "GB/s"
+        achieved = work / mean_s / (1e12 if unit == "TFLOP/s" else 1e9)
+        out[name] = {"bound": bound, "achieved": achieved, "peak": peak, "unit": unit, "frac": achieved / peak,
+                     "traffic": None, "launches_per_step": per_step, "ms_per_step": ms,
+                     "share": ms / step_ms, "work_per_launch": work,
+                     "peak_source": ("cuBLAS DGEMM 4096^3 measured in this run (FP64 pipe)" if bound == "fp64"
+                                     else f"MEASURED_PEAKS.json ({peak_src})")}
     return out
 
 
@@ -542,7 +590,8 @@ def run_reference(args, world, rank):
     t0 = time.perf_counter()
     fit(d)
     rate = probe / (time.perf_counter() - t0)
-    m = int(min(p.n, max(probe, rate * args.cpu_seconds)))
+    per_step_s = min(args.cpu_seconds, 120.0 / (args.steps + args.warmup))
+    m = int(min(p.n, max(probe, rate * per_step_s)))
     d = mf.synth_generate_host(p, 0, m, with_truth=False)
     for _ in range(args.warmup):
         fit(d)
@@ -589,7 +638,8 @@ def main(argv=None):
     ap.add_argument("--channels", type=int, default=0, help="override the workload's channel count")
     ap.add_argument("--max-iter", type=int, default=10)
     ap.add_argument("--start", type=int, default=0, choices=[0, 1])
-    ap.add_argument("--cpu-seconds", type=float, default=3.0)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0,
+                    help="CPU work of the cpu_baseline sample; the reference arm's steps share ~2 minutes")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-parity", action="store_true")
     args = ap.parse_args(argv)

@@ -190,6 +190,27 @@ int mf_fit_count_flops(mf_context* ctx, const mf_batch* batch, const mf_options*
 #define MF_NOALLOC_MAX_CHANNELS 131072
 int mf_fit_noalloc(mf_context* ctx, const mf_batch* batch, const mf_options* opt, void* stream);
 
+/* Per-kernel timing of fits (instrumentation, off by default). The GB300
+ * counterpart of the reference's -DPROFILE timing around the batch (VTune
+ * __itt_resume/__itt_pause and std::chrono, multifit_cpu/src/multifit.cpp:
+ * 231-246): while enabled, every fit records a CUDA event on its stream before
+ * each kernel launch and after its last one (8,192 events per read). */
+enum mf_kernel_kind {
+  MF_K_FIT_FP64 = 0,  /* fit_fp64_kernel: the plain FP64 fit */
+  MF_K_MLP_INFER = 1, /* mlp_infer_kernel: warm-start predictions */
+  MF_K_SEARCH = 2,    /* search_kernel: FP32 active-set search */
+  MF_K_JUDGE = 3,     /* judge_kernel: FP64 solve, residual, KKT test, chi2 */
+  MF_K_REPAIR = 4,    /* repair_kernel: FP64 FNNLS of the channels the judge queued */
+  MF_K_COUNT = 5
+};
+/* enable != 0 creates the context's event pool (and clears it); 0 frees it. */
+int mf_profile(mf_context* ctx, int enable);
+/* Waits for the recorded fits, writes the launch count and the summed device
+ * time (ms) of every kernel kind into launches[MF_K_COUNT] and
+ * total_ms[MF_K_COUNT], and clears the record. MF_ENOMEM if more launches
+ * were made than the pool holds (the counts cover the recorded ones). */
+int mf_profile_read(mf_context* ctx, int32_t* launches, double* total_ms);
+
 /* Same fit with HOST buffers: copies inputs to the context's device staging
  * area, fits, copies results back and synchronises. Grows the staging area
  * when the batch is larger than any before it. */

@@ -105,6 +105,8 @@ class MfMlpTrainParams(C.Structure):
 
 # Exported symbols and their signatures: (name, restype, argtypes).
 NOALLOC_MAX_CHANNELS = 131072  # MF_NOALLOC_MAX_CHANNELS
+# mf_kernel_kind: the kernels mf_profile times
+KERNEL_KINDS = ("fit_fp64_kernel", "mlp_infer_kernel", "search_kernel", "judge_kernel", "repair_kernel")
 
 SIGNATURES = [
     ("mf_abi_version", C.c_int, []),
@@ -118,6 +120,8 @@ SIGNATURES = [
     ("mf_fit_count_flops", C.c_int, [C.c_void_p, C.POINTER(MfBatch), C.POINTER(MfOptions), C.c_void_p, C.c_void_p]),
     ("mf_fit_host", C.c_int, [C.c_void_p, C.POINTER(MfBatch), C.POINTER(MfOptions)]),
     ("mf_fit_noalloc", C.c_int, [C.c_void_p, C.POINTER(MfBatch), C.POINTER(MfOptions), C.c_void_p]),
+    ("mf_profile", C.c_int, [C.c_void_p, C.c_int]),
+    ("mf_profile_read", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     ("mf_build_pulse_matrix", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
     ("mf_table_operator", C.c_int, [C.POINTER(MfConditions), C.c_uint32, C.c_void_p, C.c_void_p]),
     ("mf_mlp_param_count", C.c_int, []),
@@ -330,6 +334,19 @@ class Engine:
         """mf_fit_noalloc on device pointers; returns the return code (the
         caller checks it: oversize batches are an expected MF_EINVAL)."""
         return int(self.lib.mf_fit_noalloc(self.h, C.byref(batch), C.byref(options), stream))
+
+    def profile(self, enable: bool = True):
+        """mf_profile: start (or stop) per-kernel launch timing of fits."""
+        _check(self.lib.mf_profile(self.h, int(enable)), "mf_profile")
+
+    def profile_read(self) -> dict:
+        """mf_profile_read: {kernel: (launches, total device ms)} of the fits
+        recorded since the last read (waits for them)."""
+        n = len(KERNEL_KINDS)
+        launches = (C.c_int32 * n)()
+        ms = (C.c_double * n)()
+        _check(self.lib.mf_profile_read(self.h, launches, ms), "mf_profile_read")
+        return {k: (int(launches[i]), float(ms[i])) for i, k in enumerate(KERNEL_KINDS) if launches[i]}
 
     def fit_count_flops(self, batch: MfBatch, flops_ptr: int, options: MfOptions | None = None,
                         stream: int | None = None):

@@ -85,6 +85,7 @@ struct mf_context {
   uint8_t* d_status = nullptr;
   int32_t* d_iters = nullptr;
   cudaStream_t stream = nullptr;
+  LaunchTimer timer;  // per-kernel launch timing (mf_profile), off by default
   std::mutex mu;
 };
 
@@ -143,7 +144,7 @@ int fill_args(mf_context* ctx, const mf_batch* b, const mf_options* o, FitArgs* 
 
 void fill_dev_mixed(const mf_context* c, int t, DevMixed* m);
 
-int dispatch_mixed(const mf_context* c, const FitArgs& a, const mf_options* o, cudaStream_t s) {
+int dispatch_mixed(mf_context* c, const FitArgs& a, const mf_options* o, cudaStream_t s) {
   if (o->compute_errors || o->schedule != MF_SCHED_GRID) return MF_EUNSUPPORTED;
   const bool warm = o->warm_start == MF_WARM_MLP;
   if (warm && (!c->mlp.trained || !c->tab_ok[c->mlp.set] || c->tab[c->mlp.set].N != 10)) return MF_ENOTRAINED;
@@ -214,9 +215,10 @@ int dispatch_mixed(const mf_context* c, const FitArgs& a, const mf_options* o, c
       mc.warm_amp = c->mlp.warm_amp;
       mc.warm_stride = 10;
       mc.warm_set = c->mlp.set;
+      c->timer.mark(MF_K_MLP_INFER, s);
       e = launch_mlp_infer(ia, c->sms, s);
     }
-    if (e == cudaSuccess) e = launch_fit_mixed(mc, o->block_size, s);
+    if (e == cudaSuccess) e = launch_fit_mixed(mc, o->block_size, s, &c->timer);
     if (e != cudaSuccess) {
       set_last_error("mixed fit launch", e);
       return MF_ECUDA;
@@ -225,16 +227,31 @@ int dispatch_mixed(const mf_context* c, const FitArgs& a, const mf_options* o, c
   return MF_OK;
 }
 
-int dispatch(const mf_context* c, const FitArgs& a, const mf_options* o, cudaStream_t s, bool instrumented) {
+int dispatch_form(mf_context* c, const FitArgs& a, const mf_options* o, cudaStream_t s, bool instrumented) {
   if (o->precision == MF_PREC_MIXED) return dispatch_mixed(c, a, o, s);
   if (o->precision != MF_PREC_FP64 || o->schedule != MF_SCHED_GRID || o->warm_start != MF_WARM_NONE)
     return MF_EUNSUPPORTED;
-  cudaError_t e = launch_fit_fp64(a, o->block_size, s, instrumented);
+  cudaError_t e = launch_fit_fp64(a, o->block_size, s, instrumented, &c->timer);
   if (e != cudaSuccess) {
     set_last_error("fit_fp64 launch", e);
     return MF_ECUDA;
   }
   return MF_OK;
+}
+
+int dispatch(mf_context* c, const FitArgs& a, const mf_options* o, cudaStream_t s, bool instrumented) {
+  const int rc = dispatch_form(c, a, o, s, instrumented);
+  c->timer.mark(-1, s);  // end of this fit's launches
+  return rc;
+}
+
+void destroy_timer(LaunchTimer& t) {
+  if (!t.ev) return;
+  for (int i = 0; i < LaunchTimer::kEvents; ++i) cudaEventDestroy(t.ev[i]);
+  delete[] t.ev;
+  t.ev = nullptr;
+  t.used = 0;
+  t.overflow = false;
 }
 
 void free_staging(mf_context* c) {
@@ -423,8 +440,61 @@ void mf_destroy(mf_context* c) {
   cudaFree(c->ws_x);
   cudaFree(c->ws_queue);
   cudaFree(c->ws_qcount);
+  destroy_timer(c->timer);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
+}
+
+int mf_profile(mf_context* c, int enable) {
+  if (!c) return MF_EINVAL;
+  std::lock_guard<std::mutex> g(c->mu);
+  destroy_timer(c->timer);
+  if (!enable) return MF_OK;
+  c->timer.ev = new (std::nothrow) cudaEvent_t[LaunchTimer::kEvents];
+  if (!c->timer.ev) return MF_ENOMEM;
+  cudaError_t e = cudaSetDevice(c->device);
+  int made = 0;
+  for (; made < LaunchTimer::kEvents && e == cudaSuccess; ++made) e = cudaEventCreate(&c->timer.ev[made]);
+  if (e != cudaSuccess) {
+    for (int i = 0; i + 1 < made; ++i) cudaEventDestroy(c->timer.ev[i]);
+    delete[] c->timer.ev;
+    c->timer.ev = nullptr;
+    set_last_error("mf_profile: cudaEventCreate", e);
+    return MF_ECUDA;
+  }
+  return MF_OK;
+}
+
+int mf_profile_read(mf_context* c, int32_t* launches, double* total_ms) {
+  if (!c || !launches || !total_ms) return MF_EINVAL;
+  std::lock_guard<std::mutex> g(c->mu);
+  for (int k = 0; k < MF_K_COUNT; ++k) {
+    launches[k] = 0;
+    total_ms[k] = 0.;
+  }
+  LaunchTimer& t = c->timer;
+  if (!t.ev) return MF_EINVAL;
+  cudaError_t e = t.used ? cudaEventSynchronize(t.ev[t.used - 1]) : cudaSuccess;
+  for (int i = 0; e == cudaSuccess && i + 1 < t.used; ++i) {
+    if (t.kind[i] < 0) continue;
+    float ms = 0.f;
+    e = cudaEventElapsedTime(&ms, t.ev[i], t.ev[i + 1]);
+    launches[t.kind[i]] += 1;
+    total_ms[t.kind[i]] += ms;
+  }
+  const bool overflow = t.overflow;
+  t.used = 0;
+  t.overflow = false;
+  if (e != cudaSuccess) {
+    set_last_error("mf_profile_read", e);
+    return MF_ECUDA;
+  }
+  if (overflow) {
+    std::snprintf(g_last_error, sizeof(g_last_error), "mf_profile_read: more than %d launches since the last read",
+                  LaunchTimer::kEvents - 1);
+    return MF_ENOMEM;
+  }
+  return MF_OK;
 }
 
 int mf_set_conditions(mf_context* c, int t, const mf_conditions* cond) {

@@ -517,11 +517,12 @@ __global__ void __launch_bounds__(128) fit_fp64_kernel(const FitArgs a, int set,
 }  // namespace
 
 template <bool C>
-cudaError_t launch_sets(const FitArgs& a, int block, cudaStream_t s) {
+cudaError_t launch_sets(const FitArgs& a, int block, cudaStream_t s, LaunchTimer* tm) {
   const unsigned grid = unsigned((a.n + block - 1) / block);
   for (int t = 0; t < a.n_ctypes; ++t) {
     const DevConditions& c = a.cond[t];
     const int flag = t == 0;
+    if (tm) tm->mark(MF_K_FIT_FP64, s);
     if (c.N == 10 && c.K == 10) fit_fp64_kernel<10, 10, C><<<grid, block, 0, s>>>(a, t, flag);
     else if (c.N == 8 && c.K == 8) fit_fp64_kernel<8, 8, C><<<grid, block, 0, s>>>(a, t, flag);
     else fit_fp64_kernel<0, 0, C><<<grid, block, 0, s>>>(a, t, flag);
@@ -531,10 +532,10 @@ cudaError_t launch_sets(const FitArgs& a, int block, cudaStream_t s) {
   return cudaSuccess;
 }
 
-cudaError_t launch_fit_fp64(const FitArgs& a, int block, cudaStream_t s, bool instrumented) {
+cudaError_t launch_fit_fp64(const FitArgs& a, int block, cudaStream_t s, bool instrumented, LaunchTimer* tm) {
   if (a.n == 0) return cudaSuccess;
   if (block <= 0) block = 128;
-  return instrumented ? launch_sets<true>(a, block, s) : launch_sets<false>(a, block, s);
+  return instrumented ? launch_sets<true>(a, block, s, tm) : launch_sets<false>(a, block, s, tm);
 }
 
 }  // namespace mfgb

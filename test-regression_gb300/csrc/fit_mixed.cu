@@ -476,7 +476,10 @@ __global__ void __launch_bounds__(128) repair_kernel(const MixedArgs a, int set)
 
 // One search, judge and repair launch per condition set (lanes of other sets return at
 // once); out-of-range set indices are flagged by the first judge launch.
-cudaError_t launch_fit_mixed(const MixedArgs& a, int block, cudaStream_t s) {
+cudaError_t launch_fit_mixed(const MixedArgs& a, int block, cudaStream_t s, LaunchTimer* tm) {
+  auto mark = [&](int k) {
+    if (tm) tm->mark(k, s);
+  };
   if (a.n == 0) return cudaSuccess;
   if (block <= 0) block = 128;
   const unsigned grid = unsigned((a.n + block - 1) / block);
@@ -490,13 +493,19 @@ cudaError_t launch_fit_mixed(const MixedArgs& a, int block, cudaStream_t s) {
     const DevMixed& T = a.tab[t];
     const bool warm = a.warm_mask && t == a.warm_set;
     if (T.N == 10 && T.K == 10) {
+      mark(MF_K_SEARCH);
       if (warm) search_kernel<10, 10, true><<<grid, block, 0, s>>>(a, t);
       else search_kernel<10, 10, false><<<grid, block, 0, s>>>(a, t);
+      mark(MF_K_JUDGE);
       judge_kernel<10, 10><<<jgrid, 128, 0, s>>>(a, t, flag_bad);
+      mark(MF_K_REPAIR);
       repair_kernel<10, 10><<<rgrid, 128, 0, s>>>(a, t);
     } else if (T.N == 8 && T.K == 8) {
+      mark(MF_K_SEARCH);
       search_kernel<8, 8, false><<<grid, block, 0, s>>>(a, t);
+      mark(MF_K_JUDGE);
       judge_kernel<8, 8><<<jgrid, 128, 0, s>>>(a, t, flag_bad);
+      mark(MF_K_REPAIR);
       repair_kernel<8, 8><<<rgrid, 128, 0, s>>>(a, t);
     } else {
       return cudaErrorInvalidValue;

@@ -58,7 +58,32 @@ struct FitArgs {
 enum : uint8_t { CH_NNLS_MAXITER = 1, CH_OUTER_MAXITER = 2, CH_NONFINITE = 4, CH_BADINPUT = 8 };
 
 // Launchers (fit_fp64.cu).
-cudaError_t launch_fit_fp64(const FitArgs& a, int block, cudaStream_t s, bool instrumented);
+// Per-kernel launch timing of fits (mf_profile): a CUDA event recorded on the
+// launch stream before every kernel launch and after a fit's last launch; the
+// time between two consecutive events belongs to the kernel launched after
+// the first. Off unless enabled; the pool is created by mf_profile.
+struct LaunchTimer {
+  static constexpr int kEvents = 8192;
+  cudaEvent_t* ev = nullptr;  // [kEvents]
+  int8_t kind[kEvents];       // MF_K_* of the launch that follows event i; -1: end of a fit
+  int used = 0;
+  bool overflow = false;
+  void mark(int k, cudaStream_t s) {
+    if (!ev) return;
+    if (used >= kEvents) {
+      overflow = true;
+      return;
+    }
+    if (cudaEventRecord(ev[used], s) != cudaSuccess) {
+      overflow = true;
+      return;
+    }
+    kind[used++] = int8_t(k);
+  }
+};
+
+cudaError_t launch_fit_fp64(const FitArgs& a, int block, cudaStream_t s, bool instrumented,
+                            LaunchTimer* tm = nullptr);
 
 // Host tables of one condition set for the mixed / warm forms (tables.cu).
 struct HostTables {
@@ -127,7 +152,7 @@ struct MixedArgs {
 };
 // Channels per chunk of a mixed fit (the size of the hand-off workspace).
 constexpr int64_t MIXED_CHUNK = int64_t(1) << 21;
-cudaError_t launch_fit_mixed(const MixedArgs& a, int block, cudaStream_t s);
+cudaError_t launch_fit_mixed(const MixedArgs& a, int block, cudaStream_t s, LaunchTimer* tm = nullptr);
 
 
 

@@ -102,3 +102,28 @@ def test_mixed_rejects_unsupported(mf, cuda):
     with pytest.raises(mf.MultifitError):
         eng.fit_host(s, np.full(2, 0.044), options=mf.default_options(precision=mf.PREC_MIXED))
     eng.close()
+
+
+def test_profile_counts_and_times_every_launch(mf, cuda):
+    """mf_profile: one record per kernel launch on the fit's stream, with
+    positive device times, for the mixed form on two condition sets and for
+    the plain FP64 form; nothing is recorded once it is disabled."""
+    eng = mf.Engine(0)
+    eng.set_conditions(0, mf.synth_conditions(mf.SYNTH_ECAL)[0])
+    eng.set_conditions(1, mf.synth_conditions(mf.SYNTH_HCAL)[0])
+    db = DeviceBatch(mf, cuda, 20_000, ctype=True)
+    db.generate(mf, mf.synth_params(21, 20_000, pileup_mean=-8.0, hcal_fraction=0.4))
+    eng.profile(True)
+    for _ in range(2):
+        eng.fit_device(db.batch, mf.default_options(precision=mf.PREC_MIXED, max_iter_nnls=1000))
+    eng.fit_device(db.batch, mf.default_options())
+    rec = eng.profile_read()
+    assert {k: v[0] for k, v in rec.items()} == {"search_kernel": 4, "judge_kernel": 4, "repair_kernel": 4,
+                                                  "fit_fp64_kernel": 2}
+    assert all(ms > 0 for _, ms in rec.values())
+    assert eng.profile_read() == {}  # the read clears the record
+    eng.profile(False)
+    eng.fit_device(db.batch, mf.default_options())
+    with pytest.raises(mf.MultifitError):
+        eng.profile_read()
+    eng.close()
