@@ -316,6 +316,9 @@ def run_ours(args, world, rank, local):
         torch.cuda.synchronize()
         form_amp = amp.clone()
         form_mask = mask.clone()
+        # the clones run on torch's default stream and the fits below on `stream`
+        # (non-blocking): let the copies finish before anything overwrites amp/mask
+        torch.cuda.synchronize()
         # the plain FP64 drop-in on the same inputs (the denominator of the headline ratio)
         popt = mf.default_options()
         eng.fit_device(batch, popt, stream.cuda_stream)
@@ -349,6 +352,7 @@ def run_ours(args, world, rank, local):
                     "active_set_identical_frac": float(same.double().mean().item())}
         amp.copy_(form_amp)
         mask.copy_(form_mask)
+        torch.cuda.synchronize()
 
     # parity spot check of this run's output against the oracle
     parity = None
@@ -482,8 +486,8 @@ def kernel_rooflines(mf, eng, kernels, args, n, ctype, plain_flops, form_fp64_fl
     work per launch over its mean launch time (CUDA events from mf_profile).
 
     fit_fp64_kernel: the plain fit's executed FP64 flops (instrumented count).
-    judge_kernel: N(N+1) + 6NK FP64 flops per channel of its set (whitening,
-      dense passive-set solve, residual, gradient; FMA = 2).
+    judge_kernel: N(N+1) + 4NK FP64 flops per channel of its set (whitening,
+      dense passive-set solve, residual; FMA = 2).
     repair_kernel: the rest of the form's counted FP64 flops.
     mlp_infer_kernel: MLP_FLOPS_PER_CHANNEL on the tensor cores (BF16).
     search_kernel: FP32 and latency-bound; its HBM bytes (samples, pederr,
@@ -500,7 +504,7 @@ def kernel_rooflines(mf, eng, kernels, args, n, ctype, plain_flops, form_fp64_fl
         if c is None:
             continue
         N, K = c.nsamples, c.npulses
-        judge += m * (N * (N + 1) + 6 * N * K)
+        judge += m * (N * (N + 1) + 4 * N * K)
     warm = args.form == "warm"
     out = {}
     for name, (launches, total) in kernels.items():

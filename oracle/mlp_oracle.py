@@ -41,16 +41,18 @@ def bf16(x):
     return u.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
-_erf = np.vectorize(math.erf)
+# GELU, tanh form (Hendrycks & Gimpel 2016), the function the engine's network uses
+_C0 = math.sqrt(2.0 / math.pi)
+_C1 = 0.044715
 
 
 def gelu(z):
-    return 0.5 * z * (1.0 + _erf(z / math.sqrt(2.0)))
+    return 0.5 * z * (1.0 + np.tanh(_C0 * (z + _C1 * z ** 3)))
 
 
 def gelu_grad(z):
-    cdf = 0.5 * (1.0 + _erf(z / math.sqrt(2.0)))
-    return cdf + z * np.exp(-0.5 * z * z) / math.sqrt(2.0 * math.pi)
+    t = np.tanh(_C0 * (z + _C1 * z ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * _C0 * (1.0 + 3.0 * _C1 * z * z)
 
 
 def softplus(x):

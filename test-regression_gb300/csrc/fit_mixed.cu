@@ -14,11 +14,13 @@
 //     writes the passive mask and the FP32 amplitudes of each channel.
 //   judge_kernel   (FP64, lean, branch-free: every lane the same FP64
 //     instructions): y in FP64, the FP64 solve on the FP32 passive set, the
-//     FP64 residual and gradient, the KKT test max w < eps * pederr^2 (the
-//     reference's absolute eps on the pederr-scaled gradient,
-//     PulseChiSqSNNLS.cpp:242), and chi2 = ||y - G x||^2 / pederr^2.
-//     A failed test continues the loop in FP64, so the result is the FP64 KKT
-//     point whatever the FP32 search found.
+//     FP64 residual, chi2 = ||y - G x||^2 / pederr^2, and the KKT test
+//     max w < eps * pederr^2 (the reference's absolute eps on the
+//     pederr-scaled gradient, PulseChiSqSNNLS.cpp:242) screened in FP32 with
+//     a rounding bound. A channel the screen cannot pass (or whose FP64
+//     amplitudes are not positive) is queued for
+//   repair_kernel  (FP64): the FNNLS loop in FP64 to the FP64 KKT point, so
+//     the result is the FP64 KKT point whatever the FP32 search found.
 //
 // Why two kernels: on this GPU an FP64 warp instruction costs the full pipe
 // time whatever the number of active lanes, and FP64 results have long
@@ -308,6 +310,42 @@ __device__ __forceinline__ void residual_gradient(const DevMixed& T, const doubl
   }
 }
 
+// The judge's common path: the FP64 residual r = y - G x (kept for chi2) and
+// an FP32 screen of the KKT test on it. The FP32 gradient w_k = G_k^T r of a
+// column outside m is accurate to (N + 2) 2^-24 sum_i |G_ik r_i| < 2^-19 sum
+// (N <= 10 rounded FMAs, plus the rounding of G and r to FP32); a column passes
+// only if w_k plus that bound stays below tol, so every column the FP64 test
+// w_k >= tol could flag is sent to the FP64 repair, and only columns within
+// that bound of tol are sent there needlessly. Returns true when no column
+// needs the FP64 test.
+template <int N, int K>
+__device__ __forceinline__ bool residual64_screen32(const DevMixed& T, const double* y, const double* x, unsigned m,
+                                                    double* r, float tol) {
+#pragma unroll
+  for (int i = 0; i < N; ++i) r[i] = y[i];
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      if (i >= T.gfz[k]) r[i] = fma(-T.G64[k * N + i], x[k], r[i]);
+  float rf[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) rf[i] = float(r[i]);
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    float w = 0.f, mag = 0.f;
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      if (i >= T.gfz[k]) {
+        w = fmaf(T.G32[k * N + i], rf[i], w);
+        mag = fmaf(fabsf(T.G32[k * N + i]), fabsf(rf[i]), mag);
+      }
+    if (!(m & (1u << k)) && !(fmaf(0x1p-19f, mag, w) < tol)) ok = false;
+  }
+  return ok;
+}
+
 // y = L_R^-1 s in FP64 (packed rows, no division); returns true for a
 // non-finite or non-positive input.
 template <int N>
@@ -383,7 +421,7 @@ __device__ __forceinline__ void judge_repair(const MixedArgs& a, const DevMixed&
   unsigned m = a.ws_mask[ch];
   const unsigned cnt = a.ws_count[ch];
   int adds = int(cnt & 255u), solves = int(cnt >> 8) + 1;
-  int f64 = N * (N + 1) + 6 * N * K;
+  int f64 = N * (N + 1) + 4 * N * K;  // the judge's attempt
   auto s64 = [&](unsigned mm, double* out) {
     solve64_dense<N, K>(T, mm, y, out);
     f64 += 2 * N * K;
@@ -441,12 +479,7 @@ __global__ void __launch_bounds__(128, 6) judge_kernel(const MixedArgs a, int se
 #pragma unroll
   for (int k = 0; k < K; ++k)
     if ((m & (1u << k)) && !pos64(x[k])) ok = false;
-  if (ok) {
-    double wmax;
-    int imax;
-    residual_gradient<N, K>(T, y, x, m, r, wmax, imax);
-    ok = imax < 0 || !(wmax >= a.eps * sig * sig);
-  }
+  if (ok) ok = residual64_screen32<N, K>(T, y, x, m, r, float(a.eps * sig * sig));
   if (!ok) {
     // compaction: append the channel to the repair queue (one atomic per warp)
     const unsigned act = __activemask();
@@ -458,7 +491,7 @@ __global__ void __launch_bounds__(128, 6) judge_kernel(const MixedArgs a, int se
     return;
   }
   write_outputs<N, K>(a, T, ch, x, r, sig, bad, true, int(cnt & 255u), int(cnt >> 8) + 1,
-                      N * (N + 1) + 6 * N * K);
+                      N * (N + 1) + 4 * N * K);
 }
 
 // Channels the judge queued, in full warps: an FP64 warp instruction costs the

@@ -237,10 +237,10 @@ struct InferSmem {
 // GELU, packed as the BF16 A fragment of the next layer's k16 slice.
 __device__ __forceinline__ void gelu_pack(const float (&c0)[4], const float (&c1)[4], const float* bias, int col0,
                                           uint32_t (&h)[4]) {
-  h[0] = pack_bf16(gelu(c0[0] + bias[col0]), gelu(c0[1] + bias[col0 + 1]));
-  h[1] = pack_bf16(gelu(c0[2] + bias[col0]), gelu(c0[3] + bias[col0 + 1]));
-  h[2] = pack_bf16(gelu(c1[0] + bias[col0 + 8]), gelu(c1[1] + bias[col0 + 9]));
-  h[3] = pack_bf16(gelu(c1[2] + bias[col0 + 8]), gelu(c1[3] + bias[col0 + 9]));
+  h[0] = pack_bf16(gelu_fast(c0[0] + bias[col0]), gelu_fast(c0[1] + bias[col0 + 1]));
+  h[1] = pack_bf16(gelu_fast(c0[2] + bias[col0]), gelu_fast(c0[3] + bias[col0 + 1]));
+  h[2] = pack_bf16(gelu_fast(c1[0] + bias[col0 + 8]), gelu_fast(c1[1] + bias[col0 + 9]));
+  h[3] = pack_bf16(gelu_fast(c1[2] + bias[col0 + 8]), gelu_fast(c1[3] + bias[col0 + 9]));
 }
 
 // The MLP of the warp's 32 rows of S.X into S.O. The m16n8 accumulators of a
