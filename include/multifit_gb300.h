@@ -120,7 +120,9 @@ typedef struct mf_options {
   int32_t warm_start;     /* enum mf_warm */
   int32_t compute_errors; /* 1: MINOS-like in-time uncertainty (DoFit, PulseChiSqSNNLS.cpp:75-146) */
   int32_t block_size;     /* threads per block; 0 = tuned default */
-  int32_t blocks_per_sm;  /* persistent schedule: resident blocks per SM; 0 = tuned default */
+  int32_t blocks_per_sm;  /* persistent schedule: cap on resident blocks per SM; 0 = the occupancy limit */
+  int32_t channels_per_warp; /* persistent schedule, FP32 search: 1, 2, 4, 8 or 32 channels per warp
+                                (32 / that many lanes per channel); 0 = tuned (mf_autotune) or 32 */
 } mf_options;
 
 /* A batch of channels. Every pointer is a DEVICE pointer for mf_fit and a
@@ -190,6 +192,23 @@ int mf_fit_count_flops(mf_context* ctx, const mf_batch* batch, const mf_options*
 #define MF_NOALLOC_MAX_CHANNELS 131072
 int mf_fit_noalloc(mf_context* ctx, const mf_batch* batch, const mf_options* opt, void* stream);
 
+/* Autotuner of the persistent schedule (the uneven ECAL/HCAL batches). One
+ * point of the sweep: */
+typedef struct mf_tune_point {
+  int32_t block_size;        /* threads per block of the FP32 search: 64, 128, 256, 512 */
+  int32_t channels_per_warp; /* channels a warp of the FP32 search fits at once: 1, 2, 4, 8, 32 */
+  double ms;                 /* best of 3 timed fits of the batch (CUDA events), after one warm-up */
+} mf_tune_point;
+#define MF_TUNE_POINTS 20
+/* Sweeps block_size x channels_per_warp for opt (precision MF_PREC_MIXED, any
+ * warm start) on the given device batch (its outputs are overwritten), keeps
+ * the fastest in the context (used when a persistent-schedule fit leaves
+ * block_size / channels_per_warp at 0) and writes up to max_points points.
+ * Synchronous. The reference has no tuner (its launch shape is fixed:
+ * multifit_gpu/src/PulseChiSqSNNLSWrapper.cu:29-31, 256 threads per block). */
+int mf_autotune(mf_context* ctx, const mf_batch* batch, const mf_options* opt, mf_tune_point* points,
+                int max_points, int* n_points);
+
 /* Per-kernel timing of fits (instrumentation, off by default). The GB300
  * counterpart of the reference's -DPROFILE timing around the batch (VTune
  * __itt_resume/__itt_pause and std::chrono, multifit_cpu/src/multifit.cpp:
@@ -198,10 +217,11 @@ int mf_fit_noalloc(mf_context* ctx, const mf_batch* batch, const mf_options* opt
 enum mf_kernel_kind {
   MF_K_FIT_FP64 = 0,  /* fit_fp64_kernel: the plain FP64 fit */
   MF_K_MLP_INFER = 1, /* mlp_infer_kernel: warm-start predictions */
-  MF_K_SEARCH = 2,    /* search_kernel: FP32 active-set search */
-  MF_K_JUDGE = 3,     /* judge_kernel: FP64 solve, residual, KKT test, chi2 */
-  MF_K_REPAIR = 4,    /* repair_kernel: FP64 FNNLS of the channels the judge queued */
-  MF_K_COUNT = 5
+  MF_K_SEARCH = 2,    /* search_kernel / search_persist: FP32 active-set search */
+  MF_K_JUDGE = 3,     /* judge_kernel / judge_persist: FP64 solve, residual, KKT test, chi2 */
+  MF_K_REPAIR = 4,    /* repair_kernel / repair_persist: FP64 FNNLS of the channels the judge queued */
+  MF_K_PARTITION = 5, /* partition_kernel: per-set channel lists of the persistent schedule */
+  MF_K_COUNT = 6
 };
 /* enable != 0 creates the context's event pool (and clears it); 0 frees it. */
 int mf_profile(mf_context* ctx, int enable);

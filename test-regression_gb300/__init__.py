@@ -65,6 +65,7 @@ class MfOptions(C.Structure):
         ("compute_errors", C.c_int32),
         ("block_size", C.c_int32),
         ("blocks_per_sm", C.c_int32),
+        ("channels_per_warp", C.c_int32),
     ]
 
 
@@ -84,6 +85,13 @@ class MfBatch(C.Structure):
         ("status", C.c_void_p),
         ("iters", C.c_void_p),
     ]
+
+
+class MfTunePoint(C.Structure):
+    _fields_ = [("block_size", C.c_int32), ("channels_per_warp", C.c_int32), ("ms", C.c_double)]
+
+
+TUNE_POINTS = 20  # MF_TUNE_POINTS
 
 
 class MfSynthParams(C.Structure):
@@ -106,7 +114,8 @@ class MfMlpTrainParams(C.Structure):
 # Exported symbols and their signatures: (name, restype, argtypes).
 NOALLOC_MAX_CHANNELS = 131072  # MF_NOALLOC_MAX_CHANNELS
 # mf_kernel_kind: the kernels mf_profile times
-KERNEL_KINDS = ("fit_fp64_kernel", "mlp_infer_kernel", "search_kernel", "judge_kernel", "repair_kernel")
+KERNEL_KINDS = ("fit_fp64_kernel", "mlp_infer_kernel", "search_kernel", "judge_kernel", "repair_kernel",
+                "partition_kernel")
 
 SIGNATURES = [
     ("mf_abi_version", C.c_int, []),
@@ -120,6 +129,8 @@ SIGNATURES = [
     ("mf_fit_count_flops", C.c_int, [C.c_void_p, C.POINTER(MfBatch), C.POINTER(MfOptions), C.c_void_p, C.c_void_p]),
     ("mf_fit_host", C.c_int, [C.c_void_p, C.POINTER(MfBatch), C.POINTER(MfOptions)]),
     ("mf_fit_noalloc", C.c_int, [C.c_void_p, C.POINTER(MfBatch), C.POINTER(MfOptions), C.c_void_p]),
+    ("mf_autotune", C.c_int, [C.c_void_p, C.POINTER(MfBatch), C.POINTER(MfOptions), C.c_void_p, C.c_int,
+                              C.POINTER(C.c_int)]),
     ("mf_profile", C.c_int, [C.c_void_p, C.c_int]),
     ("mf_profile_read", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     ("mf_build_pulse_matrix", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
@@ -334,6 +345,16 @@ class Engine:
         """mf_fit_noalloc on device pointers; returns the return code (the
         caller checks it: oversize batches are an expected MF_EINVAL)."""
         return int(self.lib.mf_fit_noalloc(self.h, C.byref(batch), C.byref(options), stream))
+
+    def autotune(self, batch: MfBatch, options: MfOptions) -> list:
+        """mf_autotune: sweep of the persistent schedule's launch shape on this
+        device batch; returns [(block_size, channels_per_warp, ms)], the
+        fastest being kept by the context."""
+        pts = (MfTunePoint * TUNE_POINTS)()
+        n = C.c_int(0)
+        _check(self.lib.mf_autotune(self.h, C.byref(batch), C.byref(options), pts, TUNE_POINTS, C.byref(n)),
+               "mf_autotune")
+        return [(p.block_size, p.channels_per_warp, p.ms) for p in pts[: n.value]]
 
     def profile(self, enable: bool = True):
         """mf_profile: start (or stop) per-kernel launch timing of fits."""

@@ -53,6 +53,14 @@ int make_dev_conditions(const mf_conditions& c, DevConditions* d) {
 
 using namespace mfgb;
 
+// The launch arguments a captured persistent-schedule graph was built from;
+// a call with byte-identical arguments replays the graph.
+struct GraphKey {
+  MixedArgs m;
+  MlpInferArgs ia;
+  int warm, block, lanes;
+};
+
 struct mf_context {
   int device = 0;
   DevConditions cond[MF_MAX_CTYPES];
@@ -71,6 +79,15 @@ struct mf_context {
   float* ws_x = nullptr;
   int* ws_queue = nullptr;
   unsigned* ws_qcount = nullptr;
+  // persistent schedule: per-set channel lists and counters; tuned launch shape
+  int* ws_list = nullptr;
+  unsigned* ws_sched = nullptr;
+  int tuned_block = 0;  // mf_autotune result (0: not tuned, use 128)
+  int tuned_lanes = 0;  // lanes per channel of the FP32 search (0: not tuned, use 1)
+  // CUDA graph of the last persistent-schedule fit (captured on cap_stream)
+  cudaStream_t cap_stream = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  GraphKey graph_key;
   // staging area for mf_fit_host
   int64_t cap = 0;
   int cap_ss = 0, cap_as = 0;
@@ -100,6 +117,10 @@ int check_options(const mf_options* o) {
   if (o->warm_start != MF_WARM_NONE && o->warm_start != MF_WARM_MLP) return MF_EINVAL;
   if (o->nnls_start != MF_START_REFERENCE && o->nnls_start != MF_START_SUPPORT) return MF_EINVAL;
   if (o->block_size < 0 || o->block_size > 1024 || (o->block_size % 32)) return MF_EINVAL;
+  if (o->blocks_per_sm < 0) return MF_EINVAL;
+  const int cpw = o->channels_per_warp;
+  if (cpw != 0 && cpw != 1 && cpw != 2 && cpw != 4 && cpw != 8 && cpw != 32) return MF_EINVAL;
+  if (o->schedule == MF_SCHED_PERSISTENT && o->block_size > 512) return MF_EINVAL;
   return MF_OK;
 }
 
@@ -145,7 +166,10 @@ int fill_args(mf_context* ctx, const mf_batch* b, const mf_options* o, FitArgs* 
 void fill_dev_mixed(const mf_context* c, int t, DevMixed* m);
 
 int dispatch_mixed(mf_context* c, const FitArgs& a, const mf_options* o, cudaStream_t s) {
-  if (o->compute_errors || o->schedule != MF_SCHED_GRID) return MF_EUNSUPPORTED;
+  if (o->compute_errors) return MF_EUNSUPPORTED;
+  const bool persistent = o->schedule == MF_SCHED_PERSISTENT;
+  const int block = o->block_size ? o->block_size : (persistent && c->tuned_block ? c->tuned_block : 128);
+  const int lanes = o->channels_per_warp ? 32 / o->channels_per_warp : (c->tuned_lanes ? c->tuned_lanes : 1);
   const bool warm = o->warm_start == MF_WARM_MLP;
   if (warm && (!c->mlp.trained || !c->tab_ok[c->mlp.set] || c->tab[c->mlp.set].N != 10)) return MF_ENOTRAINED;
   MixedArgs m;
@@ -180,8 +204,12 @@ int dispatch_mixed(mf_context* c, const FitArgs& a, const mf_options* o, cudaStr
   m.ws_queue = c->ws_queue;
   m.ws_qcount = c->ws_qcount;
   m.sms = c->sms;
-  if (!m.ws_mask) return MF_ENOMEM;
+  m.ws_list = c->ws_list;
+  m.ws_sched = c->ws_sched;
+  m.blocks_per_sm = o->blocks_per_sm;
+  if (!m.ws_mask || !m.ws_list) return MF_ENOMEM;
   MlpInferArgs ia;
+  std::memset(&ia, 0, sizeof(ia));
   if (warm) {
     fill_infer_args(c->mlp, c->tab[c->mlp.set], 0, &ia);
     ia.sample_stride = a.sample_stride;
@@ -190,6 +218,8 @@ int dispatch_mixed(mf_context* c, const FitArgs& a, const mf_options* o, cudaStr
     ia.warm_stride = 10;
   }
   const int64_t cap = warm && MlpState::kChunk < MIXED_CHUNK ? MlpState::kChunk : MIXED_CHUNK;
+  // every launch of the fit, chunk by chunk, on stream st
+  auto enqueue = [&](cudaStream_t st, LaunchTimer* tm) -> cudaError_t {
   for (int64_t off = 0; off < a.n; off += cap) {
     const int64_t cnt = a.n - off < cap ? a.n - off : cap;
     MixedArgs mc = m;
@@ -207,22 +237,63 @@ int dispatch_mixed(mf_context* c, const FitArgs& a, const mf_options* o, cudaStr
     cudaError_t e = cudaSuccess;
     if (warm) {
       // learned warm start: predictions of this chunk into the network's workspace
-      ia.n = cnt;
-      ia.samples = mc.samples;
-      ia.pederr = mc.pederr;
-      ia.ctype = mc.ctype;
+      MlpInferArgs ic = ia;
+      ic.n = cnt;
+      ic.samples = mc.samples;
+      ic.pederr = mc.pederr;
+      ic.ctype = mc.ctype;
       mc.warm_mask = c->mlp.warm_mask;
       mc.warm_amp = c->mlp.warm_amp;
       mc.warm_stride = 10;
       mc.warm_set = c->mlp.set;
-      c->timer.mark(MF_K_MLP_INFER, s);
-      e = launch_mlp_infer(ia, c->sms, s);
+      if (tm) tm->mark(MF_K_MLP_INFER, st);
+      e = launch_mlp_infer(ic, c->sms, st);
     }
-    if (e == cudaSuccess) e = launch_fit_mixed(mc, o->block_size, s, &c->timer);
-    if (e != cudaSuccess) {
-      set_last_error("mixed fit launch", e);
-      return MF_ECUDA;
+    if (e == cudaSuccess) {
+      e = persistent ? launch_fit_mixed_persistent(mc, block, lanes, st, tm)
+                     : launch_fit_mixed(mc, o->block_size, st, tm);
     }
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+  };
+  cudaError_t e = cudaSuccess;
+  if (!persistent || c->timer.ev) {
+    // grid schedule, or per-launch timing requested: launch directly
+    e = enqueue(s, &c->timer);
+  } else {
+    // persistent schedule: replay the CUDA graph of this exact launch sequence,
+    // capturing (and instantiating) it first when the arguments changed
+    GraphKey key;
+    std::memset(&key, 0, sizeof(key));
+    key.m = m;
+    key.ia = ia;
+    key.warm = warm;
+    key.block = block;
+    key.lanes = lanes;
+    if (!c->graph_exec || std::memcmp(&key, &c->graph_key, sizeof(key)) != 0) {
+      if (!c->cap_stream) e = cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking);
+      cudaGraph_t g = nullptr;
+      if (e == cudaSuccess) e = cudaStreamBeginCapture(c->cap_stream, cudaStreamCaptureModeThreadLocal);
+      if (e == cudaSuccess) {
+        const cudaError_t le = enqueue(c->cap_stream, nullptr);
+        e = cudaStreamEndCapture(c->cap_stream, &g);
+        if (le != cudaSuccess) e = le;
+      }
+      cudaGraphExec_t x = nullptr;
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&x, g, 0);
+      if (g) cudaGraphDestroy(g);
+      if (e == cudaSuccess) {
+        if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+        c->graph_exec = x;
+        c->graph_key = key;
+      }
+    }
+    if (e == cudaSuccess) e = cudaGraphLaunch(c->graph_exec, s);
+  }
+  if (e != cudaSuccess) {
+    set_last_error("mixed fit launch", e);
+    return MF_ECUDA;
   }
   return MF_OK;
 }
@@ -310,6 +381,8 @@ int upload_tables(mf_context* c, int t) {
     if (e == cudaSuccess) e = cudaMalloc(&c->ws_x, sizeof(float) * MIXED_CHUNK * KMAX);
     if (e == cudaSuccess) e = cudaMalloc(&c->ws_queue, sizeof(int) * MIXED_CHUNK);
     if (e == cudaSuccess) e = cudaMalloc(&c->ws_qcount, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMalloc(&c->ws_list, sizeof(int) * MIXED_CHUNK * MF_MAX_CTYPES);
+    if (e == cudaSuccess) e = cudaMalloc(&c->ws_sched, sizeof(unsigned) * SCHED_WORDS);
   }
   if (e != cudaSuccess) {
     set_last_error("table upload", e);
@@ -440,9 +513,68 @@ void mf_destroy(mf_context* c) {
   cudaFree(c->ws_x);
   cudaFree(c->ws_queue);
   cudaFree(c->ws_qcount);
+  cudaFree(c->ws_list);
+  cudaFree(c->ws_sched);
   destroy_timer(c->timer);
+  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+  if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
+}
+
+int mf_autotune(mf_context* c, const mf_batch* b, const mf_options* o, mf_tune_point* points, int max_points,
+                int* n_points) {
+  if (n_points) *n_points = 0;
+  FitArgs a;
+  int rc = fill_args(c, b, o, &a);
+  if (rc) return rc;
+  if (o->precision != MF_PREC_MIXED) return MF_EUNSUPPORTED;
+  if (b->n == 0 || max_points < 0 || (max_points > 0 && !points)) return MF_EINVAL;
+  static const int blocks[] = {64, 128, 256, 512};
+  static const int cpws[] = {32, 8, 4, 2, 1};
+  cudaStream_t s = c->stream;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  int best_block = 0, best_cpw = 0, n = 0;
+  double best = 0.;
+  for (int bi = 0; bi < 4 && e == cudaSuccess && rc == MF_OK; ++bi) {
+    for (int ci = 0; ci < 5 && e == cudaSuccess && rc == MF_OK; ++ci) {
+      mf_options t = *o;
+      t.schedule = MF_SCHED_PERSISTENT;
+      t.block_size = blocks[bi];
+      t.channels_per_warp = cpws[ci];
+      double ms_best = 0.;
+      for (int rep = 0; rep < 4 && rc == MF_OK && e == cudaSuccess; ++rep) {
+        e = cudaEventRecord(e0, s);
+        if (e == cudaSuccess) rc = dispatch(c, a, &t, s, false);
+        if (rc == MF_OK && e == cudaSuccess) e = cudaEventRecord(e1, s);
+        if (rc == MF_OK && e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (rc == MF_OK && e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && (rep == 1 || ms < ms_best)) ms_best = ms;  // rep 0 is the warm-up (and graph capture)
+      }
+      if (rc != MF_OK || e != cudaSuccess) break;
+      if (n < max_points) points[n] = mf_tune_point{blocks[bi], cpws[ci], ms_best};
+      ++n;
+      if (best_block == 0 || ms_best < best) {
+        best = ms_best;
+        best_block = blocks[bi];
+        best_cpw = cpws[ci];
+      }
+    }
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (rc != MF_OK) return rc;
+  if (e != cudaSuccess) {
+    set_last_error("mf_autotune", e);
+    return MF_ECUDA;
+  }
+  c->tuned_block = best_block;
+  c->tuned_lanes = 32 / best_cpw;
+  if (n_points) *n_points = n < max_points ? n : max_points;
+  return MF_OK;
 }
 
 int mf_profile(mf_context* c, int enable) {

@@ -149,10 +149,20 @@ struct MixedArgs {
   int* ws_queue;           // channels the FP64 judge hands to the repair kernel
   unsigned* ws_qcount;     // their number (zeroed by the search launch)
   int sms;
+  // persistent schedule (fit_sched.cu): per-set channel lists [MF_MAX_CTYPES][MIXED_CHUNK]
+  // and SCHED_WORDS counters (list sizes, work counters, repair-queue sizes)
+  int* ws_list;
+  unsigned* ws_sched;
+  int blocks_per_sm;       // cap on resident blocks per SM (0: the occupancy limit)
 };
+constexpr int SCHED_WORDS = 16;
 // Channels per chunk of a mixed fit (the size of the hand-off workspace).
 constexpr int64_t MIXED_CHUNK = int64_t(1) << 21;
 cudaError_t launch_fit_mixed(const MixedArgs& a, int block, cudaStream_t s, LaunchTimer* tm = nullptr);
+// Persistent work-stealing schedule: per-set channel lists, then per set the
+// FP32 search (block threads, `lanes` lanes per channel), judge and repair.
+cudaError_t launch_fit_mixed_persistent(const MixedArgs& a, int block, int lanes, cudaStream_t s,
+                                        LaunchTimer* tm = nullptr);
 
 
 

@@ -1,0 +1,455 @@
+// Device code shared by the grid (fit_mixed.cu) and persistent (fit_sched.cu)
+// schedules of the mixed-precision multifit: the passive-set solves from the
+// operator tables, the FNNLS inner loop, and the per-channel bodies of the FP32
+// search, the FP64 judge and the FP64 repair. Both schedules run the same
+// per-channel arithmetic, so their results are identical.
+#pragma once
+#include <cfloat>
+
+#include "mf_internal.h"
+
+namespace mfgb {
+namespace {
+
+
+// Passive-set solves from the operator table (tables.cu): rows of the set's
+// columns, p x N packed at offset[m]. The loops are predicated on the mask, so
+// every lane issues the same instruction stream; only the addresses differ.
+template <int N, int K>
+__device__ __forceinline__ void solve32(const DevMixed& T, unsigned m, const float* y32, float* s) {
+  const float* P = T.pinv32 + __ldg(T.offset + m);
+  int r = 0;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    float acc = 0.f;
+    if (m & (1u << k)) {
+      const float2* row = reinterpret_cast<const float2*>(P + r * N);
+#pragma unroll
+      for (int q = 0; q < N / 2; ++q) {
+        const float2 v = __ldg(row + q);
+        acc = fmaf(v.x, y32[2 * q], acc);
+        acc = fmaf(v.y, y32[2 * q + 1], acc);
+      }
+      ++r;
+    }
+    s[k] = acc;
+  }
+}
+
+template <int N, int K>
+__device__ __forceinline__ void solve64(const DevMixed& T, unsigned m, const double* y, double* s) {
+  const double* P = T.pinv64 + __ldg(T.offset + m);
+  int r = 0;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    double acc = 0.;
+    if (m & (1u << k)) {
+      const double2* row = reinterpret_cast<const double2*>(P + r * N);
+#pragma unroll
+      for (int q = 0; q < N / 2; ++q) {
+        const double2 v = __ldg(row + q);
+        acc = fma(v.x, y[2 * q], acc);
+        acc = fma(v.y, y[2 * q + 1], acc);
+      }
+      ++r;
+    }
+    s[k] = acc;
+  }
+}
+
+// The same solve without branches: every lane computes all K rows, rows of
+// columns outside the set read the table's zero row. On this GPU an FP64 warp
+// instruction costs the full pipe time whatever the number of active lanes, so
+// the FP64 judge keeps all 32 lanes busy on every instruction.
+template <int N, int K>
+__device__ __forceinline__ void solve64_dense(const DevMixed& T, unsigned m, const double* y, double* s) {
+  const double* P = T.pinv64 + __ldg(T.offset + m);
+  const double* Z = T.pinv64 + T.zero_row;
+  int r = 0;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const bool in = (m >> k) & 1u;
+    const double2* row = reinterpret_cast<const double2*>(in ? P + r * N : Z);
+    r += in ? 1 : 0;
+    double acc = 0.;
+#pragma unroll
+    for (int q = 0; q < N / 2; ++q) {
+      const double2 v = __ldg(row + q);
+      acc = fma(v.x, y[2 * q], acc);
+      acc = fma(v.y, y[2 * q + 1], acc);
+    }
+    s[k] = acc;
+  }
+}
+
+// x > 0 for a finite double, decided on its bit pattern (integer ops, which
+// keeps the compare off the FP64 pipe)
+__device__ __forceinline__ bool pos64(double v) {
+  const int hi = __double2hiint(v);
+  const unsigned lo = unsigned(__double2loint(v));
+  return (hi > 0 || (hi == 0 && lo != 0u)) && hi < 0x7ff00000;
+}
+
+// FNNLS inner loop (nnls/src/inplace_fnnls.cu:175-230) on a bit mask: solve
+// the passive set; if some component is not positive, step from the feasible
+// x towards s until the first one hits zero and drop it. Returns the solves.
+template <int K, typename F, typename Solve>
+__device__ __forceinline__ int inner_loop(unsigned& m, F* x, Solve solve) {
+  int solves = 0;
+  for (int guard = 0; guard <= K && m; ++guard) {
+    F s[K];
+    solve(m, s);
+    ++solves;
+    bool allpos = true;
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+      if ((m & (1u << k)) && !(s[k] > F(0))) allpos = false;
+    if (allpos) {
+#pragma unroll
+      for (int k = 0; k < K; ++k)
+        if (m & (1u << k)) x[k] = s[k];
+      return solves;
+    }
+    F alpha = F(3.0e38);
+    int ai = -1;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      if ((m & (1u << k)) && !(s[k] > F(0))) {
+        const F ratio = x[k] / (x[k] - s[k]);
+        if (ai < 0 || ratio < alpha) {
+          alpha = ratio;
+          ai = k;
+        }
+      }
+    }
+    if (!(alpha >= F(0))) alpha = F(0);  // 0/0 from a column that entered at zero
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+      if (m & (1u << k)) x[k] = x[k] + alpha * (s[k] - x[k]);
+    x[ai] = F(0);
+    m &= ~(1u << ai);
+  }
+  return solves;
+}
+
+// c = G^T y in FP32 and sum_i |G_ik y_i| (its rounding-error scale)
+template <int N, int K>
+__device__ __forceinline__ void gram_rhs32(const DevMixed& T, const float* y32, float* c, float* cmag) {
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    float acc = 0.f, mag = 0.f;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      acc = fmaf(T.G32[k * N + i], y32[i], acc);
+      mag = fmaf(fabsf(T.G32[k * N + i]), fabsf(y32[i]), mag);
+    }
+    c[k] = acc;
+    if (cmag) cmag[k] = mag;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP32 active-set search
+// ---------------------------------------------------------------------------
+// The FP32 search of channel ch (one lane): writes the hand-off (passive mask,
+// add and solve counts, FP32 amplitudes) for the FP64 judge.
+template <int N, int K, bool WARM>
+__device__ __forceinline__ void search_body(const MixedArgs& a, const DevMixed& T, int64_t ch) {
+  const double* in = a.samples + ch * a.sample_stride;
+  float sf[N], y32[N], ynorm2 = 0.f;
+#pragma unroll
+  for (int i = 0; i < N; ++i) sf[i] = float(in[i]);
+  {
+    int w = 0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      float acc = 0.f;
+#pragma unroll
+      for (int j = 0; j <= i; ++j) acc = fmaf(T.W32[w + j], sf[j], acc);
+      w += i + 1;
+      y32[i] = acc;
+      ynorm2 = fmaf(acc, acc, ynorm2);
+    }
+  }
+  float c32[K];
+  gram_rhs32<N, K>(T, y32, c32, nullptr);
+  const float ynorm = sqrtf(ynorm2);
+  const unsigned full = (1u << K) - 1u;
+  unsigned m = 0;
+  float x32[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) x32[k] = 0.f;
+  int adds = 0, solves = 0;
+  auto s32 = [&](unsigned mm, float* out) { solve32<N, K>(T, mm, y32, out); };
+  if (WARM) {
+    m = unsigned(a.warm_mask[ch]) & full;
+    const float* wa = a.warm_amp + ch * a.warm_stride;
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+      if (m & (1u << k)) x32[k] = fmaxf(wa[k], 1e-30f);
+    if (m) solves += inner_loop<K>(m, x32, s32);
+  }
+  for (int it = 0; it < a.max_iter32; ++it) {
+    float wmax = 0.f;
+    int imax = -1;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      if (m & (1u << k)) continue;
+      float acc = c32[k];
+#pragma unroll
+      for (int j = 0; j < K; ++j) acc = fmaf(-T.H32[k * KMAX + j], x32[j], acc);
+      // relative stop: w_k against |G_k| |y| at the FP32 resolution
+      const float tol = a.tol32 * T.gnorm32[k] * ynorm;
+      if (acc > tol && (imax < 0 || acc > wmax)) {
+        wmax = acc;
+        imax = k;
+      }
+    }
+    if (imax < 0) break;
+    m |= 1u << imax;
+    ++adds;
+    solves += inner_loop<K>(m, x32, s32);
+  }
+  // Columns whose gradient FP32 cannot prove negative (within its rounding
+  // error of zero) may still carry a positive FP64 gradient, which the FP64
+  // judge's absolute threshold eps * pederr^2 would add one at a time. Add
+  // them here as a batch; the inner loop drops those that come out negative.
+  {
+    float cmag[K], cc[K];
+    gram_rhs32<N, K>(T, y32, cc, cmag);
+    unsigned amb = 0;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      if (m & (1u << k)) continue;
+      float acc = c32[k], mag = cmag[k];
+#pragma unroll
+      for (int j = 0; j < K; ++j) {
+        const float hx = T.H32[k * KMAX + j] * x32[j];
+        acc -= hx;
+        mag += fabsf(hx);
+      }
+      if (acc >= -4e-6f * mag) amb |= 1u << k;
+    }
+    if (amb) {
+      m |= amb;
+      adds += __popc(amb);
+      solves += inner_loop<K>(m, x32, s32);
+    }
+  }
+  a.ws_mask[ch] = uint16_t(m);
+  a.ws_count[ch] = uint16_t((adds < 255 ? adds : 255) | ((solves < 255 ? solves : 255) << 8));
+  float* wx = a.ws_x + ch * K;
+#pragma unroll
+  for (int k = 0; k < K; ++k) wx[k] = x32[k];
+}
+
+// ---------------------------------------------------------------------------
+// FP64 judge
+// ---------------------------------------------------------------------------
+
+// FP64 residual r = y - G x (dense; G's structural zeros are skipped
+// uniformly) and the index and value of the largest gradient w = G^T r over
+// the columns outside the passive set m (and, with viol, the mask of those at
+// or above tol).
+template <int N, int K>
+__device__ __forceinline__ void residual_gradient(const DevMixed& T, const double* y, const double* x, unsigned m,
+                                                  double* r, double& wmax, int& imax, double tol = 0.,
+                                                  unsigned* viol = nullptr) {
+#pragma unroll
+  for (int i = 0; i < N; ++i) r[i] = y[i];
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      if (i >= T.gfz[k]) r[i] = fma(-T.G64[k * N + i], x[k], r[i]);
+  wmax = 0.;
+  imax = -1;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    double w = 0.;
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      if (i >= T.gfz[k]) w = fma(T.G64[k * N + i], r[i], w);
+    const bool cand = !(m & (1u << k)) && (imax < 0 || w > wmax);
+    wmax = cand ? w : wmax;
+    imax = cand ? k : imax;
+    if (viol && !(m & (1u << k)) && w >= tol) *viol |= 1u << k;
+  }
+}
+
+// The judge's common path: the FP64 residual r = y - G x (kept for chi2) and
+// an FP32 screen of the KKT test on it. The FP32 gradient w_k = G_k^T r of a
+// column outside m is accurate to (N + 2) 2^-24 sum_i |G_ik r_i| < 2^-19 sum
+// (N <= 10 rounded FMAs, plus the rounding of G and r to FP32); a column passes
+// only if w_k plus that bound stays below tol, so every column the FP64 test
+// w_k >= tol could flag is sent to the FP64 repair, and only columns within
+// that bound of tol are sent there needlessly. Returns true when no column
+// needs the FP64 test.
+template <int N, int K>
+__device__ __forceinline__ bool residual64_screen32(const DevMixed& T, const double* y, const double* x, unsigned m,
+                                                    double* r, float tol) {
+#pragma unroll
+  for (int i = 0; i < N; ++i) r[i] = y[i];
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      if (i >= T.gfz[k]) r[i] = fma(-T.G64[k * N + i], x[k], r[i]);
+  float rf[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) rf[i] = float(r[i]);
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    float w = 0.f, mag = 0.f;
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      if (i >= T.gfz[k]) {
+        w = fmaf(T.G32[k * N + i], rf[i], w);
+        mag = fmaf(fabsf(T.G32[k * N + i]), fabsf(rf[i]), mag);
+      }
+    if (!(m & (1u << k)) && !(fmaf(0x1p-19f, mag, w) < tol)) ok = false;
+  }
+  return ok;
+}
+
+// y = L_R^-1 s in FP64 (packed rows, no division); returns true for a
+// non-finite or non-positive input.
+template <int N>
+__device__ __forceinline__ bool whiten64(const MixedArgs& a, const DevMixed& T, int64_t ch, double* y, double& sig) {
+  const double* in = a.samples + ch * a.sample_stride;
+  sig = a.pederr[ch];
+  bool bad = !isfinite(sig) || !(sig > 0.);
+  double s[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    s[i] = in[i];
+    bad = bad || !isfinite(s[i]);
+  }
+  int w = 0;
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    double acc = 0.;
+#pragma unroll
+    for (int j = 0; j <= i; ++j) acc = fma(T.W64[w + j], s[j], acc);
+    w += i + 1;
+    y[i] = acc;
+  }
+  return bad;
+}
+
+// Outputs of a judged channel: amplitudes, chi2 from the residual, in-time
+// amplitude, active mask (support of x), status, counters, FP64 flops.
+template <int N, int K>
+__device__ __forceinline__ void write_outputs(const MixedArgs& a, const DevMixed& T, int64_t ch, const double* x,
+                                              const double* r, double sig, bool bad, bool converged, int adds,
+                                              int solves, int f64) {
+  double chi2 = 0.;
+#pragma unroll
+  for (int i = 0; i < N; ++i) chi2 = fma(r[i], r[i], chi2);
+  chi2 = chi2 / (sig * sig);
+  f64 += 2 * N + 2;
+  double* out = a.amplitudes + ch * a.amp_stride;
+  bool finite = isfinite(chi2);
+  uint16_t support = 0;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    out[k] = x[k];
+    finite = finite && isfinite(x[k]);
+    if (pos64(x[k])) support |= uint16_t(1u << k);
+  }
+  for (int k = K; k < a.amp_stride && k < KMAX; ++k) out[k] = 0.;
+  a.chi2[ch] = chi2;
+  if (a.intime) a.intime[ch] = T.intime_col >= 0 ? x[T.intime_col] : 0.;
+  if (a.active_mask) a.active_mask[ch] = support;
+  if (a.status) {
+    uint8_t st = 0;
+    if (!converged) st |= CH_NNLS_MAXITER;
+    if (!finite) st |= CH_NONFINITE;
+    if (bad) st |= CH_BADINPUT;
+    a.status[ch] = st;
+  }
+  if (a.iters) {
+    const int fo = adds < 4095 ? adds : 4095;
+    const int fi = solves < 4095 ? solves : 4095;
+    a.iters[ch] = 1 | (fo << 8) | (fi << 20);
+  }
+  if (a.flops) a.flops[ch] = double(f64);
+}
+
+// The repair path (the FP64 solve on the FP32 set has a non-positive
+// component, or the FP64 KKT test fails), self-contained: the FNNLS loop in
+// FP64 from the FP32 passive set and the feasible FP32 amplitudes, to the FP64
+// KKT point; writes the channel's outputs.
+template <int N, int K>
+__device__ __forceinline__ void judge_repair(const MixedArgs& a, const DevMixed& T, int64_t ch) {
+  double y[N], sig;
+  const bool bad = whiten64<N>(a, T, ch, y, sig);
+  unsigned m = a.ws_mask[ch];
+  const unsigned cnt = a.ws_count[ch];
+  int adds = int(cnt & 255u), solves = int(cnt >> 8) + 1;
+  int f64 = N * (N + 1) + 4 * N * K;  // the judge's attempt
+  auto s64 = [&](unsigned mm, double* out) {
+    solve64_dense<N, K>(T, mm, y, out);
+    f64 += 2 * N * K;
+  };
+  double x[K], r[N];
+  const float* wx = a.ws_x + ch * K;
+#pragma unroll
+  for (int k = 0; k < K; ++k) x[k] = double(wx[k]);
+  solves += inner_loop<K>(m, x, s64);
+  const double tol64 = a.eps * sig * sig;
+  bool converged = false;
+  double wmax;
+  int imax;
+  for (int it = 0; it < a.max_iter64; ++it) {
+    unsigned viol = 0;
+    residual_gradient<N, K>(T, y, x, m, r, wmax, imax, tol64, &viol);
+    f64 += 4 * N * K;
+    if (viol == 0u) {
+      converged = true;
+      break;
+    }
+    // add every violating column at once (the KKT point of this strictly
+    // convex problem is unique, so the order of additions does not matter)
+    m |= viol;
+    adds += __popc(viol);
+    solves += inner_loop<K>(m, x, s64);
+  }
+  if (!converged) residual_gradient<N, K>(T, y, x, m, r, wmax, imax);  // residual of the last state
+  write_outputs<N, K>(a, T, ch, x, r, sig, bad, converged, adds, solves, f64);
+}
+
+// The FP64 judge of channel ch (one lane): writes the outputs, or appends the
+// channel to the repair queue (ws_queue, counted in *qcount).
+template <int N, int K>
+__device__ __forceinline__ void judge_body(const MixedArgs& a, const DevMixed& T, int64_t ch, unsigned* qcount) {
+  double y[N], sig;
+  const bool bad = whiten64<N>(a, T, ch, y, sig);
+  const unsigned m = a.ws_mask[ch];
+  const unsigned cnt = a.ws_count[ch];
+  // common path, straight-line: the FP64 solve on the FP32 passive set, the
+  // residual and gradient, the KKT test max w < eps * pederr^2
+  double x[K], r[N];
+  solve64_dense<N, K>(T, m, y, x);
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+    if ((m & (1u << k)) && !pos64(x[k])) ok = false;
+  if (ok) ok = residual64_screen32<N, K>(T, y, x, m, r, float(a.eps * sig * sig));
+  if (!ok) {
+    // compaction: append the channel to the repair queue (one atomic per warp)
+    const unsigned act = __activemask();
+    const int lane = threadIdx.x & 31, leader = __ffs(act) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(qcount, unsigned(__popc(act)));
+    base = __shfl_sync(act, base, leader);
+    a.ws_queue[base + __popc(act & ((1u << lane) - 1u))] = int(ch);
+    return;
+  }
+  write_outputs<N, K>(a, T, ch, x, r, sig, bad, true, int(cnt & 255u), int(cnt >> 8) + 1,
+                      N * (N + 1) + 4 * N * K);
+}
+
+}  // namespace
+}  // namespace mfgb

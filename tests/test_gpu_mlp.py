@@ -155,3 +155,26 @@ def test_mixed_fp64_flop_counter(mf, cuda):
     # whitening 110 + one FP64 solve + residual + chi2 at least
     assert (f >= 110 + 20 + 22).all() and f.mean() < 2000
     eng.close()
+
+
+def test_inference_matches_cpu_network(mf, cuda, mlp_engine):
+    """mlp_infer_kernel (BF16 mma.sync, FP32 accumulation, GELU through the
+    hardware tanh.approx.f32) against the FP64 checker network with exact tanh
+    and the same BF16 rounding points, on the same BF16 features. The hardware
+    tanh's relative error (<= 2^-10.987) moves a hidden activation by at most
+    2^-12 relative, under half a BF16 ulp (2^-9), so it only flips the rounding
+    of a minority of activations by one ulp: the raw outputs must agree to 2 %
+    of max(1, |output|) per value and 0.2 % on average."""
+    eng = mlp_engine
+    B = 4096
+    db = train_set(mf, cuda, eng, B, seed=41)
+    _, X, _, _ = eng.mlp_gradient(db.batch, mf.mlp_params(epochs=1, batch=B))
+    logits = cuda.zeros((B, 32), dtype=cuda.float32, device="cuda")
+    mask = cuda.zeros(B, dtype=cuda.int16, device="cuda")
+    amp = cuda.zeros((B, 10), dtype=cuda.float32, device="cuda")
+    eng.mlp_predict(db.batch, mask.data_ptr(), amp.data_ptr(), logits.data_ptr())
+    cuda.cuda.synchronize()
+    ref = mo.forward(mo.unflatten(eng.mlp_get_weights()), X.astype(np.float64))["O"]
+    rel = np.abs(logits.cpu().numpy() - ref) / np.maximum(1.0, np.abs(ref))
+    assert rel.max() <= 2e-2, rel.max()
+    assert rel.mean() <= 2e-3, rel.mean()
