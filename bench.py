@@ -166,12 +166,19 @@ FORM_DESC = {
 MLP_FLOPS_PER_CHANNEL = 2 * (12 * 128 + 128 * 128 + 128 * 20)
 
 
-def form_options(mf, args):
+def schedule_of(mf, args, mixed_sets):
+    if args.schedule == "auto":  # persistent work stealing pays for batches of several condition sets
+        return mf.SCHED_PERSISTENT if mixed_sets and args.form != "fp64" else mf.SCHED_GRID
+    return {"grid": mf.SCHED_GRID, "persistent": mf.SCHED_PERSISTENT}[args.schedule]
+
+
+def form_options(mf, args, mixed_sets=False):
     if args.form == "fp64":
         return mf.default_options(max_iter_nnls=args.max_iter, nnls_start=args.start)
+    sched = schedule_of(mf, args, mixed_sets)
     if args.form == "mixed":
-        return mf.default_options(precision=mf.PREC_MIXED, max_iter_nnls=1000)
-    return mf.default_options(precision=mf.PREC_MIXED, warm_start=mf.WARM_MLP, max_iter_nnls=1000)
+        return mf.default_options(precision=mf.PREC_MIXED, max_iter_nnls=1000, schedule=sched)
+    return mf.default_options(precision=mf.PREC_MIXED, warm_start=mf.WARM_MLP, max_iter_nnls=1000, schedule=sched)
 
 
 def train_warm_start(mf, eng, torch, args, rank):
@@ -237,7 +244,7 @@ def run_ours(args, world, rank, local):
     if mixed:
         hcal, _ = mf.synth_conditions(mf.SYNTH_HCAL)
         eng.set_conditions(1, hcal)
-    opt = form_options(mf, args)
+    opt = form_options(mf, args, mixed)
 
     dev = "cuda"
     samples = torch.zeros((n, 10), dtype=torch.float64, device=dev)
@@ -278,6 +285,14 @@ def run_ours(args, world, rank, local):
         form_fp64_flops = float(flops.sum().item())
     del flops
 
+    tune = None
+    if args.autotune and opt.schedule == mf.SCHED_PERSISTENT:
+        t0 = time.perf_counter()
+        pts = eng.autotune(batch, opt)
+        best = min(pts, key=lambda q: q[2])
+        tune = {"seconds": time.perf_counter() - t0, "best": {"block_size": best[0], "channels_per_warp": best[1]},
+                "points_ms": {f"b{q[0]}_cpw{q[1]}": round(q[2], 4) for q in pts}}
+
     def step():
         with torch.cuda.stream(stream):
             flush.zero_()
@@ -305,6 +320,15 @@ def run_ours(args, world, rank, local):
     kernels = eng.profile_read()
     eng.profile(False)
     times = [e0.elapsed_time(e1) for e0, e1 in evs]
+    graph_ms = None
+    if opt.schedule == mf.SCHED_PERSISTENT:
+        # the same steps replayed as the captured CUDA graph (per-kernel timing
+        # off, which is what makes the engine use the graph)
+        step()
+        torch.cuda.synchronize()
+        gev = [step() for _ in range(args.steps)]
+        torch.cuda.synchronize()
+        graph_ms = sum(e0.elapsed_time(e1) for e0, e1 in gev) / len(gev)
     step_ms = sum(times) / len(times)
     step_ms_max = max_over_ranks(step_ms, world, device=dev)
     value = n * world / (step_ms_max * 1e-3)
@@ -459,6 +483,12 @@ def run_ours(args, world, rank, local):
                 "nnls_start": ["reference", "support"][opt.nnls_start] if args.form == "fp64" else "KKT-converged",
                 "l2": "flushed between steps (256 MB write)",
                 "parallelism": f"replicas x{world}",
+                "schedule": ["grid", "persistent work-stealing"][opt.schedule],
+                "launch_shape": {"block_size": opt.block_size or "tuned/default",
+                                 "channels_per_warp": opt.channels_per_warp or "tuned/default"},
+                "autotune": tune,
+                "graph_replay_ms_per_step": graph_ms,
+                "timed_region_launches": "direct (per-kernel CUDA events on)" if graph_ms else "direct",
             },
             "e2e": {"value": n * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "entry": "mf_fit_host (pinned host buffers)"},
@@ -520,6 +550,9 @@ def kernel_rooflines(mf, eng, kernels, args, n, ctype, plain_flops, form_fp64_fl
         elif name == "mlp_infer_kernel":
             work = n * MLP_FLOPS_PER_CHANNEL / per_step
             bound, peak, unit = "tensor", peaks["bf16_tflops"], "TFLOP/s"
+        elif name == "partition_kernel":  # ctype in, channel lists out
+            work = n * (1 + 4) / per_step
+            bound, peak, unit = "hbm", peaks["hbm_gbs"], "GB/s"
         else:  # search_kernel
             work = n * (10 * 8 + 8 + (2 + 40 if warm else 0) + 2 + 2 + 40) / per_step
             bound, peak, unit = "hbm", peaks["hbm_gbs"], "GB/s"
@@ -636,6 +669,11 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--form", choices=["warm", "mixed", "fp64"], default="warm")
+    ap.add_argument("--schedule", choices=["auto", "grid", "persistent"], default="auto",
+                    help="auto: persistent work stealing for workloads of several condition sets "
+                         "(mixed/warm forms), else grid")
+    ap.add_argument("--autotune", action="store_true",
+                    help="sweep the persistent schedule's launch shape on the workload first (untimed)")
     ap.add_argument("--workload", default="", help="default: warm-eval-10m (warm/mixed), ecal-1m-pu2 (fp64)")
     ap.add_argument("--train-channels", type=int, default=0)
     ap.add_argument("--train-epochs", type=int, default=3)

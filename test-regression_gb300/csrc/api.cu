@@ -207,6 +207,7 @@ int dispatch_mixed(mf_context* c, const FitArgs& a, const mf_options* o, cudaStr
   m.ws_list = c->ws_list;
   m.ws_sched = c->ws_sched;
   m.blocks_per_sm = o->blocks_per_sm;
+  m.list_identity = a.ctype == nullptr ? 1 : 0;
   if (!m.ws_mask || !m.ws_list) return MF_ENOMEM;
   MlpInferArgs ia;
   std::memset(&ia, 0, sizeof(ia));

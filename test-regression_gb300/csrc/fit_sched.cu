@@ -9,7 +9,8 @@
 //
 //   partition_kernel  one pass over ctype: per-set channel lists (warp-aggregated
 //                     atomics, one per set present in a warp), out-of-range sets
-//                     flagged BADINPUT;
+//                     flagged BADINPUT (skipped for a batch without ctype, whose
+//                     list is the identity);
 //   search_persist    FP32 search over a set's list, L lanes per channel
 //                     (32 / L channels per warp), each warp taking the next
 //                     32 / L channels from an atomic counter when it is done;
@@ -197,7 +198,7 @@ template <int N, int K, int L, bool WARM>
 __global__ void __launch_bounds__(512) search_persist(const MixedArgs a, int set) {
   constexpr unsigned G = 32 / L;  // channels per warp
   const DevMixed& T = a.tab[set];
-  const unsigned total = a.ws_sched[SCHED_COUNT + set];
+  const unsigned total = a.list_identity ? unsigned(a.n) : a.ws_sched[SCHED_COUNT + set];
   const int* list = a.ws_list + int64_t(set) * MIXED_CHUNK;
   const int lane = threadIdx.x & 31, sub = lane % L;
   const unsigned gmask = L == 32 ? kFull : (((1u << L) - 1u) << (lane - sub));
@@ -206,8 +207,9 @@ __global__ void __launch_bounds__(512) search_persist(const MixedArgs a, int set
     if (base >= total) break;
     const unsigned i = base + unsigned(lane / L);
     if (i < total) {
-      if constexpr (L == 1) search_body<N, K, WARM>(a, T, int64_t(list[i]));
-      else search_body_coop<N, K, L, WARM>(a, T, int64_t(list[i]), sub, gmask);
+      const int64_t ch = a.list_identity ? int64_t(i) : int64_t(list[i]);
+      if constexpr (L == 1) search_body<N, K, WARM>(a, T, ch);
+      else search_body_coop<N, K, L, WARM>(a, T, ch, sub, gmask);
     }
   }
 }
@@ -215,14 +217,17 @@ __global__ void __launch_bounds__(512) search_persist(const MixedArgs a, int set
 template <int N, int K>
 __global__ void __launch_bounds__(128, 6) judge_persist(const MixedArgs a, int set) {
   const DevMixed& T = a.tab[set];
-  const unsigned total = a.ws_sched[SCHED_COUNT + set];
+  const unsigned total = a.list_identity ? unsigned(a.n) : a.ws_sched[SCHED_COUNT + set];
   const int* list = a.ws_list + int64_t(set) * MIXED_CHUNK;
   const int lane = threadIdx.x & 31;
   for (;;) {
     const unsigned base = steal(a.ws_sched + SCHED_STEAL + set * 3 + 1, 32u);
     if (base >= total) break;
     const unsigned i = base + unsigned(lane);
-    if (i < total) judge_body<N, K>(a, T, int64_t(list[i]), a.ws_sched + SCHED_QUEUE + set);
+    if (i < total) {
+      const int64_t ch = a.list_identity ? int64_t(i) : int64_t(list[i]);
+      judge_body<N, K>(a, T, ch, a.ws_sched + SCHED_QUEUE + set);
+    }
   }
 }
 
@@ -302,9 +307,11 @@ cudaError_t launch_fit_mixed_persistent(const MixedArgs& a, int block, int lanes
   if (block % 32 || block > 512 || !a.ws_list || !a.ws_sched) return cudaErrorInvalidValue;
   cudaError_t e = cudaMemsetAsync(a.ws_sched, 0, sizeof(unsigned) * SCHED_WORDS, s);
   if (e != cudaSuccess) return e;
-  if (tm) tm->mark(MF_K_PARTITION, s);
-  partition_kernel<<<wave(partition_kernel, 256, a), 256, 0, s>>>(a);
-  e = cudaGetLastError();
+  if (!a.list_identity) {
+    if (tm) tm->mark(MF_K_PARTITION, s);
+    partition_kernel<<<wave(partition_kernel, 256, a), 256, 0, s>>>(a);
+    e = cudaGetLastError();
+  }
   for (int t = 0; t < a.n_ctypes && e == cudaSuccess; ++t) {
     const DevMixed& T = a.tab[t];
     const bool warm = a.warm_mask && t == a.warm_set;

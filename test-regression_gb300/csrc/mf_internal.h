@@ -154,6 +154,7 @@ struct MixedArgs {
   int* ws_list;
   unsigned* ws_sched;
   int blocks_per_sm;       // cap on resident blocks per SM (0: the occupancy limit)
+  int list_identity;       // one condition set, no ctype: the list is 0..n-1 (no partition pass)
 };
 constexpr int SCHED_WORDS = 16;
 // Channels per chunk of a mixed fit (the size of the hand-off workspace).

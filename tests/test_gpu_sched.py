@@ -128,3 +128,21 @@ def test_autotune_sweeps_and_keeps_the_fastest(mf, cuda):
                                   channels_per_warp=best[1]))
     assert_identical(tuned, db.outputs_host())
     eng.close()
+
+
+def test_single_set_batch_skips_partition_and_matches_grid(mf, cuda):
+    """A batch without ctype has one condition set: the persistent kernels walk
+    the identity list (no partition launch) and match the grid bit for bit."""
+    eng = mf.Engine(0)
+    eng.set_conditions(0, mf.synth_conditions(mf.SYNTH_ECAL)[0])
+    db = DeviceBatch(mf, cuda, 100_003)
+    db.generate(mf, mf.synth_params(58, 100_003, intime_log=True, lo=0.1, hi=1000.0, pileup_mean=4.0))
+    eng.fit_device(db.batch, opts(mf))
+    grid = db.outputs_host()
+    eng.profile(True)
+    eng.fit_device(db.batch, opts(mf, schedule=mf.SCHED_PERSISTENT))
+    rec = eng.profile_read()
+    eng.profile(False)
+    assert "partition_kernel" not in rec and rec["judge_kernel"][0] == 1
+    assert_identical(db.outputs_host(), grid)
+    eng.close()
