@@ -1,0 +1,60 @@
+"""The engine on the committed golden fixtures (tests/golden/): the plain FP64
+kernel must reproduce the fixtures' fits bit for bit (reference start with
+max_iter 10, support start to KKT convergence, MINOS-like errors, with and
+without a pulse covariance, HCAL 8x8 and hand-made edge channels); the mixed
+form must land within its bounds (<= 1e-4 normwise relative amplitude error,
+identical active sets) of the KKT fixtures."""
+import os
+
+import numpy as np
+import pytest
+
+from _helpers import DeviceBatch
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+FITS = ["ecal_c0", "ecal_logamp", "hcal", "ecal_fpc", "edge"]
+MODES = {"ref": dict(nnls_start=0, max_iter_nnls=10), "kkt": dict(nnls_start=1, max_iter_nnls=1000),
+         "err": dict(nnls_start=1, max_iter_nnls=1000, compute_errors=1)}
+
+
+def setup(mf, cuda, name):
+    d = dict(np.load(os.path.join(GOLDEN, f"fits_{name}.npz")))
+    eng = mf.Engine(0)
+    eng.set_conditions(0, mf.make_conditions(d["P"], d["R"], d["bxs"], fullpulsecov=d.get("fullpulsecov")))
+    n = d["samples"].shape[0]
+    db = DeviceBatch(mf, cuda, n)
+    db.samples[:n] = cuda.from_numpy(d["samples"]).cuda()
+    db.pederr[:n] = cuda.from_numpy(d["pederr"]).cuda()
+    cuda.cuda.synchronize()
+    return d, eng, db
+
+
+@pytest.mark.parametrize("name", FITS)
+@pytest.mark.parametrize("mode", list(MODES))
+def test_fp64_kernel_reproduces_fixture(mf, cuda, name, mode):
+    d, eng, db = setup(mf, cuda, name)
+    eng.fit_device(db.batch, mf.default_options(**MODES[mode]))
+    o = db.outputs_host()
+    K = d["P"].shape[1]
+    assert np.array_equal(o["amplitudes"][:, :K], d[f"{mode}_amplitudes"])
+    for k in ("chi2", "active_mask", "status"):
+        assert np.array_equal(o[k], d[f"{mode}_{k}"]), k
+    if mode == "err":
+        assert np.array_equal(o["errors"], d["err_errors"], equal_nan=True)
+    eng.close()
+
+
+@pytest.mark.parametrize("name", ["ecal_c0", "ecal_logamp", "hcal", "edge"])
+def test_mixed_form_within_bounds_of_kkt_fixture(mf, cuda, name):
+    d, eng, db = setup(mf, cuda, name)
+    eng.fit_device(db.batch, mf.default_options(precision=mf.PREC_MIXED, max_iter_nnls=1000))
+    o = db.outputs_host()
+    K = d["P"].shape[1]
+    r = d["kkt_amplitudes"]
+    ok = d["kkt_status"] == 0
+    err = np.abs(o["amplitudes"][:, :K] - r).max(axis=1) / np.maximum(np.abs(r).max(axis=1), 1e-300)
+    assert (err[ok] <= 1e-4).all(), err[ok].max()
+    assert (o["active_mask"][ok] == d["kkt_active_mask"][ok]).all()
+    eng.close()
