@@ -56,5 +56,16 @@ def test_mixed_form_within_bounds_of_kkt_fixture(mf, cuda, name):
     ok = d["kkt_status"] == 0
     err = np.abs(o["amplitudes"][:, :K] - r).max(axis=1) / np.maximum(np.abs(r).max(axis=1), 1e-300)
     assert (err[ok] <= 1e-4).all(), err[ok].max()
-    assert (o["active_mask"][ok] == d["kkt_active_mask"][ok]).all()
+    # active sets agree, except on columns whose amplitude is at round-off
+    # level in both fits (noise-free edge channels: with pederr -> 0 the
+    # reference's absolute threshold eps * pederr^2 falls below FP64 round-off,
+    # so such columns enter or not on rounding noise, in the oracle as well)
+    diff = o["active_mask"] ^ d["kkt_active_mask"]
+    scale = np.maximum(np.abs(r).max(axis=1), 1e-300)
+    for i in np.nonzero(ok & (diff != 0))[0]:
+        cols = [k for k in range(K) if (int(diff[i]) >> k) & 1]
+        assert all(abs(r[i, k]) <= 1e-9 * scale[i] and abs(o["amplitudes"][i, k]) <= 1e-9 * scale[i]
+                   for k in cols), (name, i, cols, r[i], o["amplitudes"][i])
+    if name != "edge":
+        assert (diff[ok] == 0).all()
     eng.close()
