@@ -117,15 +117,25 @@ class ClockSampler:
 
 
 def dist_setup(args):
+    """One process per GPU (torchrun env). NCCL for our arm on GPUs; gloo for the
+    CPU reference arm and wherever CUDA is absent (the CPU tests of this logic)."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
+        import torch
         import torch.distributed as dist
 
-        backend = "nccl" if args.impl != "reference" else "gloo"
+        backend = "nccl" if args.impl != "reference" and torch.cuda.is_available() else "gloo"
         dist.init_process_group(backend=backend)
     return world, rank, local
+
+
+def shard_range(rank: int, per_rank: int):
+    """Channels [first, first + per_rank) of the seeded channel stream that a
+    rank fits: channels are independent, so ranks fit disjoint contiguous
+    shards with no collective on the data path (weak scaling)."""
+    return rank * per_rank, per_rank
 
 
 def max_over_ranks(x: float, world: int, device=None) -> float:
@@ -255,7 +265,7 @@ def run_ours(args, world, rank, local):
     intime = torch.zeros(n, dtype=torch.float64, device=dev)
     mask = torch.zeros(n, dtype=torch.int16, device=dev)
     status = torch.zeros(n, dtype=torch.uint8, device=dev)
-    first = rank * n  # each rank fits its own shard of the channel stream
+    first, _ = shard_range(rank, n)  # each rank fits its own shard of the channel stream
     mf.synth_generate_device(p, first, n, samples.data_ptr(), pederr.data_ptr(),
                              ctype.data_ptr() if mixed else None)
     batch = mf.Engine._batch(n, 10, 10, samples.data_ptr(), pederr.data_ptr(),
