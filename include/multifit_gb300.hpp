@@ -53,7 +53,7 @@ class SmallVector {
   int n_ = 0;
 };
 typedef SmallVector<double> PulseVector;
-typedef SmallVector<char> BXVector;
+typedef SmallVector<signed char> BXVector;  // signed on every target (plain char is unsigned on Arm)
 
 class Error : public std::runtime_error {
  public:
@@ -89,7 +89,7 @@ class Context {
     double fp[MF_FULLPULSE_MAX];
     int8_t bx[MF_MAX_PULSES];
     for (int i = 0; i < MF_FULLPULSE_MAX; ++i) fp[i] = fullpulse(i);
-    for (int k = 0; k < K; ++k) bx[k] = int8_t(bxs(k));
+    for (int k = 0; k < K; ++k) bx[k] = static_cast<int8_t>(bxs(k));
     check(mf_build_pulse_matrix(fp, bx, N, K, c.pulse_matrix), "mf_build_pulse_matrix");
     for (int j = 0; j < N; ++j)
       for (int i = 0; i < N; ++i) c.noise_cor[j * N + i] = samplecor(i, j);
@@ -156,7 +156,7 @@ class PulseChiSqSNNLS {
     int intime = -1;  // the first pulse with bx == 0 (PulseChiSqSNNLS.cpp:79-85)
     for (int k = 0; k < K; ++k) {
       x_[k] = amp[k];
-      bxs_[k] = char(bxs(k));
+      bxs_[k] = static_cast<signed char>(bxs(k));
       if (intime < 0 && bxs(k) == 0) intime = k;
     }
     if (compute_errors_ && intime >= 0) errors_[intime] = err;  // its MINOS-like uncertainty

@@ -69,7 +69,10 @@ int main(int argc, char** argv) {
           }
         const double ampl = status ? func.X()[int(ip_in_time)] : 0.;
         double x[10] = {};
-        for (int ip = 0; ip < func.BXs().rows(); ++ip) x[int(func.BXs().coeff(ip)) + 5] = func.X()[ip];
+        for (int ip = 0; ip < func.BXs().rows(); ++ip) {
+          const int slot = int(func.BXs().coeff(ip)) + 5;
+          if (slot >= 0 && slot < 10) x[slot] = func.X()[ip];
+        }
         const int st = status ? 1 : 0;
         std::fwrite(&chi2, 8, 1, o);
         std::fwrite(&ampl, 8, 1, o);
@@ -85,7 +88,10 @@ int main(int argc, char** argv) {
         const double chi2 = fit.ChiSq(size_t(c));
         const int st = (fit.status(size_t(c)) & MF_CH_BADINPUT) ? 0 : 1;
         double x[10] = {};
-        for (int ip = 0; ip < 10; ++ip) x[bxs.v[ip] + 5] = fit.X(size_t(c))[ip];
+        for (int ip = 0; ip < 10; ++ip) {
+          const int slot = int(bxs.v[ip]) + 5;
+          if (slot >= 0 && slot < 10) x[slot] = fit.X(size_t(c))[ip];
+        }
         const double ampl = st ? x[5] : 0.;
         std::fwrite(&chi2, 8, 1, o);
         std::fwrite(&ampl, 8, 1, o);

@@ -15,18 +15,20 @@ from _helpers import DeviceBatch
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def build_driver(mf, tmp_path):
+def build_driver(mf, tmp_path, extra=()):
     exe = str(tmp_path / "dropin_driver")
     lib_dir = os.path.dirname(mf.LIB_PATH)
-    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror", *extra, "-I", os.path.join(ROOT, "include"),
            os.path.join(ROOT, "tests", "cpp", "dropin_driver.cpp"), "-L", lib_dir, "-lmultifit_gb300",
            f"-Wl,-rpath,{lib_dir}", "-o", exe]
     subprocess.run(cmd, check=True, capture_output=True)
     return exe
 
 
-def test_dropin_compiles_and_links(mf, tmp_path):
-    exe = build_driver(mf, tmp_path)
+@pytest.mark.parametrize("extra", [(), ("-funsigned-char",)])
+def test_dropin_compiles_and_links(mf, tmp_path, extra):
+    """Also with plain char unsigned, as on Arm (the bx offsets are negative)."""
+    exe = build_driver(mf, tmp_path, extra)
     out = subprocess.run(["nm", "-u", exe], capture_output=True, text=True).stdout
     assert "mf_fit_host" in out and "mf_set_conditions" in out
 
