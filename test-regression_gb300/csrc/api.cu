@@ -102,6 +102,10 @@ struct mf_context {
   uint8_t* d_status = nullptr;
   int32_t* d_iters = nullptr;
   cudaStream_t stream = nullptr;
+  // mf_fit_host pipeline: copy-in and copy-out streams, per-chunk events
+  cudaStream_t h2d_stream = nullptr, d2h_stream = nullptr;
+  static constexpr int kHostChunks = 64;
+  cudaEvent_t in_done[kHostChunks] = {}, fit_done[kHostChunks] = {};
   LaunchTimer timer;  // per-kernel launch timing (mf_profile), off by default
   std::mutex mu;
 };
@@ -165,7 +169,7 @@ int fill_args(mf_context* ctx, const mf_batch* b, const mf_options* o, FitArgs* 
 
 void fill_dev_mixed(const mf_context* c, int t, DevMixed* m);
 
-int dispatch_mixed(mf_context* c, const FitArgs& a, const mf_options* o, cudaStream_t s) {
+int dispatch_mixed(mf_context* c, const FitArgs& a, const mf_options* o, cudaStream_t s, bool allow_graph) {
   if (o->compute_errors) return MF_EUNSUPPORTED;
   const bool persistent = o->schedule == MF_SCHED_PERSISTENT;
   const int block = o->block_size ? o->block_size : (persistent && c->tuned_block ? c->tuned_block : 128);
@@ -259,8 +263,9 @@ int dispatch_mixed(mf_context* c, const FitArgs& a, const mf_options* o, cudaStr
   return cudaSuccess;
   };
   cudaError_t e = cudaSuccess;
-  if (!persistent || c->timer.ev) {
-    // grid schedule, or per-launch timing requested: launch directly
+  if (!persistent || c->timer.ev || !allow_graph) {
+    // grid schedule, per-launch timing requested, or a caller that varies the
+    // arguments every call (the chunks of mf_fit_host): launch directly
     e = enqueue(s, &c->timer);
   } else {
     // persistent schedule: replay the CUDA graph of this exact launch sequence,
@@ -299,8 +304,9 @@ int dispatch_mixed(mf_context* c, const FitArgs& a, const mf_options* o, cudaStr
   return MF_OK;
 }
 
-int dispatch_form(mf_context* c, const FitArgs& a, const mf_options* o, cudaStream_t s, bool instrumented) {
-  if (o->precision == MF_PREC_MIXED) return dispatch_mixed(c, a, o, s);
+int dispatch_form(mf_context* c, const FitArgs& a, const mf_options* o, cudaStream_t s, bool instrumented,
+                  bool allow_graph) {
+  if (o->precision == MF_PREC_MIXED) return dispatch_mixed(c, a, o, s, allow_graph);
   if (o->precision != MF_PREC_FP64 || o->schedule != MF_SCHED_GRID || o->warm_start != MF_WARM_NONE)
     return MF_EUNSUPPORTED;
   cudaError_t e = launch_fit_fp64(a, o->block_size, s, instrumented, &c->timer);
@@ -311,8 +317,9 @@ int dispatch_form(mf_context* c, const FitArgs& a, const mf_options* o, cudaStre
   return MF_OK;
 }
 
-int dispatch(mf_context* c, const FitArgs& a, const mf_options* o, cudaStream_t s, bool instrumented) {
-  const int rc = dispatch_form(c, a, o, s, instrumented);
+int dispatch(mf_context* c, const FitArgs& a, const mf_options* o, cudaStream_t s, bool instrumented,
+             bool allow_graph = true) {
+  const int rc = dispatch_form(c, a, o, s, instrumented, allow_graph);
   c->timer.mark(-1, s);  // end of this fit's launches
   return rc;
 }
@@ -519,6 +526,12 @@ void mf_destroy(mf_context* c) {
   destroy_timer(c->timer);
   if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
   if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
+  for (int i = 0; i < mf_context::kHostChunks; ++i) {
+    if (c->in_done[i]) cudaEventDestroy(c->in_done[i]);
+    if (c->fit_done[i]) cudaEventDestroy(c->fit_done[i]);
+  }
+  if (c->h2d_stream) cudaStreamDestroy(c->h2d_stream);
+  if (c->d2h_stream) cudaStreamDestroy(c->d2h_stream);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -662,6 +675,11 @@ int mf_fit_count_flops(mf_context* c, const mf_batch* b, const mf_options* o, do
   return dispatch(c, a, o, (cudaStream_t)stream, true);
 }
 
+// Host-pointer fit, pipelined: the batch is cut into chunks (>= 2^20
+// channels, at most 64); the copy-in of chunk i+1 (h2d stream) and the
+// copy-out of chunk i-1 (d2h stream) run under the fit of chunk i (the
+// context stream), ordered by events. With pinned host buffers the step costs
+// about max(copies, fit) instead of their sum.
 int mf_fit_host(mf_context* c, const mf_batch* hb, const mf_options* o) {
   if (!c || !hb) return MF_EINVAL;
   std::lock_guard<std::mutex> g(c->mu);
@@ -670,42 +688,80 @@ int mf_fit_host(mf_context* c, const mf_batch* hb, const mf_options* o) {
   if (n == 0) return MF_OK;
   int rc = grow_staging(c, n, hb->sample_stride, hb->amp_stride);
   if (rc) return rc;
-  cudaStream_t s = c->stream;
+  {  // validate once on the whole batch before any copy
+    mf_batch db = *hb;
+    db.samples = c->d_samples;
+    db.pederr = c->d_pederr;
+    db.ctype = hb->ctype ? c->d_ctype : nullptr;
+    db.amplitudes = c->d_amp;
+    db.chi2 = c->d_chi2;
+    FitArgs a;
+    rc = fill_args(c, &db, o, &a);
+    if (rc) return rc;
+  }
   cudaError_t e = cudaSuccess;
-  auto cp = [&](void* dst, const void* src, size_t bytes, cudaMemcpyKind k) {
-    if (e == cudaSuccess && src && dst) e = cudaMemcpyAsync(dst, src, bytes, k, s);
-  };
-  cp(c->d_samples, hb->samples, sizeof(double) * n * hb->sample_stride, cudaMemcpyHostToDevice);
-  cp(c->d_pederr, hb->pederr, sizeof(double) * n, cudaMemcpyHostToDevice);
-  if (hb->ctype) cp(c->d_ctype, hb->ctype, n, cudaMemcpyHostToDevice);
+  if (!c->h2d_stream) e = cudaStreamCreateWithFlags(&c->h2d_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess && !c->d2h_stream) e = cudaStreamCreateWithFlags(&c->d2h_stream, cudaStreamNonBlocking);
+  for (int i = 0; i < mf_context::kHostChunks && e == cudaSuccess; ++i) {
+    if (!c->in_done[i]) e = cudaEventCreateWithFlags(&c->in_done[i], cudaEventDisableTiming);
+    if (e == cudaSuccess && !c->fit_done[i]) e = cudaEventCreateWithFlags(&c->fit_done[i], cudaEventDisableTiming);
+  }
   if (e != cudaSuccess) {
-    set_last_error("H2D copy", e);
+    set_last_error("mf_fit_host: stream/event setup", e);
     return MF_ECUDA;
   }
-  mf_batch db = *hb;
-  db.samples = c->d_samples;
-  db.pederr = c->d_pederr;
-  db.ctype = hb->ctype ? c->d_ctype : nullptr;
-  db.amplitudes = c->d_amp;
-  db.chi2 = c->d_chi2;
-  db.intime = hb->intime ? c->d_intime : nullptr;
-  db.errors = hb->errors ? c->d_errors : nullptr;
-  db.active_mask = hb->active_mask ? c->d_mask : nullptr;
-  db.status = hb->status ? c->d_status : nullptr;
-  db.iters = hb->iters ? c->d_iters : nullptr;
-  FitArgs a;
-  rc = fill_args(c, &db, o, &a);
-  if (rc) return rc;
-  rc = dispatch(c, a, o, s, false);
-  if (rc) return rc;
-  cp(hb->amplitudes, c->d_amp, sizeof(double) * n * hb->amp_stride, cudaMemcpyDeviceToHost);
-  cp(hb->chi2, c->d_chi2, sizeof(double) * n, cudaMemcpyDeviceToHost);
-  if (hb->intime) cp(hb->intime, c->d_intime, sizeof(double) * n, cudaMemcpyDeviceToHost);
-  if (hb->errors) cp(hb->errors, c->d_errors, sizeof(double) * n, cudaMemcpyDeviceToHost);
-  if (hb->active_mask) cp(hb->active_mask, c->d_mask, sizeof(uint16_t) * n, cudaMemcpyDeviceToHost);
-  if (hb->status) cp(hb->status, c->d_status, n, cudaMemcpyDeviceToHost);
-  if (hb->iters) cp(hb->iters, c->d_iters, sizeof(int32_t) * n, cudaMemcpyDeviceToHost);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  const int64_t min_chunk = int64_t(1) << 20;
+  int64_t chunk = (n + mf_context::kHostChunks - 1) / mf_context::kHostChunks;
+  if (chunk < min_chunk) chunk = min_chunk;
+  const int nchunks = int((n + chunk - 1) / chunk);
+  const int ss = hb->sample_stride, as = hb->amp_stride;
+  auto cp = [&](void* dst, const void* src, size_t bytes, cudaMemcpyKind k, cudaStream_t st) {
+    if (e == cudaSuccess && src && dst && bytes) e = cudaMemcpyAsync(dst, src, bytes, k, st);
+  };
+  for (int i = 0; i < nchunks && e == cudaSuccess && rc == MF_OK; ++i) {
+    const int64_t off = i * chunk, m = (n - off < chunk) ? n - off : chunk;
+    // copy in
+    cp(c->d_samples + off * ss, hb->samples + off * ss, sizeof(double) * m * ss, cudaMemcpyHostToDevice, c->h2d_stream);
+    cp(c->d_pederr + off, hb->pederr + off, sizeof(double) * m, cudaMemcpyHostToDevice, c->h2d_stream);
+    if (hb->ctype) cp(c->d_ctype + off, hb->ctype + off, m, cudaMemcpyHostToDevice, c->h2d_stream);
+    if (e == cudaSuccess) e = cudaEventRecord(c->in_done[i], c->h2d_stream);
+    // fit
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->in_done[i], 0);
+    if (e != cudaSuccess) break;
+    mf_batch db = *hb;
+    db.n = m;
+    db.samples = c->d_samples + off * ss;
+    db.pederr = c->d_pederr + off;
+    db.ctype = hb->ctype ? c->d_ctype + off : nullptr;
+    db.amplitudes = c->d_amp + off * as;
+    db.chi2 = c->d_chi2 + off;
+    db.intime = hb->intime ? c->d_intime + off : nullptr;
+    db.errors = hb->errors ? c->d_errors + off : nullptr;
+    db.active_mask = hb->active_mask ? c->d_mask + off : nullptr;
+    db.status = hb->status ? c->d_status + off : nullptr;
+    db.iters = hb->iters ? c->d_iters + off : nullptr;
+    FitArgs a;
+    rc = fill_args(c, &db, o, &a);
+    if (rc == MF_OK) rc = dispatch(c, a, o, c->stream, false, false);
+    if (rc != MF_OK) break;
+    e = cudaEventRecord(c->fit_done[i], c->stream);
+    // copy out
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->d2h_stream, c->fit_done[i], 0);
+    cp(hb->amplitudes + off * as, c->d_amp + off * as, sizeof(double) * m * as, cudaMemcpyDeviceToHost, c->d2h_stream);
+    cp(hb->chi2 + off, c->d_chi2 + off, sizeof(double) * m, cudaMemcpyDeviceToHost, c->d2h_stream);
+    if (hb->intime) cp(hb->intime + off, c->d_intime + off, sizeof(double) * m, cudaMemcpyDeviceToHost, c->d2h_stream);
+    if (hb->errors) cp(hb->errors + off, c->d_errors + off, sizeof(double) * m, cudaMemcpyDeviceToHost, c->d2h_stream);
+    if (hb->active_mask)
+      cp(hb->active_mask + off, c->d_mask + off, sizeof(uint16_t) * m, cudaMemcpyDeviceToHost, c->d2h_stream);
+    if (hb->status) cp(hb->status + off, c->d_status + off, m, cudaMemcpyDeviceToHost, c->d2h_stream);
+    if (hb->iters) cp(hb->iters + off, c->d_iters + off, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, c->d2h_stream);
+  }
+  // drain all three streams, whatever happened above
+  const cudaError_t e1 = cudaStreamSynchronize(c->h2d_stream);
+  const cudaError_t e2 = cudaStreamSynchronize(c->stream);
+  const cudaError_t e3 = cudaStreamSynchronize(c->d2h_stream);
+  if (rc != MF_OK) return rc;
+  if (e == cudaSuccess) e = e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e3);
   if (e != cudaSuccess) {
     set_last_error("mf_fit_host", e);
     return MF_ECUDA;

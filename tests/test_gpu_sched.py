@@ -146,3 +146,25 @@ def test_single_set_batch_skips_partition_and_matches_grid(mf, cuda):
     assert "partition_kernel" not in rec and rec["judge_kernel"][0] == 1
     assert_identical(db.outputs_host(), grid)
     eng.close()
+
+
+@pytest.mark.parametrize("form", ["fp64", "mixed-persistent"])
+def test_pipelined_host_fit_equals_device_fit(mf, cuda, form):
+    """mf_fit_host cuts a large batch into chunks whose copy-in, fit and
+    copy-out overlap on three streams: 2,500,001 channels (3 chunks, ragged
+    last one) must come back bit-identical to mf_fit on the same inputs,
+    including out-of-range condition sets."""
+    eng = ecal_hcal(mf)
+    n = 2_500_001
+    db = mixed_batch(mf, cuda, n, seed=59)
+    db.ctype[123_457] = 9
+    cuda.cuda.synchronize()
+    o = mf.default_options() if form == "fp64" else opts(mf, schedule=mf.SCHED_PERSISTENT)
+    eng.fit_device(db.batch, o)
+    dev = db.outputs_host()
+    inp = db.inputs_host()
+    host = eng.fit_host(inp["samples"], inp["pederr"], ctype=inp["ctype"], options=o)
+    for k in ("amplitudes", "chi2", "intime", "active_mask", "status", "iters"):
+        np.testing.assert_array_equal(host[k], dev[k], err_msg=k)
+    assert dev["status"][123_457] == mf.CH_BADINPUT
+    eng.close()
