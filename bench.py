@@ -350,6 +350,7 @@ def run_ours(args, world, rank, local):
         torch.cuda.synchronize()
         form_amp = amp.clone()
         form_mask = mask.clone()
+        form_chi2 = chi2.clone()
         # the clones run on torch's default stream and the fits below on `stream`
         # (non-blocking): let the copies finish before anything overwrites amp/mask
         torch.cuda.synchronize()
@@ -378,14 +379,19 @@ def run_ours(args, world, rank, local):
         scale = amp.abs().amax(dim=1).clamp_min(1e-300)
         err = (form_amp - amp).abs().amax(dim=1) / scale
         same = (form_mask == mask)
+        chi2_err = ((form_chi2 - chi2).abs() / chi2.abs().clamp_min(1.0))[same]
         accuracy = {"reference": "plain FP64 GPU kernel, support start, max_iter 1000 (bit-identical to the oracle)",
                     "channels": n, "rel_amp_err_median": float(err.median().item()),
                     "rel_amp_err_p999": float(torch.quantile(err[: min(n, 4_000_000)].float(), 0.999).item()),
                     "rel_amp_err_max": float(err.max().item()),
                     "frac_within_1e-4": float((err <= 1e-4).double().mean().item()),
+                    "chi2_rel_err_median": float(chi2_err.median().item()) if chi2_err.numel() else None,
+                    "chi2_rel_err_max": float(chi2_err.max().item()) if chi2_err.numel() else None,
+                    "chi2_note": "|chi2 - chi2_ref| / max(chi2_ref, 1) on channels whose active sets agree",
                     "active_set_identical_frac": float(same.double().mean().item())}
         amp.copy_(form_amp)
         mask.copy_(form_mask)
+        chi2.copy_(form_chi2)
         torch.cuda.synchronize()
 
     # parity spot check of this run's output against the oracle
