@@ -537,7 +537,8 @@ def kernel_rooflines(mf, eng, kernels, args, n, ctype, plain_flops, form_fp64_fl
     repair_kernel: the rest of the form's counted FP64 flops.
     mlp_infer_kernel: MLP_FLOPS_PER_CHANNEL on the tensor cores (BF16).
     search_kernel: FP32 and latency-bound; its HBM bytes (samples, pederr,
-      warm start in; hand-off out) against the copy bandwidth."""
+      warm start in; hand-off out) against the copy bandwidth.
+    screen_kernel: FP32 (double-float screen); its HBM bytes likewise."""
     import numpy as np
 
     counts = {0: n}
@@ -566,6 +567,9 @@ def kernel_rooflines(mf, eng, kernels, args, n, ctype, plain_flops, form_fp64_fl
         elif name == "mlp_infer_kernel":
             work = n * MLP_FLOPS_PER_CHANNEL / per_step
             bound, peak, unit = "tensor", peaks["bf16_tflops"], "TFLOP/s"
+        elif name in ("screen_kernel", "fix_kernel"):  # samples + hand-off in, hand-off out (FP32)
+            work = n * (10 * 8 + 44 + 44) / per_step
+            bound, peak, unit = "hbm", peaks["hbm_gbs"], "GB/s"
         elif name == "partition_kernel":  # ctype in, channel lists out
             work = n * (1 + 4) / per_step
             bound, peak, unit = "hbm", peaks["hbm_gbs"], "GB/s"

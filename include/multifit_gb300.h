@@ -187,8 +187,8 @@ int mf_fit_count_flops(mf_context* ctx, const mf_batch* batch, const mf_options*
  *    stream capture on that device begins.
  *  - One scratch per device: calls that overlap on a device (other streams,
  *    threads or contexts) race on it; serialise them.
- *  - The only scratch word that must start at zero (the repair-queue counter)
- *    is written by the call itself before it is read. */
+ *  - The only scratch words that must start at zero (the two queue counters)
+ *    are written by the call itself before they are read. */
 #define MF_NOALLOC_MAX_CHANNELS 131072
 int mf_fit_noalloc(mf_context* ctx, const mf_batch* batch, const mf_options* opt, void* stream);
 
@@ -221,7 +221,9 @@ enum mf_kernel_kind {
   MF_K_JUDGE = 3,     /* judge_kernel / judge_persist: FP64 solve, residual, KKT test, chi2 */
   MF_K_REPAIR = 4,    /* repair_kernel / repair_persist: FP64 FNNLS of the channels the judge queued */
   MF_K_PARTITION = 5, /* partition_kernel: per-set channel lists of the persistent schedule */
-  MF_K_COUNT = 6
+  MF_K_SCREEN = 6,    /* screen_kernel / screen_persist: FP32 double-float KKT screen of the search's set */
+  MF_K_FIX = 7,       /* fix_kernel / fix_persist: FP32 FNNLS step of the channels the screen queued */
+  MF_K_COUNT = 8
 };
 /* enable != 0 creates the context's event pool (and clears it); 0 frees it. */
 int mf_profile(mf_context* ctx, int enable);

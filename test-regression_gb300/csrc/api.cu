@@ -388,7 +388,7 @@ int upload_tables(mf_context* c, int t) {
     if (e == cudaSuccess) e = cudaMalloc(&c->ws_count, sizeof(uint16_t) * MIXED_CHUNK);
     if (e == cudaSuccess) e = cudaMalloc(&c->ws_x, sizeof(float) * MIXED_CHUNK * KMAX);
     if (e == cudaSuccess) e = cudaMalloc(&c->ws_queue, sizeof(int) * MIXED_CHUNK);
-    if (e == cudaSuccess) e = cudaMalloc(&c->ws_qcount, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMalloc(&c->ws_qcount, 2 * sizeof(unsigned));  // repair and fix queues
     if (e == cudaSuccess) e = cudaMalloc(&c->ws_list, sizeof(int) * MIXED_CHUNK * MF_MAX_CTYPES);
     if (e == cudaSuccess) e = cudaMalloc(&c->ws_sched, sizeof(unsigned) * SCHED_WORDS);
   }
@@ -413,6 +413,8 @@ void fill_dev_mixed(const mf_context* c, int t, DevMixed* m) {
   std::memcpy(m->G64, h.G64, sizeof(h.G64));
   std::memcpy(m->H64, h.H64, sizeof(h.H64));
   std::memcpy(m->G32, h.G32, sizeof(h.G32));
+  std::memcpy(m->P32, h.P32, sizeof(h.P32));
+  std::memcpy(m->P32lo, h.P32lo, sizeof(h.P32lo));
   std::memcpy(m->H32, h.H32, sizeof(h.H32));
   for (int k = 0; k < K; ++k) {
     m->gnorm32[k] = float(std::sqrt(h.gnorm2[k]));
@@ -895,9 +897,10 @@ int mf_build_pulse_matrix(const double* fullpulse, const int8_t* bxs, int N, int
 // MLP warm start), no MINOS errors. The scratch is one array per device, so
 // calls whose work overlaps on one device (two streams, two host threads, two
 // contexts) race on it: serialise them, e.g. one stream per device.
-// What must start at zero: only the repair-queue counter, and the search
-// launch of every call writes it before the judge launch reads it; the other
-// scratch words are written before they are read within a call.
+// What must start at zero: only the two queue counters (screen -> fix,
+// judge -> repair), and the search launch of every call writes them before
+// the screen and judge launches read them; the other scratch words are
+// written before they are read within a call.
 // ---------------------------------------------------------------------------
 
 namespace {
@@ -909,7 +912,7 @@ constexpr size_t kOffX = 0;                                                     
 constexpr size_t kOffQueue = kOffX + kAlignUp(sizeof(float) * kNoallocMax * KMAX);  // int [max]
 constexpr size_t kOffMask = kOffQueue + kAlignUp(sizeof(int) * kNoallocMax);       // uint16 [max]
 constexpr size_t kOffCount = kOffMask + kAlignUp(sizeof(uint16_t) * kNoallocMax);  // uint16 [max]
-constexpr size_t kOffQcount = kOffCount + kAlignUp(sizeof(uint16_t) * kNoallocMax);  // unsigned
+constexpr size_t kOffQcount = kOffCount + kAlignUp(sizeof(uint16_t) * kNoallocMax);  // unsigned [2]
 constexpr size_t kNoallocBytes = kOffQcount + 256;  // 6,291,712 bytes for 131,072 channels
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];

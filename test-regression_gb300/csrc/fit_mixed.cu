@@ -12,6 +12,11 @@
 //     gradient w = G^T y - H x, solve the passive set, step back and drop
 //     columns that go non-positive -- from an empty set or the predicted one;
 //     writes the passive mask and the FP32 amplitudes of each channel.
+//   screen_kernel  (FP32, branch-free): the accurate KKT screen of the
+//     search's set in double-float arithmetic; queues the channels with
+//     columns the FP32 search missed for
+//   fix_kernel     (FP32, compacted): their FNNLS step and one more screen,
+//     so that few channels need the FP64 repair.
 //   judge_kernel   (FP64, lean, branch-free: every lane the same FP64
 //     instructions): y in FP64, the FP64 solve on the FP32 passive set, the
 //     FP64 residual, chi2 = ||y - G x||^2 / pederr^2, and the KKT test
@@ -46,11 +51,31 @@ namespace {
 template <int N, int K, bool WARM>
 __global__ void __launch_bounds__(128) search_kernel(const MixedArgs a, int set) {
   const int64_t ch = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (ch == 0) *a.ws_qcount = 0u;  // the judge launch that follows fills the repair queue
+  if (ch == 0) {  // the screen and judge launches that follow fill the fix and repair queues
+    a.ws_qcount[0] = 0u;
+    a.ws_qcount[1] = 0u;
+  }
   if (ch >= a.n) return;
   const int t = a.ctype ? int(a.ctype[ch]) : 0;
   if (t != set) return;
   search_body<N, K, WARM>(a, a.tab[set], ch);
+}
+
+template <int N, int K>
+__global__ void __launch_bounds__(128) screen_kernel(const MixedArgs a, int set) {
+  const int64_t ch = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (ch >= a.n) return;
+  const int t = a.ctype ? int(a.ctype[ch]) : 0;
+  if (t != set) return;
+  screen_body<N, K>(a, a.tab[set], ch, a.ws_qcount + 1);
+}
+
+template <int N, int K>
+__global__ void __launch_bounds__(128) fix_kernel(const MixedArgs a, int set) {
+  const DevMixed& T = a.tab[set];
+  const unsigned cnt = a.ws_qcount[1];
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x)
+    fix_body<N, K>(a, T, unsigned(a.ws_queue[i]));
 }
 
 template <int N, int K>
@@ -75,14 +100,14 @@ __global__ void __launch_bounds__(128, 6) judge_kernel(const MixedArgs a, int se
 template <int N, int K>
 __global__ void __launch_bounds__(128) repair_kernel(const MixedArgs a, int set) {
   const DevMixed& T = a.tab[set];
-  const unsigned cnt = *a.ws_qcount;
+  const unsigned cnt = a.ws_qcount[0];
   for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x)
     judge_repair<N, K>(a, T, int64_t(a.ws_queue[i]));
 }
 
 }  // namespace
 
-// One search, judge and repair launch per condition set (lanes of other sets return at
+// One search, screen, fix, judge and repair launch per condition set (lanes of other sets return at
 // once); out-of-range set indices are flagged by the first judge launch.
 cudaError_t launch_fit_mixed(const MixedArgs& a, int block, cudaStream_t s, LaunchTimer* tm) {
   auto mark = [&](int k) {
@@ -104,6 +129,10 @@ cudaError_t launch_fit_mixed(const MixedArgs& a, int block, cudaStream_t s, Laun
       mark(MF_K_SEARCH);
       if (warm) search_kernel<10, 10, true><<<grid, block, 0, s>>>(a, t);
       else search_kernel<10, 10, false><<<grid, block, 0, s>>>(a, t);
+      mark(MF_K_SCREEN);
+      screen_kernel<10, 10><<<jgrid, 128, 0, s>>>(a, t);
+      mark(MF_K_FIX);
+      fix_kernel<10, 10><<<rgrid, 128, 0, s>>>(a, t);
       mark(MF_K_JUDGE);
       judge_kernel<10, 10><<<jgrid, 128, 0, s>>>(a, t, flag_bad);
       mark(MF_K_REPAIR);
@@ -111,6 +140,10 @@ cudaError_t launch_fit_mixed(const MixedArgs& a, int block, cudaStream_t s, Laun
     } else if (T.N == 8 && T.K == 8) {
       mark(MF_K_SEARCH);
       search_kernel<8, 8, false><<<grid, block, 0, s>>>(a, t);
+      mark(MF_K_SCREEN);
+      screen_kernel<8, 8><<<jgrid, 128, 0, s>>>(a, t);
+      mark(MF_K_FIX);
+      fix_kernel<8, 8><<<rgrid, 128, 0, s>>>(a, t);
       mark(MF_K_JUDGE);
       judge_kernel<8, 8><<<jgrid, 128, 0, s>>>(a, t, flag_bad);
       mark(MF_K_REPAIR);

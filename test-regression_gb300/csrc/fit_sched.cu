@@ -14,6 +14,8 @@
 //   search_persist    FP32 search over a set's list, L lanes per channel
 //                     (32 / L channels per warp), each warp taking the next
 //                     32 / L channels from an atomic counter when it is done;
+//   screen_persist    FP32 KKT screen (double-float residual) over the list;
+//   fix_persist       FP32 FNNLS step of the channels the screen queued;
 //   judge_persist     FP64 judge over the list, 32 channels per steal;
 //   repair_persist    FP64 repair over the judge's queue, 32 per steal.
 //
@@ -34,8 +36,9 @@ constexpr unsigned kFull = 0xffffffffu;
 
 // ws_sched words
 constexpr int SCHED_COUNT = 0;   // [set] channels in the set's list
-constexpr int SCHED_STEAL = 2;   // [set * 3 + kernel] work counters (search, judge, repair)
-constexpr int SCHED_QUEUE = 8;   // [set] channels queued for repair
+constexpr int SCHED_STEAL = 2;   // [set * 5 + kernel] work counters (search, screen, fix, judge, repair)
+constexpr int SCHED_QUEUE = 12;  // [set] channels queued for repair
+constexpr int SCHED_FIXQ = 14;   // [set] channels queued by the screen for the fix
 
 __global__ void partition_kernel(const MixedArgs a) {
   const int lane = threadIdx.x & 31;
@@ -156,28 +159,6 @@ __device__ __forceinline__ void search_body_coop(const MixedArgs& a, const DevMi
     ++adds;
     solves += inner_loop<K>(m, x32, s32);
   }
-  {
-    float cmag[K], cc[K];
-    gram_rhs32<N, K>(T, y32, cc, cmag);
-    unsigned amb = 0;
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      if (m & (1u << k)) continue;
-      float acc = c32[k], mag = cmag[k];
-#pragma unroll
-      for (int j = 0; j < K; ++j) {
-        const float hx = T.H32[k * KMAX + j] * x32[j];
-        acc -= hx;
-        mag += fabsf(hx);
-      }
-      if (acc >= -4e-6f * mag) amb |= 1u << k;
-    }
-    if (amb) {
-      m |= amb;
-      adds += __popc(amb);
-      solves += inner_loop<K>(m, x32, s32);
-    }
-  }
   if (sub == 0) {
     a.ws_mask[ch] = uint16_t(m);
     a.ws_count[ch] = uint16_t((adds < 255 ? adds : 255) | ((solves < 255 ? solves : 255) << 8));
@@ -203,7 +184,7 @@ __global__ void __launch_bounds__(512) search_persist(const MixedArgs a, int set
   const int lane = threadIdx.x & 31, sub = lane % L;
   const unsigned gmask = L == 32 ? kFull : (((1u << L) - 1u) << (lane - sub));
   for (;;) {
-    const unsigned base = steal(a.ws_sched + SCHED_STEAL + set * 3 + 0, G);
+    const unsigned base = steal(a.ws_sched + SCHED_STEAL + set * 5 + 0, G);
     if (base >= total) break;
     const unsigned i = base + unsigned(lane / L);
     if (i < total) {
@@ -215,13 +196,40 @@ __global__ void __launch_bounds__(512) search_persist(const MixedArgs a, int set
 }
 
 template <int N, int K>
+__global__ void __launch_bounds__(128) screen_persist(const MixedArgs a, int set) {
+  const DevMixed& T = a.tab[set];
+  const unsigned total = a.list_identity ? unsigned(a.n) : a.ws_sched[SCHED_COUNT + set];
+  const int* list = a.ws_list + int64_t(set) * MIXED_CHUNK;
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    const unsigned base = steal(a.ws_sched + SCHED_STEAL + set * 5 + 1, 32u);
+    if (base >= total) break;
+    const unsigned i = base + unsigned(lane);
+    if (i < total) screen_body<N, K>(a, T, a.list_identity ? int64_t(i) : int64_t(list[i]), a.ws_sched + SCHED_FIXQ + set);
+  }
+}
+
+template <int N, int K>
+__global__ void __launch_bounds__(128) fix_persist(const MixedArgs a, int set) {
+  const DevMixed& T = a.tab[set];
+  const unsigned total = a.ws_sched[SCHED_FIXQ + set];
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    const unsigned base = steal(a.ws_sched + SCHED_STEAL + set * 5 + 2, 32u);
+    if (base >= total) break;
+    const unsigned i = base + unsigned(lane);
+    if (i < total) fix_body<N, K>(a, T, unsigned(a.ws_queue[i]));
+  }
+}
+
+template <int N, int K>
 __global__ void __launch_bounds__(128, 6) judge_persist(const MixedArgs a, int set) {
   const DevMixed& T = a.tab[set];
   const unsigned total = a.list_identity ? unsigned(a.n) : a.ws_sched[SCHED_COUNT + set];
   const int* list = a.ws_list + int64_t(set) * MIXED_CHUNK;
   const int lane = threadIdx.x & 31;
   for (;;) {
-    const unsigned base = steal(a.ws_sched + SCHED_STEAL + set * 3 + 1, 32u);
+    const unsigned base = steal(a.ws_sched + SCHED_STEAL + set * 5 + 3, 32u);
     if (base >= total) break;
     const unsigned i = base + unsigned(lane);
     if (i < total) {
@@ -237,7 +245,7 @@ __global__ void __launch_bounds__(128) repair_persist(const MixedArgs a, int set
   const unsigned total = a.ws_sched[SCHED_QUEUE + set];
   const int lane = threadIdx.x & 31;
   for (;;) {
-    const unsigned base = steal(a.ws_sched + SCHED_STEAL + set * 3 + 2, 32u);
+    const unsigned base = steal(a.ws_sched + SCHED_STEAL + set * 5 + 4, 32u);
     if (base >= total) break;
     const unsigned i = base + unsigned(lane);
     if (i < total) judge_repair<N, K>(a, T, int64_t(a.ws_queue[i]));
@@ -292,6 +300,10 @@ cudaError_t launch_set(const MixedArgs& a, int set, int block, int lanes, cudaSt
     default: break;
   }
   if (e != cudaSuccess) return e;
+  if (tm) tm->mark(MF_K_SCREEN, s);
+  screen_persist<N, K><<<wave(screen_persist<N, K>, 128, a), 128, 0, s>>>(a, set);
+  if (tm) tm->mark(MF_K_FIX, s);
+  fix_persist<N, K><<<wave(fix_persist<N, K>, 128, a), 128, 0, s>>>(a, set);
   if (tm) tm->mark(MF_K_JUDGE, s);
   judge_persist<N, K><<<wave(judge_persist<N, K>, 128, a), 128, 0, s>>>(a, set);
   if (tm) tm->mark(MF_K_REPAIR, s);

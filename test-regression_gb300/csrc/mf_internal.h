@@ -92,6 +92,8 @@ struct HostTables {
   float W32[KMAX * (KMAX + 1) / 2];
   double G64[KMAX * KMAX];            // G = L_R^-1 P, N x K column-major
   float G32[KMAX * KMAX];
+  float P32[KMAX * KMAX];             // P = P32 + P32lo to ~2^-48 (double-float), N x K column-major
+  float P32lo[KMAX * KMAX];
   double H64[KMAX * KMAX];            // G^T G, row-major ld KMAX
   float H32[KMAX * KMAX];
   double gnorm2[KMAX];                // |G_k|^2
@@ -110,6 +112,8 @@ struct DevMixed {
   double G64[KMAX * KMAX];
   double H64[KMAX * KMAX];
   float G32[KMAX * KMAX];
+  float P32[KMAX * KMAX];
+  float P32lo[KMAX * KMAX];
   float H32[KMAX * KMAX];
   float gnorm32[KMAX];
   int8_t gfz[KMAX];
@@ -146,8 +150,8 @@ struct MixedArgs {
   uint16_t* ws_mask;
   uint16_t* ws_count;
   float* ws_x;
-  int* ws_queue;           // channels the FP64 judge hands to the repair kernel
-  unsigned* ws_qcount;     // their number (zeroed by the search launch)
+  int* ws_queue;           // channels queued by the screen (for the fix), then by the judge (for the repair)
+  unsigned* ws_qcount;     // [0] repair queue, [1] fix queue sizes (zeroed by the search launch)
   int sms;
   // persistent schedule (fit_sched.cu): per-set channel lists [MF_MAX_CTYPES][MIXED_CHUNK]
   // and SCHED_WORDS counters (list sizes, work counters, repair-queue sizes)

@@ -149,6 +149,138 @@ __device__ __forceinline__ void gram_rhs32(const DevMixed& T, const float* y32, 
 }
 
 // ---------------------------------------------------------------------------
+// Double-float arithmetic for the search's KKT screen
+// ---------------------------------------------------------------------------
+// The FP32 search's gradient c - H x is as accurate as the FP32 solution x,
+// whose error is the FP32 table's rounding amplified by cond(G_S) (~5e4 for
+// ECAL), and no FP32 residual y - G x resolves a ~1e4 signal to its ~1 noise.
+// The screen below therefore forms y and the residual in double-float (a
+// value is an unevaluated sum hi + lo of two floats) with the error-free
+// transforms of Dekker (TwoProduct via FMA) and Knuth (TwoSum), all in FP32.
+// The _rn intrinsics keep the compiler from contracting the transforms.
+__device__ __forceinline__ void two_prod(float a, float b, float& p, float& e) {
+  p = __fmul_rn(a, b);
+  e = fmaf(a, b, -p);
+}
+
+// (hi, lo) += (p, e), renormalised.
+__device__ __forceinline__ void df_acc(float& hi, float& lo, float p, float e) {
+  const float s = __fadd_rn(hi, p);
+  const float v = __fsub_rn(s, hi);
+  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, v)), __fsub_rn(p, v));
+  const float t = __fadd_rn(__fadd_rn(err, lo), e);
+  hi = __fadd_rn(s, t);
+  lo = __fsub_rn(t, __fsub_rn(hi, s));
+}
+
+// A double as hi + lo without FP64 arithmetic: hi = its top 24 significand
+// bits (truncation), lo = the next 29 bits rounded to 24 (2^-47 relative in
+// all). Values below 2^-74 or above 2^127 keep hi alone.
+__device__ __forceinline__ void split64(double v, float& hi, float& lo) {
+  hi = __double2float_rz(v);
+  const long long b = __double_as_longlong(v);
+  const int ex = int((b >> 52) & 0x7ff);
+  lo = 0.f;
+  if (ex >= 949 && ex <= 1150) {
+    const float scale = __int_as_float((ex - 1075 + 127) << 23);  // 2^(ex - 1023 - 52)
+    lo = float(int(b & 0x1fffffffLL)) * scale;
+    if (b < 0) lo = -lo;
+  }
+}
+
+// The residual r = L_R^-1 (s - P x) of amplitudes x: u = s - P x in
+// double-float (s = sh + sl, P = P32 + P32lo, x exact floats; column by column,
+// so the N row chains interleave), then rounded to FP32 -- u is at the noise
+// level, so the FP32 whitening that follows adds only 2^-24 cond(L_R) relative
+// error (cond(L_R) = 5.7 for the ECAL correlation rho = 0.7).
+template <int N, int K>
+__device__ __forceinline__ void residual_df(const DevMixed& T, const float* sh, const float* sl, const float* x,
+                                            float* r) {
+  float uh[N], ul[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    uh[i] = sh[i];
+    ul[i] = sl[i];
+  }
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const float xk = -x[k];
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      if (i >= T.gfz[k]) {  // P and G share their structural zeros (L_R^-1 is lower triangular)
+        float p, e;
+        two_prod(T.P32[k * N + i], xk, p, e);
+        e = fmaf(T.P32lo[k * N + i], xk, e);
+        df_acc(uh[i], ul[i], p, e);
+      }
+  }
+  float u[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) u[i] = __fadd_rn(uh[i], ul[i]);
+  int w = 0;
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    float acc = 0.f;
+#pragma unroll
+    for (int j = 0; j <= i; ++j) acc = fmaf(T.W32[w + j], u[j], acc);
+    w += i + 1;
+    r[i] = acc;
+  }
+}
+
+// The KKT screen of the FP32 search's set (its own kernel between the search
+// and the judge: convergent, on the FP32 pipe, no data-dependent loop): the
+// accurate residual of the FP32 solution (residual_df), two refinement steps
+// of x on the passive set through the FP32 table (each shrinks the table's
+// error by about cond(G_S) 2^-24), the gradient w = G^T r of every column
+// outside the set; returns the mask of the columns whose gradient is
+// provably positive (w_k > 2^-16 sum_i |G_ik r_i|, a bound well above the
+// refined gradient's error) and leaves the refined amplitudes in x32 where
+// they stay feasible. solve_rhs(m, rhs, out) is the set's table solve on rhs.
+template <int N, int K, typename SolveRhs>
+__device__ __forceinline__ unsigned refine_screen(const DevMixed& T, const float* sh, const float* sl, unsigned m,
+                                                  float* x32, int& solves, SolveRhs solve_rhs) {
+  float xr[K], r[N], d[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) xr[k] = x32[k];
+  residual_df<N, K>(T, sh, sl, xr, r);
+#pragma unroll
+  for (int step = 0; step < 2; ++step) {
+    solve_rhs(m, r, d);
+#pragma unroll
+    for (int k = 0; k < K; ++k) xr[k] += d[k];
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+#pragma unroll
+      for (int i = 0; i < N; ++i)
+        if (i >= T.gfz[k]) r[i] = fmaf(-T.G32[k * N + i], d[k], r[i]);
+  }
+  solves += 2;
+  // the refined amplitudes replace the search's where they stay feasible
+  bool feasible = true;
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+    if ((m & (1u << k)) && !(xr[k] > 0.f)) feasible = false;
+  if (feasible) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) x32[k] = xr[k];
+  }
+  unsigned add = 0;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    float w = 0.f, mag = 0.f;
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      if (i >= T.gfz[k]) {
+        w = fmaf(T.G32[k * N + i], r[i], w);
+        mag = fmaf(fabsf(T.G32[k * N + i]), fabsf(r[i]), mag);
+      }
+    if (!(m & (1u << k)) && w > 0x1p-16f * mag) add |= 1u << k;
+  }
+  return add;
+}
+
+// ---------------------------------------------------------------------------
 // FP32 active-set search
 // ---------------------------------------------------------------------------
 // The FP32 search of channel ch (one lane): writes the hand-off (passive mask,
@@ -209,32 +341,6 @@ __device__ __forceinline__ void search_body(const MixedArgs& a, const DevMixed& 
     m |= 1u << imax;
     ++adds;
     solves += inner_loop<K>(m, x32, s32);
-  }
-  // Columns whose gradient FP32 cannot prove negative (within its rounding
-  // error of zero) may still carry a positive FP64 gradient, which the FP64
-  // judge's absolute threshold eps * pederr^2 would add one at a time. Add
-  // them here as a batch; the inner loop drops those that come out negative.
-  {
-    float cmag[K], cc[K];
-    gram_rhs32<N, K>(T, y32, cc, cmag);
-    unsigned amb = 0;
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      if (m & (1u << k)) continue;
-      float acc = c32[k], mag = cmag[k];
-#pragma unroll
-      for (int j = 0; j < K; ++j) {
-        const float hx = T.H32[k * KMAX + j] * x32[j];
-        acc -= hx;
-        mag += fabsf(hx);
-      }
-      if (acc >= -4e-6f * mag) amb |= 1u << k;
-    }
-    if (amb) {
-      m |= amb;
-      adds += __popc(amb);
-      solves += inner_loop<K>(m, x32, s32);
-    }
   }
   a.ws_mask[ch] = uint16_t(m);
   a.ws_count[ch] = uint16_t((adds < 255 ? adds : 255) | ((solves < 255 ? solves : 255) << 8));
@@ -420,14 +526,88 @@ __device__ __forceinline__ void judge_repair(const MixedArgs& a, const DevMixed&
   write_outputs<N, K>(a, T, ch, x, r, sig, bad, converged, adds, solves, f64);
 }
 
+// The KKT screen of channel ch (one lane, FP32, branch-free): refines the
+// search's amplitudes on its set and, when columns must be added, queues the
+// channel for fix_body (entry = ch | add mask << 21, one atomic per warp).
+template <int N, int K>
+__device__ __forceinline__ void screen_body(const MixedArgs& a, const DevMixed& T, int64_t ch, unsigned* fix_count) {
+  const unsigned m = a.ws_mask[ch];
+  float x32[K];
+  float* wx = a.ws_x + ch * K;
+#pragma unroll
+  for (int k = 0; k < K; ++k) x32[k] = wx[k];
+  const double* in = a.samples + ch * a.sample_stride;
+  float sh[N], sl[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) split64(in[i], sh[i], sl[i]);
+  int solves = 0;
+  const unsigned add = refine_screen<N, K>(T, sh, sl, m, x32, solves,
+                                           [&](unsigned mm, const float* rhs, float* out) { solve32<N, K>(T, mm, rhs, out); });
+#pragma unroll
+  for (int k = 0; k < K; ++k) wx[k] = x32[k];
+  if (add) {
+    const unsigned act = __activemask();
+    const int lane = threadIdx.x & 31, leader = __ffs(act) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(fix_count, unsigned(__popc(act)));
+    base = __shfl_sync(act, base, leader);
+    a.ws_queue[base + __popc(act & ((1u << lane) - 1u))] = int(unsigned(ch) | (add << 21));
+  }
+}
+
+// A queued channel of the screen (entry = ch | add << 21; ch < MIXED_CHUNK =
+// 2^21): the FNNLS step with the added columns in FP32 (the inner loop drops
+// those that come out non-positive), then one more screen round and, if it
+// finds more, one more step. Writes the hand-off for the judge.
+template <int N, int K>
+__device__ __forceinline__ void fix_body(const MixedArgs& a, const DevMixed& T, unsigned entry) {
+  const int64_t ch = int64_t(entry & 0x1fffffu);
+  unsigned add = entry >> 21;
+  unsigned m = a.ws_mask[ch];
+  const unsigned cnt = a.ws_count[ch];
+  int adds = int(cnt & 255u), solves = int(cnt >> 8);
+  float x32[K];
+  float* wx = a.ws_x + ch * K;
+#pragma unroll
+  for (int k = 0; k < K; ++k) x32[k] = wx[k];
+  const double* in = a.samples + ch * a.sample_stride;
+  float sh[N], sl[N], y32[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) split64(in[i], sh[i], sl[i]);
+  {
+    int w = 0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      float acc = 0.f;
+#pragma unroll
+      for (int j = 0; j <= i; ++j) acc = fmaf(T.W32[w + j], sh[j], acc);
+      w += i + 1;
+      y32[i] = acc;
+    }
+  }
+  auto s32 = [&](unsigned mm, float* out) { solve32<N, K>(T, mm, y32, out); };
+  auto srhs = [&](unsigned mm, const float* rhs, float* out) { solve32<N, K>(T, mm, rhs, out); };
+#pragma unroll 1
+  for (int round = 0; round < 2 && add; ++round) {
+    m |= add;
+    adds += __popc(add);
+    solves += inner_loop<K>(m, x32, s32);
+    add = round == 0 ? refine_screen<N, K>(T, sh, sl, m, x32, solves, srhs) : 0u;
+  }
+  a.ws_mask[ch] = uint16_t(m);
+  a.ws_count[ch] = uint16_t((adds < 255 ? adds : 255) | ((solves < 255 ? solves : 255) << 8));
+#pragma unroll
+  for (int k = 0; k < K; ++k) wx[k] = x32[k];
+}
+
 // The FP64 judge of channel ch (one lane): writes the outputs, or appends the
 // channel to the repair queue (ws_queue, counted in *qcount).
 template <int N, int K>
 __device__ __forceinline__ void judge_body(const MixedArgs& a, const DevMixed& T, int64_t ch, unsigned* qcount) {
-  double y[N], sig;
-  const bool bad = whiten64<N>(a, T, ch, y, sig);
   const unsigned m = a.ws_mask[ch];
   const unsigned cnt = a.ws_count[ch];
+  double y[N], sig;
+  const bool bad = whiten64<N>(a, T, ch, y, sig);
   // common path, straight-line: the FP64 solve on the FP32 passive set, the
   // residual and gradient, the KKT test max w < eps * pederr^2
   double x[K], r[N];

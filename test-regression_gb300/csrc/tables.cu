@@ -116,6 +116,8 @@ int build_mixed_tables(const DevConditions& c, HostTables* t) {
   for (int e = 0; e < N * K; ++e) {
     t->G64[e] = double(G[e]);
     t->G32[e] = float(G[e]);
+    t->P32[e] = float(c.P[e]);
+    t->P32lo[e] = float(c.P[e] - double(t->P32[e]));
   }
   for (int i = 0; i < K; ++i) {
     ld nrm = 0;

@@ -108,8 +108,8 @@ def test_profile_counts_persistent_launches(mf, cuda):
     eng.fit_device(db.batch, opts(mf, schedule=mf.SCHED_PERSISTENT))
     rec = eng.profile_read()
     eng.profile(False)
-    assert {k: v[0] for k, v in rec.items()} == {"partition_kernel": 1, "search_kernel": 2, "judge_kernel": 2,
-                                                  "repair_kernel": 2}
+    assert {k: v[0] for k, v in rec.items()} == {"partition_kernel": 1, "search_kernel": 2, "screen_kernel": 2, "fix_kernel": 2,
+                                                  "judge_kernel": 2, "repair_kernel": 2}
     eng.close()
 
 
