@@ -168,8 +168,11 @@ WORKLOAD_DESC = {
 
 FORM_DESC = {
     "fp64": "plain-fp64 drop-in (bit-identical to the oracle)",
-    "mixed": "mixed precision: FP32 active-set search + FP64 judge/solve/chi2, KKT-converged",
-    "warm": "learned warm start: BF16 tensor-core MLP + mixed-precision FNNLS to KKT",
+    "mixed": "mixed precision: FP32 active-set search + double-float screen + FP64 judge (solve, residual, "
+             "chi2), KKT-converged",
+    "fp32": "FP32: FP32 active-set search + double-float screen and judge (FP32 error-free transforms), "
+            "FP64 repair of the rare rejects, KKT-converged",
+    "warm": "learned warm start: BF16 tensor-core MLP + the FP32 form (double-float judge) to KKT",
 }
 # useful FLOPs of one warm-start prediction: 12 inputs -> 128 -> 128 -> 20
 # outputs, 2 per multiply-add (the network pads to 16 inputs and 32 outputs)
@@ -188,7 +191,9 @@ def form_options(mf, args, mixed_sets=False):
     sched = schedule_of(mf, args, mixed_sets)
     if args.form == "mixed":
         return mf.default_options(precision=mf.PREC_MIXED, max_iter_nnls=1000, schedule=sched)
-    return mf.default_options(precision=mf.PREC_MIXED, warm_start=mf.WARM_MLP, max_iter_nnls=1000, schedule=sched)
+    if args.form == "fp32":
+        return mf.default_options(precision=mf.PREC_FP32, max_iter_nnls=1000, schedule=sched)
+    return mf.default_options(precision=mf.PREC_FP32, warm_start=mf.WARM_MLP, max_iter_nnls=1000, schedule=sched)
 
 
 def train_warm_start(mf, eng, torch, args, rank):
@@ -216,6 +221,40 @@ def train_warm_start(mf, eng, torch, args, rank):
     return {"channels": n, "generator": "log-uniform [0.1,1000] GeV, pileup 4, seed 5", "epochs": tp.epochs,
             "batch": tp.batch, "lr": tp.lr, "epoch_loss": [float(x) for x in losses],
             "target_fit_s": t1 - t0, "train_s": t2 - t1}
+
+
+def fp32_peak_tflops(torch) -> float:
+    """cuBLAS SGEMM (TF32 off) measured in this run: the FP32-pipe roofline."""
+    n = 8192
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    a = torch.randn((n, n), dtype=torch.float32, device="cuda")
+    b = torch.randn((n, n), dtype=torch.float32, device="cuda")
+    best = 0.0
+    for _ in range(3):
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = max(best, 2.0 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    torch.backends.cuda.matmul.allow_tf32 = prev
+    return best
+
+
+def judge_df_flops(P) -> int:
+    """FP32 flops of the double-float judge per channel of a set with pulse
+    matrix P (N x K): 17 per emulated FMA (TwoProduct 3, two cross FMAs 4,
+    renormalised sum 10) over the whitening N(N+1)/2, the dense table solve
+    K N and the residual over G's structural non-zeros, plus the FP32 KKT
+    screen (4 K N) and the double-float chi2 (15 N)."""
+    import numpy as np
+
+    N, K = P.shape
+    nnz = int(sum(N - int(np.argmax(P[:, k] != 0)) if (P[:, k] != 0).any() else 0 for k in range(K)))
+    return 17 * (N * (N + 1) // 2 + K * N + nnz) + 4 * K * N + 15 * N
 
 
 def fp64_peak_tflops(torch) -> float:
@@ -464,10 +503,11 @@ def run_ours(args, world, rank, local):
 
     peaks, peak_src = measured_peaks()
     fp64_peak = fp64_peak_tflops(torch)
+    fp32_peak = fp32_peak_tflops(torch)
     bytes_per_launch = n * (10 * 8 + 8) + n * (10 * 8 + 8 + 8 + 2 + 1)
     hbm_gbs = bytes_per_launch / (step_ms * 1e-3) / 1e9
     kernel_table = kernel_rooflines(mf, eng, kernels, args, n, ctype, flops_per_launch, form_fp64_flops,
-                                    fp64_peak, peaks, peak_src, step_ms)
+                                    fp64_peak, fp32_peak, peaks, peak_src, step_ms)
     dominant = max(kernel_table, key=lambda k: kernel_table[k]["ms_per_step"])
     roof = dict(kernel_table[dominant])
     roof["kernel"] = dominant
@@ -488,7 +528,8 @@ def run_ours(args, world, rank, local):
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": {"fp64": "f64", "mixed": "f32+f64", "warm": "f32+f64 (bf16 MLP)"}[args.form],
+            "dtype": {"fp64": "f64", "mixed": "f32+f64", "fp32": "f32 (double-float judge; f64 repair)",
+                      "warm": "f32 (double-float judge; f64 repair; bf16 MLP)"}[args.form],
             "data": "synthetic (seeded Philox generator; BASELINE shapes and distributions)",
             "config": {
                 "workload": wl,
@@ -526,8 +567,8 @@ def run_ours(args, world, rank, local):
     return out
 
 
-def kernel_rooflines(mf, eng, kernels, args, n, ctype, plain_flops, form_fp64_flops, fp64_peak, peaks, peak_src,
-                     step_ms):
+def kernel_rooflines(mf, eng, kernels, args, n, ctype, plain_flops, form_fp64_flops, fp64_peak, fp32_peak, peaks,
+                     peak_src, step_ms):
     """Roofline of every kernel launched in the timed region: its algorithmic
     work per launch over its mean launch time (CUDA events from mf_profile).
 
@@ -545,13 +586,16 @@ def kernel_rooflines(mf, eng, kernels, args, n, ctype, plain_flops, form_fp64_fl
     if ctype is not None:
         ct = np.bincount(ctype.cpu().numpy(), minlength=2)
         counts = {0: int(ct[0]), 1: int(ct[1])}
-    judge = 0.0
+    judge = 0.0      # FP64 flops of the FP64 judge
+    judge_df = 0.0   # FP32 flops of the double-float judge
     for t, m in counts.items():
         c = eng.conditions.get(t)
         if c is None:
             continue
         N, K = c.nsamples, c.npulses
         judge += m * (N * (N + 1) + 4 * N * K)
+        judge_df += m * judge_df_flops(mf.conditions_arrays(c)[0])
+    df_form = args.form in ("fp32", "warm")
     warm = args.form == "warm"
     out = {}
     for name, (launches, total) in kernels.items():
@@ -560,10 +604,14 @@ def kernel_rooflines(mf, eng, kernels, args, n, ctype, plain_flops, form_fp64_fl
         mean_s = total / launches * 1e-3
         if name == "fit_fp64_kernel":
             work, bound, peak, unit = plain_flops / per_step, "fp64", fp64_peak, "TFLOP/s"
+        elif name == "judge_kernel" and df_form:
+            work, bound, peak, unit = judge_df / per_step, "fp32", fp32_peak, "TFLOP/s"
         elif name == "judge_kernel":
             work, bound, peak, unit = judge / per_step, "fp64", fp64_peak, "TFLOP/s"
         elif name == "repair_kernel":
-            work, bound, peak, unit = max(form_fp64_flops - judge, 0.0) / per_step, "fp64", fp64_peak, "TFLOP/s"
+            # the FP64 judge's share of the counted FP64 flops belongs to the judge (its repairs redo it)
+            rest = form_fp64_flops - (0.0 if df_form else judge)
+            work, bound, peak, unit = max(rest, 0.0) / per_step, "fp64", fp64_peak, "TFLOP/s"
         elif name == "mlp_infer_kernel":
             work = n * MLP_FLOPS_PER_CHANNEL / per_step
             bound, peak, unit = "tensor", peaks["bf16_tflops"], "TFLOP/s"
@@ -581,7 +629,8 @@ def kernel_rooflines(mf, eng, kernels, args, n, ctype, plain_flops, form_fp64_fl
                      "traffic": None, "launches_per_step": per_step, "ms_per_step": ms,
                      "share": ms / step_ms, "work_per_launch": work,
                      "peak_source": ("cuBLAS DGEMM 4096^3 measured in this run (FP64 pipe)" if bound == "fp64"
-                                     else f"MEASURED_PEAKS.json ({peak_src})")}
+                                     else "cuBLAS SGEMM 8192^3, TF32 off, measured in this run (FP32 pipe)"
+                                     if bound == "fp32" else f"MEASURED_PEAKS.json ({peak_src})")}
     return out
 
 
@@ -688,7 +737,7 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--form", choices=["warm", "mixed", "fp64"], default="warm")
+    ap.add_argument("--form", choices=["warm", "fp32", "mixed", "fp64"], default="warm")
     ap.add_argument("--schedule", choices=["auto", "grid", "persistent"], default="auto",
                     help="auto: persistent work stealing for workloads of several condition sets "
                          "(mixed/warm forms), else grid")

@@ -68,7 +68,9 @@ enum mf_channel_status {
 /* Arithmetic of the fit. */
 enum mf_precision {
   MF_PREC_FP64 = 0,  /* plain FP64, bit-identical to the CPU oracle's canonical order */
-  MF_PREC_MIXED = 1  /* FP32 factor/whitening/FNNLS, FP64 residual, chi2 and refinement */
+  MF_PREC_MIXED = 1, /* FP32 search and screen; FP64 refinement solve, residual and chi2 (the judge) */
+  MF_PREC_FP32 = 2   /* FP32 throughout: the judge's solve, residual and chi2 in double-float FP32
+                        arithmetic (~2^-48 per operation); FP64 only for the rare repaired channels */
 };
 
 /* How channels are scheduled onto the GPU. */

@@ -33,7 +33,7 @@ OK, EINVAL, ECUDA, ETIMEOUT, ENOMEM, EUNSUPPORTED, ENOTRAINED = range(7)
 # channel status bits
 CH_NNLS_MAXITER, CH_OUTER_MAXITER, CH_NONFINITE, CH_BADINPUT = 1, 2, 4, 8
 # options
-PREC_FP64, PREC_MIXED = 0, 1
+PREC_FP64, PREC_MIXED, PREC_FP32 = 0, 1, 2
 SCHED_GRID, SCHED_PERSISTENT = 0, 1
 WARM_NONE, WARM_MLP = 0, 1
 START_REFERENCE, START_SUPPORT = 0, 1

@@ -71,6 +71,7 @@ struct mf_context {
   int* d_offset[MF_MAX_CTYPES] = {nullptr, nullptr};
   double* d_pinv64[MF_MAX_CTYPES] = {nullptr, nullptr};
   float* d_pinv32[MF_MAX_CTYPES] = {nullptr, nullptr};
+  float* d_pinv32lo[MF_MAX_CTYPES] = {nullptr, nullptr};
   MlpState mlp;
   int sms = 152;
   // mixed-form hand-off workspace (MIXED_CHUNK channels), allocated with the tables
@@ -116,7 +117,8 @@ int check_options(const mf_options* o) {
   if (!o) return MF_EINVAL;
   if (o->max_iter_nnls < 0 || o->max_iter_outer < 0) return MF_EINVAL;
   if (!(o->dchi2_tol >= 0) || !(o->nnls_eps >= 0)) return MF_EINVAL;
-  if (o->precision != MF_PREC_FP64 && o->precision != MF_PREC_MIXED) return MF_EINVAL;
+  if (o->precision != MF_PREC_FP64 && o->precision != MF_PREC_MIXED && o->precision != MF_PREC_FP32)
+    return MF_EINVAL;
   if (o->schedule != MF_SCHED_GRID && o->schedule != MF_SCHED_PERSISTENT) return MF_EINVAL;
   if (o->warm_start != MF_WARM_NONE && o->warm_start != MF_WARM_MLP) return MF_EINVAL;
   if (o->nnls_start != MF_START_REFERENCE && o->nnls_start != MF_START_SUPPORT) return MF_EINVAL;
@@ -212,6 +214,7 @@ int dispatch_mixed(mf_context* c, const FitArgs& a, const mf_options* o, cudaStr
   m.ws_sched = c->ws_sched;
   m.blocks_per_sm = o->blocks_per_sm;
   m.list_identity = a.ctype == nullptr ? 1 : 0;
+  m.judge_df = o->precision == MF_PREC_FP32 ? 1 : 0;
   if (!m.ws_mask || !m.ws_list) return MF_ENOMEM;
   MlpInferArgs ia;
   std::memset(&ia, 0, sizeof(ia));
@@ -306,7 +309,7 @@ int dispatch_mixed(mf_context* c, const FitArgs& a, const mf_options* o, cudaStr
 
 int dispatch_form(mf_context* c, const FitArgs& a, const mf_options* o, cudaStream_t s, bool instrumented,
                   bool allow_graph) {
-  if (o->precision == MF_PREC_MIXED) return dispatch_mixed(c, a, o, s, allow_graph);
+  if (o->precision == MF_PREC_MIXED || o->precision == MF_PREC_FP32) return dispatch_mixed(c, a, o, s, allow_graph);
   if (o->precision != MF_PREC_FP64 || o->schedule != MF_SCHED_GRID || o->warm_start != MF_WARM_NONE)
     return MF_EUNSUPPORTED;
   cudaError_t e = launch_fit_fp64(a, o->block_size, s, instrumented, &c->timer);
@@ -358,6 +361,8 @@ void free_tables(mf_context* c, int t) {
   cudaFree(c->d_offset[t]);
   cudaFree(c->d_pinv64[t]);
   cudaFree(c->d_pinv32[t]);
+  cudaFree(c->d_pinv32lo[t]);
+  c->d_pinv32lo[t] = nullptr;
   c->d_offset[t] = nullptr;
   c->d_pinv64[t] = nullptr;
   c->d_pinv32[t] = nullptr;
@@ -380,9 +385,12 @@ int upload_tables(mf_context* c, int t) {
   if (e == cudaSuccess) e = cudaMalloc(&c->d_offset[t], sizeof(int) * no);
   if (e == cudaSuccess) e = cudaMalloc(&c->d_pinv64[t], sizeof(double) * np);
   if (e == cudaSuccess) e = cudaMalloc(&c->d_pinv32[t], sizeof(float) * np);
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_pinv32lo[t], sizeof(float) * np);
   if (e == cudaSuccess) e = cudaMemcpy(c->d_offset[t], h.offset.data(), sizeof(int) * no, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(c->d_pinv64[t], h.pinv64.data(), sizeof(double) * np, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(c->d_pinv32[t], h.pinv32.data(), sizeof(float) * np, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(c->d_pinv32lo[t], h.pinv32lo.data(), sizeof(float) * np, cudaMemcpyHostToDevice);
   if (e == cudaSuccess && !c->ws_mask) {
     e = cudaMalloc(&c->ws_mask, sizeof(uint16_t) * MIXED_CHUNK);
     if (e == cudaSuccess) e = cudaMalloc(&c->ws_count, sizeof(uint16_t) * MIXED_CHUNK);
@@ -410,9 +418,11 @@ void fill_dev_mixed(const mf_context* c, int t, DevMixed* m) {
   m->intime_col = c->cond[t].intime_col;
   std::memcpy(m->W64, h.W64, sizeof(h.W64));
   std::memcpy(m->W32, h.W32, sizeof(h.W32));
+  std::memcpy(m->W32lo, h.W32lo, sizeof(h.W32lo));
   std::memcpy(m->G64, h.G64, sizeof(h.G64));
   std::memcpy(m->H64, h.H64, sizeof(h.H64));
   std::memcpy(m->G32, h.G32, sizeof(h.G32));
+  std::memcpy(m->G32lo, h.G32lo, sizeof(h.G32lo));
   std::memcpy(m->P32, h.P32, sizeof(h.P32));
   std::memcpy(m->P32lo, h.P32lo, sizeof(h.P32lo));
   std::memcpy(m->H32, h.H32, sizeof(h.H32));
@@ -424,6 +434,7 @@ void fill_dev_mixed(const mf_context* c, int t, DevMixed* m) {
   m->offset = c->d_offset[t];
   m->pinv64 = c->d_pinv64[t];
   m->pinv32 = c->d_pinv32[t];
+  m->pinv32lo = c->d_pinv32lo[t];
 }
 
 int grow_staging(mf_context* c, int64_t n, int ss, int as) {
@@ -946,10 +957,10 @@ extern "C" int mf_fit_noalloc(mf_context* c, const mf_batch* b, const mf_options
   FitArgs a;
   int rc = fill_args(c, b, o, &a);
   if (rc) return rc;
-  if (o->precision != MF_PREC_MIXED || o->warm_start != MF_WARM_NONE || o->compute_errors ||
-      o->schedule != MF_SCHED_GRID) {
+  if ((o->precision != MF_PREC_MIXED && o->precision != MF_PREC_FP32) || o->warm_start != MF_WARM_NONE ||
+      o->compute_errors || o->schedule != MF_SCHED_GRID) {
     std::snprintf(g_last_error, sizeof(g_last_error),
-                  "mf_fit_noalloc: only the mixed precision, cold start, grid schedule, no errors");
+                  "mf_fit_noalloc: only the mixed or FP32 precision, cold start, grid schedule, no errors");
     return MF_EUNSUPPORTED;
   }
   if (b->n > kNoallocMax) {
@@ -1003,6 +1014,7 @@ extern "C" int mf_fit_noalloc(mf_context* c, const mf_batch* b, const mf_options
   m.ws_count = reinterpret_cast<uint16_t*>(scratch + kOffCount);
   m.ws_qcount = reinterpret_cast<unsigned*>(scratch + kOffQcount);
   m.sms = c->sms;
+  m.judge_df = o->precision == MF_PREC_FP32 ? 1 : 0;
   e = launch_fit_mixed(m, o->block_size, (cudaStream_t)stream);
   if (e != cudaSuccess) {
     set_last_error("mf_fit_noalloc launch", e);

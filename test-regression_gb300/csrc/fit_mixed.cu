@@ -17,7 +17,8 @@
 //     columns the FP32 search missed for
 //   fix_kernel     (FP32, compacted): their FNNLS step and one more screen,
 //     so that few channels need the FP64 repair.
-//   judge_kernel   (FP64, lean, branch-free: every lane the same FP64
+//   judge_kernel   (FP64 -- or, for MF_PREC_FP32, the same steps in double-float
+//     FP32 arithmetic; lean, branch-free: every lane the same FP64
 //     instructions): y in FP64, the FP64 solve on the FP32 passive set, the
 //     FP64 residual, chi2 = ||y - G x||^2 / pederr^2, and the KKT test
 //     max w < eps * pederr^2 (the reference's absolute eps on the
@@ -78,8 +79,8 @@ __global__ void __launch_bounds__(128) fix_kernel(const MixedArgs a, int set) {
     fix_body<N, K>(a, T, unsigned(a.ws_queue[i]));
 }
 
-template <int N, int K>
-__global__ void __launch_bounds__(128, 6) judge_kernel(const MixedArgs a, int set, int flag_bad) {
+template <int N, int K, bool DF>
+__global__ void __launch_bounds__(128, DF ? 4 : 6) judge_kernel(const MixedArgs a, int set, int flag_bad) {
   const int64_t ch = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (ch >= a.n) return;
   const int t = a.ctype ? int(a.ctype[ch]) : 0;
@@ -91,7 +92,8 @@ __global__ void __launch_bounds__(128, 6) judge_kernel(const MixedArgs a, int se
     return;
   }
   if (t != set) return;
-  judge_body<N, K>(a, a.tab[set], ch, a.ws_qcount);
+  if constexpr (DF) judge_df_body<N, K>(a, a.tab[set], ch, a.ws_qcount);
+  else judge_body<N, K>(a, a.tab[set], ch, a.ws_qcount);
 }
 
 // Channels the judge queued, in full warps: an FP64 warp instruction costs the
@@ -134,7 +136,8 @@ cudaError_t launch_fit_mixed(const MixedArgs& a, int block, cudaStream_t s, Laun
       mark(MF_K_FIX);
       fix_kernel<10, 10><<<rgrid, 128, 0, s>>>(a, t);
       mark(MF_K_JUDGE);
-      judge_kernel<10, 10><<<jgrid, 128, 0, s>>>(a, t, flag_bad);
+      if (a.judge_df) judge_kernel<10, 10, true><<<jgrid, 128, 0, s>>>(a, t, flag_bad);
+      else judge_kernel<10, 10, false><<<jgrid, 128, 0, s>>>(a, t, flag_bad);
       mark(MF_K_REPAIR);
       repair_kernel<10, 10><<<rgrid, 128, 0, s>>>(a, t);
     } else if (T.N == 8 && T.K == 8) {
@@ -145,7 +148,8 @@ cudaError_t launch_fit_mixed(const MixedArgs& a, int block, cudaStream_t s, Laun
       mark(MF_K_FIX);
       fix_kernel<8, 8><<<rgrid, 128, 0, s>>>(a, t);
       mark(MF_K_JUDGE);
-      judge_kernel<8, 8><<<jgrid, 128, 0, s>>>(a, t, flag_bad);
+      if (a.judge_df) judge_kernel<8, 8, true><<<jgrid, 128, 0, s>>>(a, t, flag_bad);
+      else judge_kernel<8, 8, false><<<jgrid, 128, 0, s>>>(a, t, flag_bad);
       mark(MF_K_REPAIR);
       repair_kernel<8, 8><<<rgrid, 128, 0, s>>>(a, t);
     } else {

@@ -222,8 +222,8 @@ __global__ void __launch_bounds__(128) fix_persist(const MixedArgs a, int set) {
   }
 }
 
-template <int N, int K>
-__global__ void __launch_bounds__(128, 6) judge_persist(const MixedArgs a, int set) {
+template <int N, int K, bool DF>
+__global__ void __launch_bounds__(128, DF ? 4 : 6) judge_persist(const MixedArgs a, int set) {
   const DevMixed& T = a.tab[set];
   const unsigned total = a.list_identity ? unsigned(a.n) : a.ws_sched[SCHED_COUNT + set];
   const int* list = a.ws_list + int64_t(set) * MIXED_CHUNK;
@@ -234,7 +234,8 @@ __global__ void __launch_bounds__(128, 6) judge_persist(const MixedArgs a, int s
     const unsigned i = base + unsigned(lane);
     if (i < total) {
       const int64_t ch = a.list_identity ? int64_t(i) : int64_t(list[i]);
-      judge_body<N, K>(a, T, ch, a.ws_sched + SCHED_QUEUE + set);
+      if constexpr (DF) judge_df_body<N, K>(a, T, ch, a.ws_sched + SCHED_QUEUE + set);
+      else judge_body<N, K>(a, T, ch, a.ws_sched + SCHED_QUEUE + set);
     }
   }
 }
@@ -305,7 +306,8 @@ cudaError_t launch_set(const MixedArgs& a, int set, int block, int lanes, cudaSt
   if (tm) tm->mark(MF_K_FIX, s);
   fix_persist<N, K><<<wave(fix_persist<N, K>, 128, a), 128, 0, s>>>(a, set);
   if (tm) tm->mark(MF_K_JUDGE, s);
-  judge_persist<N, K><<<wave(judge_persist<N, K>, 128, a), 128, 0, s>>>(a, set);
+  if (a.judge_df) judge_persist<N, K, true><<<wave(judge_persist<N, K, true>, 128, a), 128, 0, s>>>(a, set);
+  else judge_persist<N, K, false><<<wave(judge_persist<N, K, false>, 128, a), 128, 0, s>>>(a, set);
   if (tm) tm->mark(MF_K_REPAIR, s);
   repair_persist<N, K><<<wave(repair_persist<N, K>, 128, a), 128, 0, s>>>(a, set);
   return cudaGetLastError();

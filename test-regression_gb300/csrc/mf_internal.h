@@ -90,8 +90,10 @@ struct HostTables {
   int N = 0, K = 0;
   double W64[KMAX * (KMAX + 1) / 2];  // L_R^-1, packed lower rows
   float W32[KMAX * (KMAX + 1) / 2];
+  float W32lo[KMAX * (KMAX + 1) / 2];  // W = W32 + W32lo to ~2^-48 (double-float)
   double G64[KMAX * KMAX];            // G = L_R^-1 P, N x K column-major
   float G32[KMAX * KMAX];
+  float G32lo[KMAX * KMAX];
   float P32[KMAX * KMAX];             // P = P32 + P32lo to ~2^-48 (double-float), N x K column-major
   float P32lo[KMAX * KMAX];
   double H64[KMAX * KMAX];            // G^T G, row-major ld KMAX
@@ -101,6 +103,7 @@ struct HostTables {
   std::vector<int> offset;            // per passive-set mask: offset of its p x N pseudo-inverse
   std::vector<double> pinv64;
   std::vector<float> pinv32;
+  std::vector<float> pinv32lo;        // pinv64 = pinv32 + pinv32lo to ~2^-48
 };
 int build_mixed_tables(const DevConditions& c, HostTables* t);
 
@@ -109,9 +112,11 @@ struct DevMixed {
   int N, K, intime_col;
   double W64[KMAX * (KMAX + 1) / 2];
   float W32[KMAX * (KMAX + 1) / 2];
+  float W32lo[KMAX * (KMAX + 1) / 2];
   double G64[KMAX * KMAX];
   double H64[KMAX * KMAX];
   float G32[KMAX * KMAX];
+  float G32lo[KMAX * KMAX];
   float P32[KMAX * KMAX];
   float P32lo[KMAX * KMAX];
   float H32[KMAX * KMAX];
@@ -121,6 +126,7 @@ struct DevMixed {
   const int* offset;
   const double* pinv64;
   const float* pinv32;
+  const float* pinv32lo;
 };
 
 struct MixedArgs {
@@ -159,6 +165,7 @@ struct MixedArgs {
   unsigned* ws_sched;
   int blocks_per_sm;       // cap on resident blocks per SM (0: the occupancy limit)
   int list_identity;       // one condition set, no ctype: the list is 0..n-1 (no partition pass)
+  int judge_df;            // MF_PREC_FP32: the judge in double-float FP32 arithmetic instead of FP64
 };
 constexpr int SCHED_WORDS = 16;
 // Channels per chunk of a mixed fit (the size of the hand-off workspace).

@@ -444,17 +444,11 @@ __device__ __forceinline__ bool whiten64(const MixedArgs& a, const DevMixed& T, 
   return bad;
 }
 
-// Outputs of a judged channel: amplitudes, chi2 from the residual, in-time
-// amplitude, active mask (support of x), status, counters, FP64 flops.
+// Outputs of a judged channel: amplitudes, chi2, in-time amplitude, active
+// mask (support of x), status, counters, FP64 flops.
 template <int N, int K>
-__device__ __forceinline__ void write_outputs(const MixedArgs& a, const DevMixed& T, int64_t ch, const double* x,
-                                              const double* r, double sig, bool bad, bool converged, int adds,
-                                              int solves, int f64) {
-  double chi2 = 0.;
-#pragma unroll
-  for (int i = 0; i < N; ++i) chi2 = fma(r[i], r[i], chi2);
-  chi2 = chi2 / (sig * sig);
-  f64 += 2 * N + 2;
+__device__ __forceinline__ void store_outputs(const MixedArgs& a, const DevMixed& T, int64_t ch, const double* x,
+                                              double chi2, bool bad, bool converged, int adds, int solves, int f64) {
   double* out = a.amplitudes + ch * a.amp_stride;
   bool finite = isfinite(chi2);
   uint16_t support = 0;
@@ -481,6 +475,18 @@ __device__ __forceinline__ void write_outputs(const MixedArgs& a, const DevMixed
     a.iters[ch] = 1 | (fo << 8) | (fi << 20);
   }
   if (a.flops) a.flops[ch] = double(f64);
+}
+
+// The same with chi2 = ||r||^2 / pederr^2 from the FP64 residual.
+template <int N, int K>
+__device__ __forceinline__ void write_outputs(const MixedArgs& a, const DevMixed& T, int64_t ch, const double* x,
+                                              const double* r, double sig, bool bad, bool converged, int adds,
+                                              int solves, int f64) {
+  double chi2 = 0.;
+#pragma unroll
+  for (int i = 0; i < N; ++i) chi2 = fma(r[i], r[i], chi2);
+  chi2 = chi2 / (sig * sig);
+  store_outputs<N, K>(a, T, ch, x, chi2, bad, converged, adds, solves, f64 + 2 * N + 2);
 }
 
 // The repair path (the FP64 solve on the FP32 set has a non-positive
@@ -629,6 +635,134 @@ __device__ __forceinline__ void judge_body(const MixedArgs& a, const DevMixed& T
   }
   write_outputs<N, K>(a, T, ch, x, r, sig, bad, true, int(cnt & 255u), int(cnt >> 8) + 1,
                       N * (N + 1) + 4 * N * K);
+}
+
+
+// ---------------------------------------------------------------------------
+// The judge in double-float FP32 arithmetic (MF_PREC_FP32)
+// ---------------------------------------------------------------------------
+// The FP64 judge's steps -- y = L_R^-1 s, the solve x = G_S^+ y from the
+// operator table, the residual r = y - G x, chi2 -- with every value an
+// unevaluated float pair (hi + lo) and every product and sum through the
+// error-free transforms above: ~2^-48 relative per operation against FP64's
+// 2^-53, so amplitudes keep ~cond(G_S) 2^-48 (< 1e-9) relative accuracy. An
+// emulated FMA costs ~17 FP32 flops, but on this GPU the FP32 pipe is ~64x
+// the FP64 pipe. The KKT test is the FP64 judge's (FP32 screen with the
+// 2^-19 rounding bound); rejected channels go to the same FP64 repair.
+
+// acc += (ah + al) (bh + bl), dropping al * bl (2^-48 relative).
+__device__ __forceinline__ void df_fma(float& hi, float& lo, float ah, float al, float bh, float bl) {
+  float p, e;
+  two_prod(ah, bh, p, e);
+  e = fmaf(ah, bl, e);
+  e = fmaf(al, bh, e);
+  df_acc(hi, lo, p, e);
+}
+
+// A finite double, decided on its exponent bits (no FP64 instruction).
+__device__ __forceinline__ bool finite64(double v) {
+  return ((__double2hiint(v) >> 20) & 0x7ff) != 0x7ff;
+}
+
+template <int N, int K>
+__device__ __forceinline__ void judge_df_body(const MixedArgs& a, const DevMixed& T, int64_t ch, unsigned* qcount) {
+  const unsigned m = a.ws_mask[ch];
+  const unsigned cnt = a.ws_count[ch];
+  const double* in = a.samples + ch * a.sample_stride;
+  const double sig = a.pederr[ch];
+  bool bad = !finite64(sig) || !pos64(sig);
+  float sh[N], sl[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    bad = bad || !finite64(in[i]);
+    split64(in[i], sh[i], sl[i]);
+  }
+  // y = L_R^-1 s
+  float yh[N], yl[N];
+  {
+    int w = 0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      float hi = 0.f, lo = 0.f;
+#pragma unroll
+      for (int j = 0; j <= i; ++j) df_fma(hi, lo, T.W32[w + j], T.W32lo[w + j], sh[j], sl[j]);
+      w += i + 1;
+      yh[i] = hi;
+      yl[i] = lo;
+    }
+  }
+  // x = G_S^+ y through the table's float pairs (rows outside the set read the zero row)
+  float xh[K], xl[K];
+  {
+    const int off = __ldg(T.offset + m);
+    int r = 0;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const bool inset = (m >> k) & 1u;
+      const int row = inset ? off + r * N : T.zero_row;
+      r += inset ? 1 : 0;
+      float hi = 0.f, lo = 0.f;
+#pragma unroll
+      for (int i = 0; i < N; ++i) df_fma(hi, lo, __ldg(T.pinv32 + row + i), __ldg(T.pinv32lo + row + i), yh[i], yl[i]);
+      xh[k] = hi;
+      xl[k] = lo;
+    }
+  }
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+    if ((m & (1u << k)) && !(xh[k] > 0.f || (xh[k] == 0.f && xl[k] > 0.f))) ok = false;
+  // r = y - G x
+  float rh[N], rl[N], rf[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    rh[i] = yh[i];
+    rl[i] = yl[i];
+  }
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      if (i >= T.gfz[k]) df_fma(rh[i], rl[i], -T.G32[k * N + i], -T.G32lo[k * N + i], xh[k], xl[k]);
+#pragma unroll
+  for (int i = 0; i < N; ++i) rf[i] = __fadd_rn(rh[i], rl[i]);
+  if (ok) {
+    const float tol = float(a.eps * sig * sig);
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      float w = 0.f, mag = 0.f;
+#pragma unroll
+      for (int i = 0; i < N; ++i)
+        if (i >= T.gfz[k]) {
+          w = fmaf(T.G32[k * N + i], rf[i], w);
+          mag = fmaf(fabsf(T.G32[k * N + i]), fabsf(rf[i]), mag);
+        }
+      if (!(m & (1u << k)) && !(fmaf(0x1p-19f, mag, w) < tol)) ok = false;
+    }
+  }
+  if (!ok) {
+    const unsigned act = __activemask();
+    const int lane = threadIdx.x & 31, leader = __ffs(act) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(qcount, unsigned(__popc(act)));
+    base = __shfl_sync(act, base, leader);
+    a.ws_queue[base + __popc(act & ((1u << lane) - 1u))] = int(ch);
+    return;
+  }
+  // chi2 = ||r||^2 / pederr^2, the sum in double-float
+  float ch2 = 0.f, cl2 = 0.f;
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    float p, e;
+    two_prod(rh[i], rh[i], p, e);
+    e = fmaf(2.f * rh[i], rl[i], e);
+    df_acc(ch2, cl2, p, e);
+  }
+  double x[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) x[k] = double(xh[k]) + double(xl[k]);
+  const double chi2 = (double(ch2) + double(cl2)) / (sig * sig);
+  store_outputs<N, K>(a, T, ch, x, chi2, bad, true, int(cnt & 255u), int(cnt >> 8) + 1, K + 4);
 }
 
 }  // namespace

@@ -10,7 +10,8 @@
 // pseudo-inverse G_S^+ = (G_S^T G_S)^-1 G_S^T, which depends on S only. The
 // engine therefore builds, once per condition set, the pseudo-inverse of
 // every non-empty S (columns in ascending order) by Householder QR in long
-// double, and stores it in FP64 and FP32 (p x N rows per set, packed). A
+// double, and stores it in FP64, FP32 and as a float pair (hi + lo, for the
+// double-float judge; p x N rows per set, packed). A
 // passive-set solve on the device is then one small matrix-vector product read
 // from an L1/L2-resident table;
 // its error is ~cond(G_S) * eps (the QR-level bound), not cond(G_S)^2 * eps
@@ -112,10 +113,12 @@ int build_mixed_tables(const DevConditions& c, HostTables* t) {
     for (int j = 0; j <= i; ++j, ++w) {
       t->W64[w] = double(W[i][j]);
       t->W32[w] = float(W[i][j]);
+      t->W32lo[w] = float(W[i][j] - ld(t->W32[w]));
     }
   for (int e = 0; e < N * K; ++e) {
     t->G64[e] = double(G[e]);
     t->G32[e] = float(G[e]);
+    t->G32lo[e] = float(G[e] - ld(t->G32[e]));
     t->P32[e] = float(c.P[e]);
     t->P32lo[e] = float(c.P[e] - double(t->P32[e]));
   }
@@ -148,6 +151,7 @@ int build_mixed_tables(const DevConditions& c, HostTables* t) {
   t->offset[nmask] = total;  // followed by one zero row (the branch-free solves read it)
   t->pinv64.assign(total + N, 0.0);
   t->pinv32.assign(total + N, 0.0f);
+  t->pinv32lo.assign(total + N, 0.0f);
   std::vector<ld> A(N * KMAX), pinv(KMAX * N);
   for (int m = 1; m < nmask; ++m) {
     int p = 0;
@@ -160,6 +164,7 @@ int build_mixed_tables(const DevConditions& c, HostTables* t) {
     for (int e = 0; e < p * N; ++e) {
       t->pinv64[t->offset[m] + e] = double(pinv[e]);
       t->pinv32[t->offset[m] + e] = float(pinv[e]);
+      t->pinv32lo[t->offset[m] + e] = float(pinv[e] - ld(t->pinv32[t->offset[m] + e]));
     }
   }
   return MF_OK;

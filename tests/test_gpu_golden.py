@@ -46,10 +46,12 @@ def test_fp64_kernel_reproduces_fixture(mf, cuda, name, mode):
     eng.close()
 
 
+@pytest.mark.parametrize("prec", ["mixed", "fp32"])
 @pytest.mark.parametrize("name", ["ecal_c0", "ecal_logamp", "hcal", "edge"])
-def test_mixed_form_within_bounds_of_kkt_fixture(mf, cuda, name):
+def test_mixed_form_within_bounds_of_kkt_fixture(mf, cuda, name, prec):
     d, eng, db = setup(mf, cuda, name)
-    eng.fit_device(db.batch, mf.default_options(precision=mf.PREC_MIXED, max_iter_nnls=1000))
+    precision = {"mixed": mf.PREC_MIXED, "fp32": mf.PREC_FP32}[prec]
+    eng.fit_device(db.batch, mf.default_options(precision=precision, max_iter_nnls=1000))
     o = db.outputs_host()
     K = d["P"].shape[1]
     r = d["kkt_amplitudes"]

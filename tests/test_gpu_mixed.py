@@ -1,6 +1,7 @@
-"""GPU mixed-precision form (FP32 active-set search with table solves, FP64
-judge, FP64 chi2) against the FP64 oracle run to KKT convergence (support
-start, max_iter 1000), on the same seeded inputs.
+"""GPU mixed-precision forms against the FP64 oracle run to KKT convergence
+(support start, max_iter 1000), on the same seeded inputs: MF_PREC_MIXED
+(FP32 search and screen, FP64 judge: refinement solve, residual, chi2) and
+MF_PREC_FP32 (the same judge in double-float FP32 arithmetic).
 
 Tolerances (floating point): per channel the normwise relative amplitude
 error max_k |a_k - a_ref_k| / max_k |a_ref_k| must be <= 1e-4 (the headline
@@ -25,10 +26,17 @@ def relerr(a, r):
     return np.abs(a[:, : r.shape[1]] - r).max(axis=1) / scale
 
 
-def run_mixed(mf, cuda, eng, params, n, ctype=False, **opt):
+PRECISIONS = pytest.mark.parametrize("prec", ["mixed", "fp32"])
+
+
+def prec_of(mf, prec):
+    return {"mixed": mf.PREC_MIXED, "fp32": mf.PREC_FP32}[prec]
+
+
+def run_mixed(mf, cuda, eng, params, n, ctype=False, prec="mixed", **opt):
     db = DeviceBatch(mf, cuda, n, ctype=ctype)
     db.generate(mf, params)
-    eng.fit_device(db.batch, mf.default_options(precision=mf.PREC_MIXED, max_iter_nnls=1000, **opt))
+    eng.fit_device(db.batch, mf.default_options(precision=prec_of(mf, prec), max_iter_nnls=1000, **opt))
     return db.inputs_host(), db.outputs_host()
 
 
@@ -45,31 +53,34 @@ def check_against_oracle(mf, oracle, eng, inp, gpu, frac=0.999):
     return err, same
 
 
+@PRECISIONS
 @pytest.mark.parametrize("wl", ["ecal-pu2", "ecal-logamp-pu4"])
-def test_mixed_vs_oracle_ecal(mf, oracle, cuda, wl):
+def test_mixed_vs_oracle_ecal(mf, oracle, cuda, wl, prec):
     params = {"ecal-pu2": mf.synth_params(2, 50_000, pileup_mean=2.0),
               "ecal-logamp-pu4": mf.synth_params(3, 50_000, intime_log=True, lo=0.1, hi=1000.0,
                                                  pileup_mean=4.0)}[wl]
     eng = mf.Engine(0)
     cond, _ = mf.synth_conditions(mf.SYNTH_ECAL)
     eng.set_conditions(0, cond)
-    inp, gpu = run_mixed(mf, cuda, eng, params, 50_000)
+    inp, gpu = run_mixed(mf, cuda, eng, params, 50_000, prec=prec)
     check_against_oracle(mf, oracle, eng, inp, gpu)
     eng.close()
 
 
-def test_mixed_vs_oracle_ecal_hcal(mf, oracle, cuda):
+@PRECISIONS
+def test_mixed_vs_oracle_ecal_hcal(mf, oracle, cuda, prec):
     eng = mf.Engine(0)
     eng.set_conditions(0, mf.synth_conditions(mf.SYNTH_ECAL)[0])
     eng.set_conditions(1, mf.synth_conditions(mf.SYNTH_HCAL)[0])
     params = mf.synth_params(4, 40_000, pileup_mean=-8.0, hcal_fraction=0.4)
-    inp, gpu = run_mixed(mf, cuda, eng, params, 40_000, ctype=True)
+    inp, gpu = run_mixed(mf, cuda, eng, params, 40_000, ctype=True, prec=prec)
     check_against_oracle(mf, oracle, eng, inp, gpu)
     eng.close()
 
 
-def test_mixed_matches_fp64_gpu_path(mf, cuda):
-    """Mixed form vs the plain FP64 kernel run to convergence, full batch on the GPU."""
+@PRECISIONS
+def test_mixed_matches_fp64_gpu_path(mf, cuda, prec):
+    """Mixed forms vs the plain FP64 kernel run to convergence, full batch on the GPU."""
     eng = mf.Engine(0)
     eng.set_conditions(0, mf.synth_conditions(mf.SYNTH_ECAL)[0])
     n = 200_000
@@ -80,7 +91,7 @@ def test_mixed_matches_fp64_gpu_path(mf, cuda):
     db.generate(mf, p)
     eng.fit_device(db.batch, mf.default_options(max_iter_nnls=1000, nnls_start=mf.START_SUPPORT))
     f64 = db.outputs_host()
-    eng.fit_device(db.batch, mf.default_options(precision=mf.PREC_MIXED, max_iter_nnls=1000))
+    eng.fit_device(db.batch, mf.default_options(precision=prec_of(mf, prec), max_iter_nnls=1000))
     mix = db.outputs_host()
     err = relerr(mix["amplitudes"], f64["amplitudes"])
     assert (err <= AMP_TOL).mean() >= 0.999
@@ -126,4 +137,26 @@ def test_profile_counts_and_times_every_launch(mf, cuda):
     eng.fit_device(db.batch, mf.default_options())
     with pytest.raises(mf.MultifitError):
         eng.profile_read()
+    eng.close()
+
+
+def test_fp32_judge_accuracy_and_agreement_with_fp64_judge(mf, cuda):
+    """The double-float judge against the FP64 judge on the same search and
+    screen: amplitudes within 1e-9 normwise relative (~cond(G_S) 2^-48), chi2
+    within 1e-9 relative, the same active sets on >= 99.99 % of channels."""
+    eng = mf.Engine(0)
+    eng.set_conditions(0, mf.synth_conditions(mf.SYNTH_ECAL)[0])
+    n = 200_000
+    db = DeviceBatch(mf, cuda, n)
+    db.generate(mf, mf.synth_params(3, n, intime_log=True, lo=0.1, hi=1000.0, pileup_mean=4.0))
+    eng.fit_device(db.batch, mf.default_options(precision=mf.PREC_MIXED, max_iter_nnls=1000))
+    f64 = db.outputs_host()
+    eng.fit_device(db.batch, mf.default_options(precision=mf.PREC_FP32, max_iter_nnls=1000))
+    df = db.outputs_host()
+    same = df["active_mask"] == f64["active_mask"]
+    assert same.mean() >= 0.9999
+    err = relerr(df["amplitudes"], f64["amplitudes"])[same]
+    assert np.percentile(err, 99.9) <= 1e-9 and err.max() <= 1e-6, (np.percentile(err, 99.9), err.max())
+    c = f64["chi2"][same]
+    assert (np.abs(df["chi2"][same] - c) <= 1e-9 * np.maximum(c, 1.0)).mean() >= 0.999
     eng.close()

@@ -76,7 +76,7 @@ def test_training_reduces_loss_and_warm_fit_parity(mf, oracle, cuda, mlp_engine)
     m = 20_000
     ev = DeviceBatch(mf, cuda, m)
     ev.generate(mf, mf.synth_params(6, m, intime_log=True, lo=0.1, hi=1000.0, pileup_mean=4.0))
-    eng.fit_device(ev.batch, mf.default_options(precision=mf.PREC_MIXED, warm_start=mf.WARM_MLP, max_iter_nnls=1000))
+    eng.fit_device(ev.batch, mf.default_options(precision=mf.PREC_FP32, warm_start=mf.WARM_MLP, max_iter_nnls=1000))
     warm = ev.outputs_host()
     eng.fit_device(ev.batch, mf.default_options(precision=mf.PREC_MIXED, max_iter_nnls=1000))
     cold = ev.outputs_host()

@@ -31,7 +31,8 @@ def mixed_batch(mf, cuda, n, seed):
 
 
 def opts(mf, **kw):
-    return mf.default_options(precision=mf.PREC_MIXED, max_iter_nnls=1000, **kw)
+    kw.setdefault("precision", mf.PREC_MIXED)
+    return mf.default_options(max_iter_nnls=1000, **kw)
 
 
 def assert_identical(a, b):
@@ -39,13 +40,16 @@ def assert_identical(a, b):
         np.testing.assert_array_equal(a[k], b[k], err_msg=k)
 
 
-def test_persistent_one_lane_is_bitwise_grid(mf, cuda):
+@pytest.mark.parametrize("prec", ["mixed", "fp32"])
+def test_persistent_one_lane_is_bitwise_grid(mf, cuda, prec):
     eng = ecal_hcal(mf)
     db = mixed_batch(mf, cuda, 300_001, seed=51)  # odd size: partial last warp
-    eng.fit_device(db.batch, opts(mf))
+    p = {"mixed": mf.PREC_MIXED, "fp32": mf.PREC_FP32}[prec]
+    eng.fit_device(db.batch, opts(mf, precision=p))
     grid = db.outputs_host()
     for block in (64, 256, 512):
-        eng.fit_device(db.batch, opts(mf, schedule=mf.SCHED_PERSISTENT, block_size=block, channels_per_warp=32))
+        eng.fit_device(db.batch, opts(mf, precision=p, schedule=mf.SCHED_PERSISTENT, block_size=block,
+                                      channels_per_warp=32))
         assert_identical(db.outputs_host(), grid)
     assert (grid["status"] == 0).all()
     eng.close()
