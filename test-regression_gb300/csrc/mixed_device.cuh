@@ -708,10 +708,25 @@ __device__ __forceinline__ void judge_df_body(const MixedArgs& a, const DevMixed
       xl[k] = lo;
     }
   }
+  // Round-off bounds of the double-float solve (table and y exact to ~2^-48,
+  // each double-float multiply-add ~2^-48 relative, N <= 10 terms per sum):
+  // |x - x_S| <= N 2^-48 ||G_S^+|| ||y|| < 2^-44.6 ||G_S^+|| ||y|| and the
+  // residual error |G_S (x - x_S)| < 2^-44.6 cond(G_S) ||y||, with the
+  // set-independent bounds ||G_S^+|| <= ||G^+||_F and cond(G_S) <= ||G||_F
+  // ||G^+||_F (singular-value interlacing). Where the true residual is tiny
+  // (near-exact fits, e.g. ten active pulses on ten samples) these errors can
+  // flip the sign of a gradient or an amplitude, so decisions inside the
+  // bounds (2^-45 here) go to the FP64 repair.
+  float ynorm2 = 0.f;
+#pragma unroll
+  for (int i = 0; i < N; ++i) ynorm2 = fmaf(yh[i], yh[i], ynorm2);
+  const float ynorm = sqrtf(ynorm2);
+  const float xbound = 0x1p-45f * T.pinv_norm * ynorm;
+  const float rbound = 0x1p-45f * T.kappa * ynorm;
   bool ok = true;
 #pragma unroll
   for (int k = 0; k < K; ++k)
-    if ((m & (1u << k)) && !(xh[k] > 0.f || (xh[k] == 0.f && xl[k] > 0.f))) ok = false;
+    if ((m & (1u << k)) && !(xh[k] > xbound)) ok = false;
   // r = y - G x
   float rh[N], rl[N], rf[N];
 #pragma unroll
@@ -737,7 +752,7 @@ __device__ __forceinline__ void judge_df_body(const MixedArgs& a, const DevMixed
           w = fmaf(T.G32[k * N + i], rf[i], w);
           mag = fmaf(fabsf(T.G32[k * N + i]), fabsf(rf[i]), mag);
         }
-      if (!(m & (1u << k)) && !(fmaf(0x1p-19f, mag, w) < tol)) ok = false;
+      if (!(m & (1u << k)) && !(fmaf(0x1p-19f, mag, fmaf(T.gnorm32[k], rbound, w)) < tol)) ok = false;
     }
   }
   if (!ok) {
