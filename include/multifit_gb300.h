@@ -175,8 +175,8 @@ int mf_fit(mf_context* ctx, const mf_batch* batch, const mf_options* opt, void* 
  * FP64 operations (the bound of that kernel) for the mixed precision. */
 int mf_fit_count_flops(mf_context* ctx, const mf_batch* batch, const mf_options* opt, double* flops, void* stream);
 
-/* Same fit as mf_fit with the mixed precision (cold start, grid schedule, no
- * errors), for callers that may not allocate device memory per call: a module
+/* Same fit as mf_fit with the mixed or FP32 precision (cold start, grid
+ * schedule, no errors), for callers that may not allocate device memory per call: a module
  * of a multi-threaded event-processing framework whose caching allocator owns
  * the device memory, where cudaMalloc/cudaFree would synchronise the device
  * under every other event in flight. The search-to-judge hand-off lives in a
@@ -202,8 +202,8 @@ typedef struct mf_tune_point {
   double ms;                 /* best of 3 timed fits of the batch (CUDA events), after one warm-up */
 } mf_tune_point;
 #define MF_TUNE_POINTS 20
-/* Sweeps block_size x channels_per_warp for opt (precision MF_PREC_MIXED, any
- * warm start) on the given device batch (its outputs are overwritten), keeps
+/* Sweeps block_size x channels_per_warp for opt (precision MF_PREC_MIXED or
+ * MF_PREC_FP32, any warm start) on the given device batch (its outputs are overwritten), keeps
  * the fastest in the context (used when a persistent-schedule fit leaves
  * block_size / channels_per_warp at 0) and writes up to max_points points.
  * Synchronous. The reference has no tuner (its launch shape is fixed:

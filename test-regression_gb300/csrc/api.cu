@@ -557,7 +557,7 @@ int mf_autotune(mf_context* c, const mf_batch* b, const mf_options* o, mf_tune_p
   FitArgs a;
   int rc = fill_args(c, b, o, &a);
   if (rc) return rc;
-  if (o->precision != MF_PREC_MIXED) return MF_EUNSUPPORTED;
+  if (o->precision != MF_PREC_MIXED && o->precision != MF_PREC_FP32) return MF_EUNSUPPORTED;
   if (b->n == 0 || max_points < 0 || (max_points > 0 && !points)) return MF_EINVAL;
   static const int blocks[] = {64, 128, 256, 512};
   static const int cpws[] = {32, 8, 4, 2, 1};
