@@ -493,11 +493,15 @@ def run_ours(args, world, rank, local):
     for _ in range(args.warmup):
         e2e_step()
     barrier(world)
-    t0 = time.perf_counter()
+    e2e_times = []
     for _ in range(args.steps):
+        t0 = time.perf_counter()
         e2e_step()
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    e2e_s = max_over_ranks(e2e_s, world, device=dev)
+        e2e_times.append(time.perf_counter() - t0)
+    # the median step: the host side of these machines is shared, and a step
+    # that waited on someone else's host-memory traffic says nothing of the engine
+    e2e_sorted = sorted(e2e_times)
+    e2e_s = max_over_ranks(e2e_sorted[len(e2e_sorted) // 2], world, device=dev)
     h2d = n * (10 * 8 + 8 + (1 if mixed else 0))
     d2h = n * (10 * 8 + 8 + 8 + 2 + 1)
 
@@ -548,7 +552,10 @@ def run_ours(args, world, rank, local):
                 "timed_region_launches": "direct (per-kernel CUDA events on)" if graph_ms else "direct",
             },
             "e2e": {"value": n * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "entry": "mf_fit_host (pinned host buffers)"},
+                    "d2h_bytes_per_step": d2h, "entry": "mf_fit_host (pinned host buffers, pipelined copies)",
+                    "statistic": "median step wall time",
+                    "step_ms": {"median": e2e_s * 1e3, "min": e2e_sorted[0] * 1e3, "max": e2e_sorted[-1] * 1e3,
+                                "mean": sum(e2e_times) / len(e2e_times) * 1e3}},
             "roofline": roof,
             "kernels": kernel_table,
             "roofline_hbm": {"bound": "hbm", "achieved": hbm_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
