@@ -435,8 +435,6 @@ void fill_dev_mixed(const mf_context* c, int t, DevMixed* m) {
   m->pinv64 = c->d_pinv64[t];
   m->pinv32 = c->d_pinv32[t];
   m->pinv32lo = c->d_pinv32lo[t];
-  m->pinv_norm = float(h.pinv_norm);
-  m->kappa = float(h.kappa);
 }
 
 int grow_staging(mf_context* c, int64_t n, int ss, int as) {

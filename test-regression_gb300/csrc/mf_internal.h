@@ -104,8 +104,6 @@ struct HostTables {
   std::vector<double> pinv64;
   std::vector<float> pinv32;
   std::vector<float> pinv32lo;        // pinv64 = pinv32 + pinv32lo to ~2^-48
-  double pinv_norm = 0;               // ||G^+||_F of the full set: bounds ||G_S^+||_2 of every set S
-  double kappa = 0;                   // ||G||_F ||G^+||_F: bounds cond_2(G_S) of every set S
 };
 int build_mixed_tables(const DevConditions& c, HostTables* t);
 
@@ -129,7 +127,6 @@ struct DevMixed {
   const double* pinv64;
   const float* pinv32;
   const float* pinv32lo;
-  float pinv_norm, kappa;  // HostTables::pinv_norm, kappa
 };
 
 struct MixedArgs {

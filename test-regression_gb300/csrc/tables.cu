@@ -161,13 +161,6 @@ int build_mixed_tables(const DevConditions& c, HostTables* t) {
         ++p;
       }
     if (!pinv_qr(A.data(), N, p, pinv.data())) return MF_EINVAL;  // a zero pulse column
-    if (m == nmask - 1) {  // the full set: norms that bound every subset (singular-value interlacing)
-      ld pn = 0, gn = 0;
-      for (int e = 0; e < p * N; ++e) pn += pinv[e] * pinv[e];
-      for (int e = 0; e < N * K; ++e) gn += G[e] * G[e];
-      t->pinv_norm = double(std::sqrt(pn));
-      t->kappa = double(std::sqrt(pn) * std::sqrt(gn));
-    }
     for (int e = 0; e < p * N; ++e) {
       t->pinv64[t->offset[m] + e] = double(pinv[e]);
       t->pinv32[t->offset[m] + e] = float(pinv[e]);
