@@ -586,7 +586,8 @@ def kernel_rooflines(mf, eng, kernels, args, n, ctype, plain_flops, form_fp64_fl
     mlp_infer_kernel: MLP_FLOPS_PER_CHANNEL on the tensor cores (BF16).
     search_kernel: FP32 and latency-bound; its HBM bytes (samples, pederr,
       warm start in; hand-off out) against the copy bandwidth.
-    screen_kernel: FP32 (double-float screen); its HBM bytes likewise."""
+    fix_kernel, judge_fixed_kernel: run on the queued channels only; time and
+      share, no roofline."""
     import numpy as np
 
     counts = {0: n}
@@ -622,9 +623,16 @@ def kernel_rooflines(mf, eng, kernels, args, n, ctype, plain_flops, form_fp64_fl
         elif name == "mlp_infer_kernel":
             work = n * MLP_FLOPS_PER_CHANNEL / per_step
             bound, peak, unit = "tensor", peaks["bf16_tflops"], "TFLOP/s"
-        elif name in ("screen_kernel", "fix_kernel"):  # samples + hand-off in, hand-off out (FP32)
-            work = n * (10 * 8 + 44 + 44) / per_step
+        elif name == "screen_kernel":  # samples + hand-off in, refined hand-off out (FP32 double-float)
+            work = n * (10 * 8 + 44 + 40) / per_step
             bound, peak, unit = "hbm", peaks["hbm_gbs"], "GB/s"
+        elif name in ("fix_kernel", "judge_fixed_kernel"):
+            # second-pass kernels on the queued channels only (their count is not recorded):
+            # time and share without a roofline
+            out[name] = {"bound": None, "achieved": None, "peak": None, "unit": None, "frac": None,
+                         "traffic": None, "launches_per_step": per_step, "ms_per_step": ms,
+                         "share": ms / step_ms, "work_per_launch": None, "peak_source": None}
+            continue
         elif name == "partition_kernel":  # ctype in, channel lists out
             work = n * (1 + 4) / per_step
             bound, peak, unit = "hbm", peaks["hbm_gbs"], "GB/s"

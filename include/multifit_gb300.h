@@ -180,7 +180,7 @@ int mf_fit_count_flops(mf_context* ctx, const mf_batch* batch, const mf_options*
  * of a multi-threaded event-processing framework whose caching allocator owns
  * the device memory, where cudaMalloc/cudaFree would synchronise the device
  * under every other event in flight. The search-to-judge hand-off lives in a
- * static device array (about 6 MB per device) instead of the context's
+ * static device array (about 6.5 MB per device) instead of the context's
  * workspace; the call allocates nothing. No counterpart in the reference
  * (multifit_cpu allocates nothing on the device).
  *  - n > MF_NOALLOC_MAX_CHANNELS: MF_EINVAL, mf_last_error says why.
@@ -223,9 +223,10 @@ enum mf_kernel_kind {
   MF_K_JUDGE = 3,     /* judge_kernel / judge_persist: FP64 solve, residual, KKT test, chi2 */
   MF_K_REPAIR = 4,    /* repair_kernel / repair_persist: FP64 FNNLS of the channels the judge queued */
   MF_K_PARTITION = 5, /* partition_kernel: per-set channel lists of the persistent schedule */
-  MF_K_SCREEN = 6,    /* screen_kernel / screen_persist: FP32 double-float KKT screen of the search's set */
-  MF_K_FIX = 7,       /* fix_kernel / fix_persist: FP32 FNNLS step of the channels the screen queued */
-  MF_K_COUNT = 8
+  MF_K_REJUDGE = 6,   /* judge_fixed_kernel / judge_fixed_persist: the judge of the channels the fix changed */
+  MF_K_FIX = 7,       /* fix_kernel / fix_persist: FP32 FNNLS step of the channels queued for it */
+  MF_K_SCREEN = 8,    /* screen_kernel / screen_persist: FP32 double-float KKT screen (cold starts) */
+  MF_K_COUNT = 9
 };
 /* enable != 0 creates the context's event pool (and clears it); 0 frees it. */
 int mf_profile(mf_context* ctx, int enable);

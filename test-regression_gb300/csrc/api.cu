@@ -79,6 +79,7 @@ struct mf_context {
   uint16_t* ws_count = nullptr;
   float* ws_x = nullptr;
   int* ws_queue = nullptr;
+  int* ws_fixq = nullptr;
   unsigned* ws_qcount = nullptr;
   // persistent schedule: per-set channel lists and counters; tuned launch shape
   int* ws_list = nullptr;
@@ -208,6 +209,7 @@ int dispatch_mixed(mf_context* c, const FitArgs& a, const mf_options* o, cudaStr
   m.ws_count = c->ws_count;
   m.ws_x = c->ws_x;
   m.ws_queue = c->ws_queue;
+  m.ws_fixq = c->ws_fixq;
   m.ws_qcount = c->ws_qcount;
   m.sms = c->sms;
   m.ws_list = c->ws_list;
@@ -396,6 +398,7 @@ int upload_tables(mf_context* c, int t) {
     if (e == cudaSuccess) e = cudaMalloc(&c->ws_count, sizeof(uint16_t) * MIXED_CHUNK);
     if (e == cudaSuccess) e = cudaMalloc(&c->ws_x, sizeof(float) * MIXED_CHUNK * KMAX);
     if (e == cudaSuccess) e = cudaMalloc(&c->ws_queue, sizeof(int) * MIXED_CHUNK);
+    if (e == cudaSuccess) e = cudaMalloc(&c->ws_fixq, sizeof(int) * MIXED_CHUNK);
     if (e == cudaSuccess) e = cudaMalloc(&c->ws_qcount, 2 * sizeof(unsigned));  // repair and fix queues
     if (e == cudaSuccess) e = cudaMalloc(&c->ws_list, sizeof(int) * MIXED_CHUNK * MF_MAX_CTYPES);
     if (e == cudaSuccess) e = cudaMalloc(&c->ws_sched, sizeof(unsigned) * SCHED_WORDS);
@@ -533,6 +536,7 @@ void mf_destroy(mf_context* c) {
   cudaFree(c->ws_count);
   cudaFree(c->ws_x);
   cudaFree(c->ws_queue);
+  cudaFree(c->ws_fixq);
   cudaFree(c->ws_qcount);
   cudaFree(c->ws_list);
   cudaFree(c->ws_sched);
@@ -908,10 +912,10 @@ int mf_build_pulse_matrix(const double* fullpulse, const int8_t* bxs, int N, int
 // MLP warm start), no MINOS errors. The scratch is one array per device, so
 // calls whose work overlaps on one device (two streams, two host threads, two
 // contexts) race on it: serialise them, e.g. one stream per device.
-// What must start at zero: only the two queue counters (screen -> fix,
+// What must start at zero: only the two queue counters (judge -> fix,
 // judge -> repair), and the search launch of every call writes them before
-// the screen and judge launches read them; the other scratch words are
-// written before they are read within a call.
+// the judge launches read them; the other scratch words are written before
+// they are read within a call.
 // ---------------------------------------------------------------------------
 
 namespace {
@@ -921,10 +925,11 @@ constexpr size_t kAlignUp(size_t b) { return (b + 255) & ~size_t(255); }
 // byte offsets of the hand-off arrays inside the scratch (each 256-byte aligned)
 constexpr size_t kOffX = 0;                                                     // float [max][KMAX]
 constexpr size_t kOffQueue = kOffX + kAlignUp(sizeof(float) * kNoallocMax * KMAX);  // int [max]
-constexpr size_t kOffMask = kOffQueue + kAlignUp(sizeof(int) * kNoallocMax);       // uint16 [max]
+constexpr size_t kOffFixq = kOffQueue + kAlignUp(sizeof(int) * kNoallocMax);       // int [max]
+constexpr size_t kOffMask = kOffFixq + kAlignUp(sizeof(int) * kNoallocMax);        // uint16 [max]
 constexpr size_t kOffCount = kOffMask + kAlignUp(sizeof(uint16_t) * kNoallocMax);  // uint16 [max]
 constexpr size_t kOffQcount = kOffCount + kAlignUp(sizeof(uint16_t) * kNoallocMax);  // unsigned [2]
-constexpr size_t kNoallocBytes = kOffQcount + 256;  // 6,291,712 bytes for 131,072 channels
+constexpr size_t kNoallocBytes = kOffQcount + 256;  // 6,816,000 bytes for 131,072 channels
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
 
@@ -1010,6 +1015,7 @@ extern "C" int mf_fit_noalloc(mf_context* c, const mf_batch* b, const mf_options
   m.iters = a.iters;
   m.ws_x = reinterpret_cast<float*>(scratch + kOffX);
   m.ws_queue = reinterpret_cast<int*>(scratch + kOffQueue);
+  m.ws_fixq = reinterpret_cast<int*>(scratch + kOffFixq);
   m.ws_mask = reinterpret_cast<uint16_t*>(scratch + kOffMask);
   m.ws_count = reinterpret_cast<uint16_t*>(scratch + kOffCount);
   m.ws_qcount = reinterpret_cast<unsigned*>(scratch + kOffQcount);

@@ -12,19 +12,18 @@
 //     gradient w = G^T y - H x, solve the passive set, step back and drop
 //     columns that go non-positive -- from an empty set or the predicted one;
 //     writes the passive mask and the FP32 amplitudes of each channel.
-//   screen_kernel  (FP32, branch-free): the accurate KKT screen of the
-//     search's set in double-float arithmetic; queues the channels with
-//     columns the FP32 search missed for
-//   fix_kernel     (FP32, compacted): their FNNLS step and one more screen,
-//     so that few channels need the FP64 repair.
 //   judge_kernel   (FP64 -- or, for MF_PREC_FP32, the same steps in double-float
 //     FP32 arithmetic; lean, branch-free: every lane the same FP64
 //     instructions): y in FP64, the FP64 solve on the FP32 passive set, the
 //     FP64 residual, chi2 = ||y - G x||^2 / pederr^2, and the KKT test
 //     max w < eps * pederr^2 (the reference's absolute eps on the
 //     pederr-scaled gradient, PulseChiSqSNNLS.cpp:242) screened in FP32 with
-//     a rounding bound. A channel the screen cannot pass (or whose FP64
-//     amplitudes are not positive) is queued for
+//     a rounding bound. A channel whose amplitudes are positive but whose
+//     columns provably violate the test is queued for
+//   fix_kernel     (FP32, compacted): the FNNLS step with those columns and a
+//     double-float screen of the new set, then
+//   judge_fixed_kernel: the judge again, on the fixed channels only. Every
+//     other rejected channel is queued for
 //   repair_kernel  (FP64): the FNNLS loop in FP64 to the FP64 KKT point, so
 //     the result is the FP64 KKT point whatever the FP32 search found.
 //
@@ -63,6 +62,26 @@ __global__ void __launch_bounds__(128) search_kernel(const MixedArgs a, int set)
 }
 
 template <int N, int K>
+__global__ void __launch_bounds__(128) fix_kernel(const MixedArgs a, int set) {
+  const DevMixed& T = a.tab[set];
+  const unsigned cnt = a.ws_qcount[1];
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x)
+    fix_body<N, K>(a, T, unsigned(a.ws_fixq[i]));
+}
+
+// The second judge pass: the channels the fix changed (failures go to repair).
+template <int N, int K, bool DF>
+__global__ void __launch_bounds__(128, DF ? 4 : 6) judge_fixed_kernel(const MixedArgs a, int set) {
+  const DevMixed& T = a.tab[set];
+  const unsigned cnt = a.ws_qcount[1];
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+    const int64_t ch = int64_t(unsigned(a.ws_fixq[i]) & 0x1fffffu);
+    if constexpr (DF) judge_df_body<N, K>(a, T, ch, a.ws_qcount, nullptr);
+    else judge_body<N, K>(a, T, ch, a.ws_qcount, nullptr);
+  }
+}
+
+template <int N, int K>
 __global__ void __launch_bounds__(128) screen_kernel(const MixedArgs a, int set) {
   const int64_t ch = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (ch >= a.n) return;
@@ -71,16 +90,8 @@ __global__ void __launch_bounds__(128) screen_kernel(const MixedArgs a, int set)
   screen_body<N, K>(a, a.tab[set], ch, a.ws_qcount + 1);
 }
 
-template <int N, int K>
-__global__ void __launch_bounds__(128) fix_kernel(const MixedArgs a, int set) {
-  const DevMixed& T = a.tab[set];
-  const unsigned cnt = a.ws_qcount[1];
-  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x)
-    fix_body<N, K>(a, T, unsigned(a.ws_queue[i]));
-}
-
 template <int N, int K, bool DF>
-__global__ void __launch_bounds__(128, DF ? 4 : 6) judge_kernel(const MixedArgs a, int set, int flag_bad) {
+__global__ void __launch_bounds__(128, DF ? 4 : 6) judge_kernel(const MixedArgs a, int set, int flag_bad, int fixq) {
   const int64_t ch = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (ch >= a.n) return;
   const int t = a.ctype ? int(a.ctype[ch]) : 0;
@@ -92,8 +103,9 @@ __global__ void __launch_bounds__(128, DF ? 4 : 6) judge_kernel(const MixedArgs 
     return;
   }
   if (t != set) return;
-  if constexpr (DF) judge_df_body<N, K>(a, a.tab[set], ch, a.ws_qcount);
-  else judge_body<N, K>(a, a.tab[set], ch, a.ws_qcount);
+  unsigned* fix_count = fixq ? a.ws_qcount + 1 : nullptr;
+  if constexpr (DF) judge_df_body<N, K>(a, a.tab[set], ch, a.ws_qcount, fix_count);
+  else judge_body<N, K>(a, a.tab[set], ch, a.ws_qcount, fix_count);
 }
 
 // Channels the judge queued, in full warps: an FP64 warp instruction costs the
@@ -107,20 +119,56 @@ __global__ void __launch_bounds__(128) repair_kernel(const MixedArgs a, int set)
     judge_repair<N, K>(a, T, int64_t(a.ws_queue[i]));
 }
 
-}  // namespace
-
-// One search, screen, fix, judge and repair launch per condition set (lanes of other sets return at
-// once); out-of-range set indices are flagged by the first judge launch.
-cudaError_t launch_fit_mixed(const MixedArgs& a, int block, cudaStream_t s, LaunchTimer* tm) {
+// The kernels of one condition set. Cold starts: search, screen (queues the
+// channels with provably missing columns), fix, judge, repair. Warm starts
+// (few channels need a column): search, judge (queues them itself), fix,
+// second judge on the fixed channels, repair.
+template <int N, int K>
+void launch_set(const MixedArgs& a, int t, bool warm, int flag_bad, unsigned grid, unsigned jgrid, unsigned rgrid,
+                int block, cudaStream_t s, LaunchTimer* tm) {
   auto mark = [&](int k) {
     if (tm) tm->mark(k, s);
   };
+  mark(MF_K_SEARCH);
+  if constexpr (N == 10 && K == 10) {
+    if (warm) search_kernel<N, K, true><<<grid, block, 0, s>>>(a, t);
+    else search_kernel<N, K, false><<<grid, block, 0, s>>>(a, t);
+  } else {
+    search_kernel<N, K, false><<<grid, block, 0, s>>>(a, t);
+  }
+  if (!warm) {
+    mark(MF_K_SCREEN);
+    screen_kernel<N, K><<<jgrid, 128, 0, s>>>(a, t);
+    mark(MF_K_FIX);
+    fix_kernel<N, K><<<jgrid, 128, 0, s>>>(a, t);
+  }
+  mark(MF_K_JUDGE);
+  if (a.judge_df) judge_kernel<N, K, true><<<jgrid, 128, 0, s>>>(a, t, flag_bad, warm ? 1 : 0);
+  else judge_kernel<N, K, false><<<jgrid, 128, 0, s>>>(a, t, flag_bad, warm ? 1 : 0);
+  if (warm) {
+    mark(MF_K_FIX);
+    fix_kernel<N, K><<<jgrid, 128, 0, s>>>(a, t);
+    mark(MF_K_REJUDGE);
+    if (a.judge_df) judge_fixed_kernel<N, K, true><<<jgrid, 128, 0, s>>>(a, t);
+    else judge_fixed_kernel<N, K, false><<<jgrid, 128, 0, s>>>(a, t);
+  }
+  mark(MF_K_REPAIR);
+  repair_kernel<N, K><<<rgrid, 128, 0, s>>>(a, t);
+}
+
+}  // namespace
+
+// The kernels of every condition set in turn (launch_set) (lanes of other sets return at
+// once); out-of-range set indices are flagged by the first judge launch.
+cudaError_t launch_fit_mixed(const MixedArgs& a, int block, cudaStream_t s, LaunchTimer* tm) {
   if (a.n == 0) return cudaSuccess;
   if (block <= 0) block = 128;
   const unsigned grid = unsigned((a.n + block - 1) / block);
   const unsigned jgrid = unsigned((a.n + 127) / 128);
-  // the repair grid covers the queue's worst case (every channel) with at most
-  // eight 128-thread blocks per SM, striding when the queue is longer
+  // the fix and second judge take one thread per queue slot (the queue's
+  // worst case is every channel; threads past its length exit at once): their
+  // work is gathered and latency-bound, so it wants every thread resident at
+  // once. The repair grid is at most eight 128-thread blocks per SM, striding.
   const int64_t rmax = int64_t(a.sms > 0 ? a.sms : 1) * 8;
   const unsigned rgrid = unsigned(jgrid < rmax ? jgrid : rmax);
   int flag_bad = 1;
@@ -128,30 +176,9 @@ cudaError_t launch_fit_mixed(const MixedArgs& a, int block, cudaStream_t s, Laun
     const DevMixed& T = a.tab[t];
     const bool warm = a.warm_mask && t == a.warm_set;
     if (T.N == 10 && T.K == 10) {
-      mark(MF_K_SEARCH);
-      if (warm) search_kernel<10, 10, true><<<grid, block, 0, s>>>(a, t);
-      else search_kernel<10, 10, false><<<grid, block, 0, s>>>(a, t);
-      mark(MF_K_SCREEN);
-      screen_kernel<10, 10><<<jgrid, 128, 0, s>>>(a, t);
-      mark(MF_K_FIX);
-      fix_kernel<10, 10><<<rgrid, 128, 0, s>>>(a, t);
-      mark(MF_K_JUDGE);
-      if (a.judge_df) judge_kernel<10, 10, true><<<jgrid, 128, 0, s>>>(a, t, flag_bad);
-      else judge_kernel<10, 10, false><<<jgrid, 128, 0, s>>>(a, t, flag_bad);
-      mark(MF_K_REPAIR);
-      repair_kernel<10, 10><<<rgrid, 128, 0, s>>>(a, t);
-    } else if (T.N == 8 && T.K == 8) {
-      mark(MF_K_SEARCH);
-      search_kernel<8, 8, false><<<grid, block, 0, s>>>(a, t);
-      mark(MF_K_SCREEN);
-      screen_kernel<8, 8><<<jgrid, 128, 0, s>>>(a, t);
-      mark(MF_K_FIX);
-      fix_kernel<8, 8><<<rgrid, 128, 0, s>>>(a, t);
-      mark(MF_K_JUDGE);
-      if (a.judge_df) judge_kernel<8, 8, true><<<jgrid, 128, 0, s>>>(a, t, flag_bad);
-      else judge_kernel<8, 8, false><<<jgrid, 128, 0, s>>>(a, t, flag_bad);
-      mark(MF_K_REPAIR);
-      repair_kernel<8, 8><<<rgrid, 128, 0, s>>>(a, t);
+      launch_set<10, 10>(a, t, warm, flag_bad, grid, jgrid, rgrid, block, s, tm);
+    } else if (T.N == 8 && T.K == 8 && !warm) {
+      launch_set<8, 8>(a, t, false, flag_bad, grid, jgrid, rgrid, block, s, tm);
     } else {
       return cudaErrorInvalidValue;
     }

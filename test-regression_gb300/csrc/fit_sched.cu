@@ -14,9 +14,12 @@
 //   search_persist    FP32 search over a set's list, L lanes per channel
 //                     (32 / L channels per warp), each warp taking the next
 //                     32 / L channels from an atomic counter when it is done;
-//   screen_persist    FP32 KKT screen (double-float residual) over the list;
-//   fix_persist       FP32 FNNLS step of the channels the screen queued;
-//   judge_persist     FP64 judge over the list, 32 channels per steal;
+//   screen_persist    (cold starts) FP32 double-float KKT screen over the list;
+//   judge_persist     FP64 (or double-float) judge over the list, 32 channels
+//                     per steal;
+//   fix_persist       FP32 FNNLS step of the channels the screen or (warm
+//                     starts) the judge queued for it;
+//   judge_fixed_persist  (warm starts) the judge again on those;
 //   repair_persist    FP64 repair over the judge's queue, 32 per steal.
 //
 // Grids are sized from the occupancy of each kernel (blocks per SM x SMs), so
@@ -36,9 +39,10 @@ constexpr unsigned kFull = 0xffffffffu;
 
 // ws_sched words
 constexpr int SCHED_COUNT = 0;   // [set] channels in the set's list
-constexpr int SCHED_STEAL = 2;   // [set * 5 + kernel] work counters (search, screen, fix, judge, repair)
-constexpr int SCHED_QUEUE = 12;  // [set] channels queued for repair
-constexpr int SCHED_FIXQ = 14;   // [set] channels queued by the screen for the fix
+constexpr int SCHED_STEAL = 2;   // [set * 6 + kernel] work counters (search, second judge, fix, judge, repair,
+                                 // screen)
+constexpr int SCHED_QUEUE = 14;  // [set] channels queued for repair
+constexpr int SCHED_FIXQ = 16;   // [set] channels queued by the screen or the judge for the fix
 
 __global__ void partition_kernel(const MixedArgs a) {
   const int lane = threadIdx.x & 31;
@@ -184,7 +188,7 @@ __global__ void __launch_bounds__(512) search_persist(const MixedArgs a, int set
   const int lane = threadIdx.x & 31, sub = lane % L;
   const unsigned gmask = L == 32 ? kFull : (((1u << L) - 1u) << (lane - sub));
   for (;;) {
-    const unsigned base = steal(a.ws_sched + SCHED_STEAL + set * 5 + 0, G);
+    const unsigned base = steal(a.ws_sched + SCHED_STEAL + set * 6 + 0, G);
     if (base >= total) break;
     const unsigned i = base + unsigned(lane / L);
     if (i < total) {
@@ -202,7 +206,7 @@ __global__ void __launch_bounds__(128) screen_persist(const MixedArgs a, int set
   const int* list = a.ws_list + int64_t(set) * MIXED_CHUNK;
   const int lane = threadIdx.x & 31;
   for (;;) {
-    const unsigned base = steal(a.ws_sched + SCHED_STEAL + set * 5 + 1, 32u);
+    const unsigned base = steal(a.ws_sched + SCHED_STEAL + set * 6 + 5, 32u);
     if (base >= total) break;
     const unsigned i = base + unsigned(lane);
     if (i < total) screen_body<N, K>(a, T, a.list_identity ? int64_t(i) : int64_t(list[i]), a.ws_sched + SCHED_FIXQ + set);
@@ -215,27 +219,46 @@ __global__ void __launch_bounds__(128) fix_persist(const MixedArgs a, int set) {
   const unsigned total = a.ws_sched[SCHED_FIXQ + set];
   const int lane = threadIdx.x & 31;
   for (;;) {
-    const unsigned base = steal(a.ws_sched + SCHED_STEAL + set * 5 + 2, 32u);
+    const unsigned base = steal(a.ws_sched + SCHED_STEAL + set * 6 + 2, 32u);
     if (base >= total) break;
     const unsigned i = base + unsigned(lane);
-    if (i < total) fix_body<N, K>(a, T, unsigned(a.ws_queue[i]));
+    if (i < total) fix_body<N, K>(a, T, unsigned(a.ws_fixq[i]));
+  }
+}
+
+// The second judge pass over the channels the fix changed.
+template <int N, int K, bool DF>
+__global__ void __launch_bounds__(128, DF ? 4 : 6) judge_fixed_persist(const MixedArgs a, int set) {
+  const DevMixed& T = a.tab[set];
+  const unsigned total = a.ws_sched[SCHED_FIXQ + set];
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    const unsigned base = steal(a.ws_sched + SCHED_STEAL + set * 6 + 1, 32u);
+    if (base >= total) break;
+    const unsigned i = base + unsigned(lane);
+    if (i < total) {
+      const int64_t ch = int64_t(unsigned(a.ws_fixq[i]) & 0x1fffffu);
+      if constexpr (DF) judge_df_body<N, K>(a, T, ch, a.ws_sched + SCHED_QUEUE + set, nullptr);
+      else judge_body<N, K>(a, T, ch, a.ws_sched + SCHED_QUEUE + set, nullptr);
+    }
   }
 }
 
 template <int N, int K, bool DF>
-__global__ void __launch_bounds__(128, DF ? 4 : 6) judge_persist(const MixedArgs a, int set) {
+__global__ void __launch_bounds__(128, DF ? 4 : 6) judge_persist(const MixedArgs a, int set, int fixq) {
   const DevMixed& T = a.tab[set];
   const unsigned total = a.list_identity ? unsigned(a.n) : a.ws_sched[SCHED_COUNT + set];
   const int* list = a.ws_list + int64_t(set) * MIXED_CHUNK;
   const int lane = threadIdx.x & 31;
   for (;;) {
-    const unsigned base = steal(a.ws_sched + SCHED_STEAL + set * 5 + 3, 32u);
+    const unsigned base = steal(a.ws_sched + SCHED_STEAL + set * 6 + 3, 32u);
     if (base >= total) break;
     const unsigned i = base + unsigned(lane);
     if (i < total) {
       const int64_t ch = a.list_identity ? int64_t(i) : int64_t(list[i]);
-      if constexpr (DF) judge_df_body<N, K>(a, T, ch, a.ws_sched + SCHED_QUEUE + set);
-      else judge_body<N, K>(a, T, ch, a.ws_sched + SCHED_QUEUE + set);
+      unsigned* fix_count = fixq ? a.ws_sched + SCHED_FIXQ + set : nullptr;
+      if constexpr (DF) judge_df_body<N, K>(a, T, ch, a.ws_sched + SCHED_QUEUE + set, fix_count);
+      else judge_body<N, K>(a, T, ch, a.ws_sched + SCHED_QUEUE + set, fix_count);
     }
   }
 }
@@ -246,7 +269,7 @@ __global__ void __launch_bounds__(128) repair_persist(const MixedArgs a, int set
   const unsigned total = a.ws_sched[SCHED_QUEUE + set];
   const int lane = threadIdx.x & 31;
   for (;;) {
-    const unsigned base = steal(a.ws_sched + SCHED_STEAL + set * 5 + 4, 32u);
+    const unsigned base = steal(a.ws_sched + SCHED_STEAL + set * 6 + 4, 32u);
     if (base >= total) break;
     const unsigned i = base + unsigned(lane);
     if (i < total) judge_repair<N, K>(a, T, int64_t(a.ws_queue[i]));
@@ -301,13 +324,26 @@ cudaError_t launch_set(const MixedArgs& a, int set, int block, int lanes, cudaSt
     default: break;
   }
   if (e != cudaSuccess) return e;
-  if (tm) tm->mark(MF_K_SCREEN, s);
-  screen_persist<N, K><<<wave(screen_persist<N, K>, 128, a), 128, 0, s>>>(a, set);
-  if (tm) tm->mark(MF_K_FIX, s);
-  fix_persist<N, K><<<wave(fix_persist<N, K>, 128, a), 128, 0, s>>>(a, set);
+  // cold starts screen before the judge; warm starts let the judge queue the
+  // few channels that need a column and judge them again after the fix
+  if (!WARM) {
+    if (tm) tm->mark(MF_K_SCREEN, s);
+    screen_persist<N, K><<<wave(screen_persist<N, K>, 128, a), 128, 0, s>>>(a, set);
+    if (tm) tm->mark(MF_K_FIX, s);
+    fix_persist<N, K><<<wave(fix_persist<N, K>, 128, a), 128, 0, s>>>(a, set);
+  }
   if (tm) tm->mark(MF_K_JUDGE, s);
-  if (a.judge_df) judge_persist<N, K, true><<<wave(judge_persist<N, K, true>, 128, a), 128, 0, s>>>(a, set);
-  else judge_persist<N, K, false><<<wave(judge_persist<N, K, false>, 128, a), 128, 0, s>>>(a, set);
+  if (a.judge_df) judge_persist<N, K, true><<<wave(judge_persist<N, K, true>, 128, a), 128, 0, s>>>(a, set, WARM);
+  else judge_persist<N, K, false><<<wave(judge_persist<N, K, false>, 128, a), 128, 0, s>>>(a, set, WARM);
+  if (WARM) {
+    if (tm) tm->mark(MF_K_FIX, s);
+    fix_persist<N, K><<<wave(fix_persist<N, K>, 128, a), 128, 0, s>>>(a, set);
+    if (tm) tm->mark(MF_K_REJUDGE, s);
+    if (a.judge_df)
+      judge_fixed_persist<N, K, true><<<wave(judge_fixed_persist<N, K, true>, 128, a), 128, 0, s>>>(a, set);
+    else
+      judge_fixed_persist<N, K, false><<<wave(judge_fixed_persist<N, K, false>, 128, a), 128, 0, s>>>(a, set);
+  }
   if (tm) tm->mark(MF_K_REPAIR, s);
   repair_persist<N, K><<<wave(repair_persist<N, K>, 128, a), 128, 0, s>>>(a, set);
   return cudaGetLastError();

@@ -156,7 +156,8 @@ struct MixedArgs {
   uint16_t* ws_mask;
   uint16_t* ws_count;
   float* ws_x;
-  int* ws_queue;           // channels queued by the screen (for the fix), then by the judge (for the repair)
+  int* ws_queue;           // channels the judge queues for the FP64 repair
+  int* ws_fixq;            // channels the first judge pass queues for the FP32 fix (ch | add << 21)
   unsigned* ws_qcount;     // [0] repair queue, [1] fix queue sizes (zeroed by the search launch)
   int sms;
   // persistent schedule (fit_sched.cu): per-set channel lists [MF_MAX_CTYPES][MIXED_CHUNK]
@@ -167,7 +168,7 @@ struct MixedArgs {
   int list_identity;       // one condition set, no ctype: the list is 0..n-1 (no partition pass)
   int judge_df;            // MF_PREC_FP32: the judge in double-float FP32 arithmetic instead of FP64
 };
-constexpr int SCHED_WORDS = 16;
+constexpr int SCHED_WORDS = 32;
 // Channels per chunk of a mixed fit (the size of the hand-off workspace).
 constexpr int64_t MIXED_CHUNK = int64_t(1) << 21;
 cudaError_t launch_fit_mixed(const MixedArgs& a, int block, cudaStream_t s, LaunchTimer* tm = nullptr);

@@ -82,6 +82,16 @@ __device__ __forceinline__ void solve64_dense(const DevMixed& T, unsigned m, con
   }
 }
 
+// Appends value to a queue (one atomic per warp for the lanes appending together).
+__device__ __forceinline__ void enqueue(unsigned* count, int* queue, int value) {
+  const unsigned act = __activemask();
+  const int lane = threadIdx.x & 31, leader = __ffs(act) - 1;
+  unsigned base = 0;
+  if (lane == leader) base = atomicAdd(count, unsigned(__popc(act)));
+  base = __shfl_sync(act, base, leader);
+  queue[base + __popc(act & ((1u << lane) - 1u))] = value;
+}
+
 // x > 0 for a finite double, decided on its bit pattern (integer ops, which
 // keeps the compare off the FP64 pipe)
 __device__ __forceinline__ bool pos64(double v) {
@@ -390,10 +400,10 @@ __device__ __forceinline__ void residual_gradient(const DevMixed& T, const doubl
 // only if w_k plus that bound stays below tol, so every column the FP64 test
 // w_k >= tol could flag is sent to the FP64 repair, and only columns within
 // that bound of tol are sent there needlessly. Returns true when no column
-// needs the FP64 test.
+// needs the FP64 test; add collects the columns that provably violate it.
 template <int N, int K>
 __device__ __forceinline__ bool residual64_screen32(const DevMixed& T, const double* y, const double* x, unsigned m,
-                                                    double* r, float tol) {
+                                                    double* r, float tol, unsigned& add) {
 #pragma unroll
   for (int i = 0; i < N; ++i) r[i] = y[i];
 #pragma unroll
@@ -415,6 +425,7 @@ __device__ __forceinline__ bool residual64_screen32(const DevMixed& T, const dou
         mag = fmaf(fabsf(T.G32[k * N + i]), fabsf(rf[i]), mag);
       }
     if (!(m & (1u << k)) && !(fmaf(0x1p-19f, mag, w) < tol)) ok = false;
+    if (!(m & (1u << k)) && fmaf(-0x1p-19f, mag, w) > tol) add |= 1u << k;  // provably violating
   }
   return ok;
 }
@@ -532,9 +543,10 @@ __device__ __forceinline__ void judge_repair(const MixedArgs& a, const DevMixed&
   write_outputs<N, K>(a, T, ch, x, r, sig, bad, converged, adds, solves, f64);
 }
 
-// The KKT screen of channel ch (one lane, FP32, branch-free): refines the
-// search's amplitudes on its set and, when columns must be added, queues the
-// channel for fix_body (entry = ch | add mask << 21, one atomic per warp).
+// The KKT screen of channel ch (one lane, FP32, branch-free), run on cold
+// starts before the judge: refines the search's amplitudes on its set and,
+// when columns provably violate the KKT condition, queues the channel for
+// fix_body (ws_fixq, entry ch | add mask << 21).
 template <int N, int K>
 __device__ __forceinline__ void screen_body(const MixedArgs& a, const DevMixed& T, int64_t ch, unsigned* fix_count) {
   const unsigned m = a.ws_mask[ch];
@@ -551,20 +563,15 @@ __device__ __forceinline__ void screen_body(const MixedArgs& a, const DevMixed& 
                                            [&](unsigned mm, const float* rhs, float* out) { solve32<N, K>(T, mm, rhs, out); });
 #pragma unroll
   for (int k = 0; k < K; ++k) wx[k] = x32[k];
-  if (add) {
-    const unsigned act = __activemask();
-    const int lane = threadIdx.x & 31, leader = __ffs(act) - 1;
-    unsigned base = 0;
-    if (lane == leader) base = atomicAdd(fix_count, unsigned(__popc(act)));
-    base = __shfl_sync(act, base, leader);
-    a.ws_queue[base + __popc(act & ((1u << lane) - 1u))] = int(unsigned(ch) | (add << 21));
-  }
+  if (add) enqueue(fix_count, a.ws_fixq, int(unsigned(ch) | (add << 21)));
 }
 
-// A queued channel of the screen (entry = ch | add << 21; ch < MIXED_CHUNK =
-// 2^21): the FNNLS step with the added columns in FP32 (the inner loop drops
-// those that come out non-positive), then one more screen round and, if it
-// finds more, one more step. Writes the hand-off for the judge.
+// A channel queued for fixing by the screen or the judge (entry = ch | add <<
+// 21, add = the columns that provably violate the KKT condition; ch <
+// MIXED_CHUNK = 2^21):
+// the FNNLS step with the added columns in FP32 (the inner loop drops those
+// that come out non-positive), then the double-float screen of the new set
+// and, if it finds more, one more step. Writes the hand-off for the judge.
 template <int N, int K>
 __device__ __forceinline__ void fix_body(const MixedArgs& a, const DevMixed& T, unsigned entry) {
   const int64_t ch = int64_t(entry & 0x1fffffu);
@@ -606,10 +613,13 @@ __device__ __forceinline__ void fix_body(const MixedArgs& a, const DevMixed& T, 
   for (int k = 0; k < K; ++k) wx[k] = x32[k];
 }
 
-// The FP64 judge of channel ch (one lane): writes the outputs, or appends the
-// channel to the repair queue (ws_queue, counted in *qcount).
+// The FP64 judge of channel ch (one lane): writes the outputs; or, when
+// columns provably violate the KKT condition and the amplitudes are positive
+// and fix_count is given, queues the channel for the FP32 fix (ws_fixq,
+// entry ch | add << 21); otherwise queues it for the FP64 repair (ws_queue).
 template <int N, int K>
-__device__ __forceinline__ void judge_body(const MixedArgs& a, const DevMixed& T, int64_t ch, unsigned* qcount) {
+__device__ __forceinline__ void judge_body(const MixedArgs& a, const DevMixed& T, int64_t ch, unsigned* qcount,
+                                           unsigned* fix_count) {
   const unsigned m = a.ws_mask[ch];
   const unsigned cnt = a.ws_count[ch];
   double y[N], sig;
@@ -622,15 +632,12 @@ __device__ __forceinline__ void judge_body(const MixedArgs& a, const DevMixed& T
 #pragma unroll
   for (int k = 0; k < K; ++k)
     if ((m & (1u << k)) && !pos64(x[k])) ok = false;
-  if (ok) ok = residual64_screen32<N, K>(T, y, x, m, r, float(a.eps * sig * sig));
-  if (!ok) {
-    // compaction: append the channel to the repair queue (one atomic per warp)
-    const unsigned act = __activemask();
-    const int lane = threadIdx.x & 31, leader = __ffs(act) - 1;
-    unsigned base = 0;
-    if (lane == leader) base = atomicAdd(qcount, unsigned(__popc(act)));
-    base = __shfl_sync(act, base, leader);
-    a.ws_queue[base + __popc(act & ((1u << lane) - 1u))] = int(ch);
+  unsigned add = 0;
+  const bool pos_ok = ok;
+  if (ok) ok = residual64_screen32<N, K>(T, y, x, m, r, float(a.eps * sig * sig), add);
+  if (!ok) {  // compaction into the fix or the repair queue
+    if (fix_count && pos_ok && add) enqueue(fix_count, a.ws_fixq, int(unsigned(ch) | (add << 21)));
+    else enqueue(qcount, a.ws_queue, int(ch));
     return;
   }
   write_outputs<N, K>(a, T, ch, x, r, sig, bad, true, int(cnt & 255u), int(cnt >> 8) + 1,
@@ -665,7 +672,8 @@ __device__ __forceinline__ bool finite64(double v) {
 }
 
 template <int N, int K>
-__device__ __forceinline__ void judge_df_body(const MixedArgs& a, const DevMixed& T, int64_t ch, unsigned* qcount) {
+__device__ __forceinline__ void judge_df_body(const MixedArgs& a, const DevMixed& T, int64_t ch, unsigned* qcount,
+                                              unsigned* fix_count) {
   const unsigned m = a.ws_mask[ch];
   const unsigned cnt = a.ws_count[ch];
   const double* in = a.samples + ch * a.sample_stride;
@@ -730,6 +738,8 @@ __device__ __forceinline__ void judge_df_body(const MixedArgs& a, const DevMixed
     xb[k] = 0x1p-44f * dx[k];
     if ((m & (1u << k)) && !(xh[k] > xb[k])) ok = false;
   }
+  const bool pos_ok = ok;
+  unsigned add = 0;
   // r = y - G x
   float rh[N], rl[N], rf[N];
 #pragma unroll
@@ -767,15 +777,12 @@ __device__ __forceinline__ void judge_df_body(const MixedArgs& a, const DevMixed
           werr = fmaf(fabsf(T.G32[k * N + i]), e[i], werr);
         }
       if (!(m & (1u << k)) && !(fmaf(0x1p-19f, mag, w + werr) < tol)) ok = false;
+      if (!(m & (1u << k)) && fmaf(-0x1p-19f, mag, w - werr) > tol) add |= 1u << k;  // provably violating
     }
   }
-  if (!ok) {
-    const unsigned act = __activemask();
-    const int lane = threadIdx.x & 31, leader = __ffs(act) - 1;
-    unsigned base = 0;
-    if (lane == leader) base = atomicAdd(qcount, unsigned(__popc(act)));
-    base = __shfl_sync(act, base, leader);
-    a.ws_queue[base + __popc(act & ((1u << lane) - 1u))] = int(ch);
+  if (!ok) {  // compaction into the fix or the repair queue
+    if (fix_count && pos_ok && add) enqueue(fix_count, a.ws_fixq, int(unsigned(ch) | (add << 21)));
+    else enqueue(qcount, a.ws_queue, int(ch));
     return;
   }
   // chi2 = ||r||^2 / pederr^2, the sum in double-float
