@@ -228,8 +228,8 @@ __global__ void __launch_bounds__(128) fix_persist(const MixedArgs a, int set) {
 
 // The second judge pass over the channels the fix changed.
 template <int N, int K, bool DF>
-__global__ void __launch_bounds__(128, DF ? 4 : 6) judge_fixed_persist(const MixedArgs a, int set) {
-  const DevMixed& T = a.tab[set];
+__global__ void __launch_bounds__(128, DF ? 4 : 6) judge_fixed_persist(const __grid_constant__ MixedArgs a,
+    const __grid_constant__ DevMixed T, int set) {
   const unsigned total = a.ws_sched[SCHED_FIXQ + set];
   const int lane = threadIdx.x & 31;
   for (;;) {
@@ -239,14 +239,14 @@ __global__ void __launch_bounds__(128, DF ? 4 : 6) judge_fixed_persist(const Mix
     if (i < total) {
       const int64_t ch = int64_t(unsigned(a.ws_fixq[i]) & 0x1fffffu);
       if constexpr (DF) judge_df_body<N, K>(a, T, ch, a.ws_sched + SCHED_QUEUE + set, nullptr);
-      else judge_body<N, K>(a, T, ch, a.ws_sched + SCHED_QUEUE + set, nullptr);
+      else judge_body<N, K>(a, a.tab[set], ch, a.ws_sched + SCHED_QUEUE + set, nullptr);
     }
   }
 }
 
 template <int N, int K, bool DF>
-__global__ void __launch_bounds__(128, DF ? 4 : 6) judge_persist(const MixedArgs a, int set, int fixq) {
-  const DevMixed& T = a.tab[set];
+__global__ void __launch_bounds__(128, DF ? 4 : 6) judge_persist(const __grid_constant__ MixedArgs a,
+    const __grid_constant__ DevMixed T, int set, int fixq) {
   const unsigned total = a.list_identity ? unsigned(a.n) : a.ws_sched[SCHED_COUNT + set];
   const int* list = a.ws_list + int64_t(set) * MIXED_CHUNK;
   const int lane = threadIdx.x & 31;
@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(128, DF ? 4 : 6) judge_persist(const MixedArgs
       const int64_t ch = a.list_identity ? int64_t(i) : int64_t(list[i]);
       unsigned* fix_count = fixq ? a.ws_sched + SCHED_FIXQ + set : nullptr;
       if constexpr (DF) judge_df_body<N, K>(a, T, ch, a.ws_sched + SCHED_QUEUE + set, fix_count);
-      else judge_body<N, K>(a, T, ch, a.ws_sched + SCHED_QUEUE + set, fix_count);
+      else judge_body<N, K>(a, a.tab[set], ch, a.ws_sched + SCHED_QUEUE + set, fix_count);
     }
   }
 }
@@ -333,16 +333,16 @@ cudaError_t launch_set(const MixedArgs& a, int set, int block, int lanes, cudaSt
     fix_persist<N, K><<<wave(fix_persist<N, K>, 128, a), 128, 0, s>>>(a, set);
   }
   if (tm) tm->mark(MF_K_JUDGE, s);
-  if (a.judge_df) judge_persist<N, K, true><<<wave(judge_persist<N, K, true>, 128, a), 128, 0, s>>>(a, set, WARM);
-  else judge_persist<N, K, false><<<wave(judge_persist<N, K, false>, 128, a), 128, 0, s>>>(a, set, WARM);
+  if (a.judge_df) judge_persist<N, K, true><<<wave(judge_persist<N, K, true>, 128, a), 128, 0, s>>>(a, a.tab[set], set, WARM);
+  else judge_persist<N, K, false><<<wave(judge_persist<N, K, false>, 128, a), 128, 0, s>>>(a, a.tab[set], set, WARM);
   if (WARM) {
     if (tm) tm->mark(MF_K_FIX, s);
     fix_persist<N, K><<<wave(fix_persist<N, K>, 128, a), 128, 0, s>>>(a, set);
     if (tm) tm->mark(MF_K_REJUDGE, s);
     if (a.judge_df)
-      judge_fixed_persist<N, K, true><<<wave(judge_fixed_persist<N, K, true>, 128, a), 128, 0, s>>>(a, set);
+      judge_fixed_persist<N, K, true><<<wave(judge_fixed_persist<N, K, true>, 128, a), 128, 0, s>>>(a, a.tab[set], set);
     else
-      judge_fixed_persist<N, K, false><<<wave(judge_fixed_persist<N, K, false>, 128, a), 128, 0, s>>>(a, set);
+      judge_fixed_persist<N, K, false><<<wave(judge_fixed_persist<N, K, false>, 128, a), 128, 0, s>>>(a, a.tab[set], set);
   }
   if (tm) tm->mark(MF_K_REPAIR, s);
   repair_persist<N, K><<<wave(repair_persist<N, K>, 128, a), 128, 0, s>>>(a, set);

@@ -31,6 +31,13 @@ typedef __nv_bfloat16 bf16;
 
 constexpr int BM = 64, BN = 64, BK = 32, PAD = 8;
 
+// A column enters the predicted passive set when its logit exceeds -0.5
+// (probability 0.38, not 0.5): a column predicted needlessly costs the warm
+// FP32 search one drop step, a column missed costs a fix and a second judge
+// (measured on 10M ECAL channels: 8.48 ms per fit at -0.5, 8.90 ms at 0,
+// 8.55 ms at -1, 9.34 ms at -2).
+constexpr float kMaskLogit = -0.5f;
+
 // Warp-level 32x32 tile product over one BK slice held in shared memory
 // (row-major [rows][BK+PAD], k contiguous), accumulating into acc[2][4][4].
 __device__ __forceinline__ void warp_tile_mma(const bf16 (*As)[BK + PAD], const bf16 (*Bs)[BK + PAD], int wm, int wn,
@@ -334,7 +341,7 @@ __global__ void __launch_bounds__(128) mlp_infer_kernel(const MlpInferArgs a) {
       float* wa = a.warm_amp + i * a.warm_stride;
 #pragma unroll
       for (int k = 0; k < 10; ++k) {
-        if (S.O[tid][k] > 0.f && scale > 0.f) m |= uint16_t(1u << k);
+        if (S.O[tid][k] > kMaskLogit && scale > 0.f) m |= uint16_t(1u << k);
         wa[k] = softplusf(S.O[tid][10 + k]) * scale * a.inv_gnorm[k];
       }
       a.warm_mask[i] = mine ? m : uint16_t(0);
