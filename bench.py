@@ -583,7 +583,7 @@ def kernel_rooflines(mf, eng, kernels, args, n, ctype, plain_flops, form_fp64_fl
     judge_kernel: N(N+1) + 4NK FP64 flops per channel of its set (whitening,
       dense passive-set solve, residual; FMA = 2).
     repair_kernel: the rest of the form's counted FP64 flops.
-    mlp_infer_kernel: MLP_FLOPS_PER_CHANNEL on the tensor cores (BF16).
+    mlp_infer_tc_kernel: MLP_FLOPS_PER_CHANNEL on the tensor cores (BF16, tcgen05).
     search_kernel: FP32 and latency-bound; its HBM bytes (samples, pederr,
       warm start in; hand-off out) against the copy bandwidth.
     fix_kernel, judge_fixed_kernel: run on the queued channels only; time and
@@ -620,7 +620,7 @@ def kernel_rooflines(mf, eng, kernels, args, n, ctype, plain_flops, form_fp64_fl
             # the FP64 judge's share of the counted FP64 flops belongs to the judge (its repairs redo it)
             rest = form_fp64_flops - (0.0 if df_form else judge)
             work, bound, peak, unit = max(rest, 0.0) / per_step, "fp64", fp64_peak, "TFLOP/s"
-        elif name == "mlp_infer_kernel":
+        elif name == "mlp_infer_tc_kernel":
             work = n * MLP_FLOPS_PER_CHANNEL / per_step
             bound, peak, unit = "tensor", peaks["bf16_tflops"], "TFLOP/s"
         elif name == "screen_kernel":  # samples + hand-off in, refined hand-off out (FP32 double-float)

@@ -218,7 +218,7 @@ int mf_autotune(mf_context* ctx, const mf_batch* batch, const mf_options* opt, m
  * each kernel launch and after its last one (8,192 events per read). */
 enum mf_kernel_kind {
   MF_K_FIT_FP64 = 0,  /* fit_fp64_kernel: the plain FP64 fit */
-  MF_K_MLP_INFER = 1, /* mlp_infer_kernel: warm-start predictions */
+  MF_K_MLP_INFER = 1, /* mlp_infer_tc_kernel: warm-start predictions (tcgen05) */
   MF_K_SEARCH = 2,    /* search_kernel / search_persist: FP32 active-set search */
   MF_K_JUDGE = 3,     /* judge_kernel / judge_persist: FP64 solve, residual, KKT test, chi2 */
   MF_K_REPAIR = 4,    /* repair_kernel / repair_persist: FP64 FNNLS of the channels the judge queued */

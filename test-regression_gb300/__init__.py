@@ -114,7 +114,7 @@ class MfMlpTrainParams(C.Structure):
 # Exported symbols and their signatures: (name, restype, argtypes).
 NOALLOC_MAX_CHANNELS = 131072  # MF_NOALLOC_MAX_CHANNELS
 # mf_kernel_kind: the kernels mf_profile times
-KERNEL_KINDS = ("fit_fp64_kernel", "mlp_infer_kernel", "search_kernel", "judge_kernel", "repair_kernel",
+KERNEL_KINDS = ("fit_fp64_kernel", "mlp_infer_tc_kernel", "search_kernel", "judge_kernel", "repair_kernel",
                 "partition_kernel", "judge_fixed_kernel", "fix_kernel", "screen_kernel")
 
 SIGNATURES = [

@@ -783,6 +783,18 @@ int mf_fit_host(mf_context* c, const mf_batch* hb, const mf_options* o) {
     set_last_error("mf_fit_host", e);
     return MF_ECUDA;
   }
+  if (c->mlp.infer_err) {
+    // a bounded tensor-core wait of the warm-start inference gave up: those
+    // channels were fitted from a cold start (same results), reported once
+    unsigned flags = 0;
+    e = cudaMemcpy(&flags, c->mlp.infer_err, sizeof(flags), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && flags) e = cudaMemset(c->mlp.infer_err, 0, sizeof(flags));
+    if (e != cudaSuccess) {
+      set_last_error("mf_fit_host", e);
+      return MF_ECUDA;
+    }
+    if (flags & MLP_ERR_TIMEOUT) return MF_ETIMEOUT;
+  }
   return MF_OK;
 }
 

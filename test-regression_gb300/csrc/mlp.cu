@@ -4,7 +4,8 @@
 // Network: 16 inputs (10 normalised whitened samples, log SNR, pederr, zero
 // padding) -> 128 -> GELU -> 128 -> GELU -> 32 outputs (10 passive-set logits,
 // 10 amplitude outputs, padding). BF16 weights and activations on the tensor
-// cores (mma.sync m16n8k16, FP32 accumulate); FP32 master weights, Adam.
+// cores, FP32 accumulate; FP32 master weights, Adam. Training runs its GEMMs
+// as mma.sync m16n8k16 tiles; inference runs on tcgen05 (mlp_tc.cu).
 //
 // Kernels:
 //   mlp_features_kernel   channel -> feature row (bf16) + per-channel scale
@@ -12,9 +13,8 @@
 //                         input gradients, split-K weight gradients)
 //   loss_kernel           BCE on the logits + MSE on softplus(amplitude outputs)
 //   gelu_backward_kernel, bias_grad_kernel, adam_kernel, pack_weights_kernel
-//   mlp_infer_kernel      fused features->3 layers->warm-start outputs, the
-//                         weights and the activations of a 64-channel tile in
-//                         shared memory (the path inside a timed fit)
+//   launch_mlp_infer      the inference kernel of mlp_tc.cu (the path inside
+//                         a timed fit)
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -30,13 +30,6 @@ namespace {
 typedef __nv_bfloat16 bf16;
 
 constexpr int BM = 64, BN = 64, BK = 32, PAD = 8;
-
-// A column enters the predicted passive set when its logit exceeds -0.5
-// (probability 0.38, not 0.5): a column predicted needlessly costs the warm
-// FP32 search one drop step, a column missed costs a fix and a second judge
-// (measured on 10M ECAL channels: 8.48 ms per fit at -0.5, 8.90 ms at 0,
-// 8.55 ms at -1, 9.34 ms at -2).
-constexpr float kMaskLogit = -0.5f;
 
 // Warp-level 32x32 tile product over one BK slice held in shared memory
 // (row-major [rows][BK+PAD], k contiguous), accumulating into acc[2][4][4].
@@ -228,132 +221,6 @@ __global__ void pack_weights_kernel(const float* w, bf16* wh, bf16* wt, int out,
 }
 
 // --------------------------------------------------------------------------
-// inference: one block = 128 channels (a warp's 32 rows each), weights in
-// shared memory, hidden activations chained through registers
-// --------------------------------------------------------------------------
-struct InferSmem {
-  bf16 W1[MLP_H][MLP_IN + PAD];
-  bf16 W2[MLP_H][MLP_H + PAD];
-  bf16 W3[MLP_OUT][MLP_H + PAD];
-  float b1[MLP_H], b2[MLP_H], b3[MLP_OUT];
-  bf16 X[128][MLP_IN + PAD];
-  float O[128][MLP_OUT + 1];
-};
-
-// Two adjacent n8 accumulator tiles (columns c0.. and c0+8..) after bias and
-// GELU, packed as the BF16 A fragment of the next layer's k16 slice.
-__device__ __forceinline__ void gelu_pack(const float (&c0)[4], const float (&c1)[4], const float* bias, int col0,
-                                          uint32_t (&h)[4]) {
-  h[0] = pack_bf16(gelu_fast(c0[0] + bias[col0]), gelu_fast(c0[1] + bias[col0 + 1]));
-  h[1] = pack_bf16(gelu_fast(c0[2] + bias[col0]), gelu_fast(c0[3] + bias[col0 + 1]));
-  h[2] = pack_bf16(gelu_fast(c1[0] + bias[col0 + 8]), gelu_fast(c1[1] + bias[col0 + 9]));
-  h[3] = pack_bf16(gelu_fast(c1[2] + bias[col0 + 8]), gelu_fast(c1[3] + bias[col0 + 9]));
-}
-
-// The MLP of the warp's 32 rows of S.X into S.O. The m16n8 accumulators of a
-// layer, two n8 tiles at a time, are the m16n8k16 A fragments of the next
-// layer (rows g / g+8, k pairs 2t and 8+2t), so H1 stays in registers and each
-// 16-column slice of H2 is folded into layer 3 at once.
-__device__ __forceinline__ void warp_mlp(InferSmem& S, int warp) {
-  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-#pragma unroll 1
-  for (int mt = 0; mt < 2; ++mt) {
-    const int r = warp * 32 + mt * 16 + g;
-    uint32_t a0[4];
-    a0[0] = ld32(&S.X[r][2 * t]);
-    a0[1] = ld32(&S.X[r + 8][2 * t]);
-    a0[2] = ld32(&S.X[r][8 + 2 * t]);
-    a0[3] = ld32(&S.X[r + 8][8 + 2 * t]);
-    uint32_t h1[8][4];
-#pragma unroll
-    for (int kt = 0; kt < 8; ++kt) {
-      float c0[4] = {0.f, 0.f, 0.f, 0.f}, c1[4] = {0.f, 0.f, 0.f, 0.f};
-      const uint32_t b0[2] = {ld32(&S.W1[16 * kt + g][2 * t]), ld32(&S.W1[16 * kt + g][8 + 2 * t])};
-      const uint32_t b1[2] = {ld32(&S.W1[16 * kt + 8 + g][2 * t]), ld32(&S.W1[16 * kt + 8 + g][8 + 2 * t])};
-      mma_bf16(c0, a0, b0);
-      mma_bf16(c1, a0, b1);
-      gelu_pack(c0, c1, S.b1, 16 * kt + 2 * t, h1[kt]);
-    }
-    float o[4][4];
-#pragma unroll
-    for (int n3 = 0; n3 < 4; ++n3)
-#pragma unroll
-      for (int h = 0; h < 4; ++h) o[n3][h] = 0.f;
-#pragma unroll 1
-    for (int nt = 0; nt < 8; ++nt) {
-      float c0[4] = {0.f, 0.f, 0.f, 0.f}, c1[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-      for (int kt = 0; kt < 8; ++kt) {
-        const uint32_t b0[2] = {ld32(&S.W2[16 * nt + g][16 * kt + 2 * t]),
-                                ld32(&S.W2[16 * nt + g][16 * kt + 8 + 2 * t])};
-        const uint32_t b1[2] = {ld32(&S.W2[16 * nt + 8 + g][16 * kt + 2 * t]),
-                                ld32(&S.W2[16 * nt + 8 + g][16 * kt + 8 + 2 * t])};
-        mma_bf16(c0, h1[kt], b0);
-        mma_bf16(c1, h1[kt], b1);
-      }
-      uint32_t h2[4];
-      gelu_pack(c0, c1, S.b2, 16 * nt + 2 * t, h2);
-#pragma unroll
-      for (int n3 = 0; n3 < 4; ++n3) {
-        const uint32_t b3[2] = {ld32(&S.W3[8 * n3 + g][16 * nt + 2 * t]),
-                                ld32(&S.W3[8 * n3 + g][16 * nt + 8 + 2 * t])};
-        mma_bf16(o[n3], h2, b3);
-      }
-    }
-#pragma unroll
-    for (int n3 = 0; n3 < 4; ++n3) {
-      const int c = 8 * n3 + 2 * t;
-      S.O[r][c] = o[n3][0] + S.b3[c];
-      S.O[r][c + 1] = o[n3][1] + S.b3[c + 1];
-      S.O[r + 8][c] = o[n3][2] + S.b3[c];
-      S.O[r + 8][c + 1] = o[n3][3] + S.b3[c + 1];
-    }
-  }
-}
-
-__global__ void __launch_bounds__(128) mlp_infer_kernel(const MlpInferArgs a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
-  const int tid = threadIdx.x, warp = tid >> 5;
-  for (int e = tid; e < MLP_H * MLP_IN; e += 128) S.W1[e / MLP_IN][e % MLP_IN] = a.W1[e];
-  for (int e = tid; e < MLP_H * MLP_H; e += 128) S.W2[e / MLP_H][e % MLP_H] = a.W2[e];
-  for (int e = tid; e < MLP_OUT * MLP_H; e += 128) S.W3[e / MLP_H][e % MLP_H] = a.W3[e];
-  for (int e = tid; e < MLP_H; e += 128) {
-    S.b1[e] = a.b1[e];
-    S.b2[e] = a.b2[e];
-  }
-  for (int e = tid; e < MLP_OUT; e += 128) S.b3[e] = a.b3[e];
-  __syncthreads();
-  for (int64_t base = int64_t(blockIdx.x) * 128; base < a.n; base += int64_t(gridDim.x) * 128) {
-    const int64_t i = base + tid;
-    float f[MLP_IN], scale = 0.f;
-#pragma unroll
-    for (int j = 0; j < MLP_IN; ++j) f[j] = 0.f;
-    const bool mine = i < a.n && (a.ctype ? int(a.ctype[i]) : 0) == a.set;
-    if (mine) mlp_features(a.W32, a.samples + i * a.sample_stride, a.pederr[i], f, &scale);
-#pragma unroll
-    for (int j = 0; j < MLP_IN; j += 2) *reinterpret_cast<uint32_t*>(&S.X[tid][j]) = pack_bf16(f[j], f[j + 1]);
-    __syncwarp();
-    warp_mlp(S, warp);
-    __syncwarp();
-    if (i < a.n) {
-      uint16_t m = 0;
-      float* wa = a.warm_amp + i * a.warm_stride;
-#pragma unroll
-      for (int k = 0; k < 10; ++k) {
-        if (S.O[tid][k] > kMaskLogit && scale > 0.f) m |= uint16_t(1u << k);
-        wa[k] = softplusf(S.O[tid][10 + k]) * scale * a.inv_gnorm[k];
-      }
-      a.warm_mask[i] = mine ? m : uint16_t(0);
-      if (a.logits) {
-        for (int k = 0; k < MLP_OUT; ++k) a.logits[i * MLP_OUT + k] = S.O[tid][k];
-      }
-    }
-    __syncwarp();
-  }
-}
-
-// --------------------------------------------------------------------------
 // launchers
 // --------------------------------------------------------------------------
 cudaError_t launch_gemm(int epi, bool akc, bool bkc, const GemmArgs& p, int splits, cudaStream_t s) {
@@ -371,21 +238,22 @@ cudaError_t launch_gemm(int epi, bool akc, bool bkc, const GemmArgs& p, int spli
   return cudaErrorInvalidValue;
 }
 
-size_t infer_smem_bytes() { return sizeof(InferSmem); }
-
+// The tensor-core inference kernel (mlp_tc.cu): one wave of persistent CTAs
+// of 512 threads, two per SM (each holds 256 of the SM's 512 TMEM columns and
+// half of its shared memory for its lifetime).
 cudaError_t launch_mlp_infer(const MlpInferArgs& a, int sms, cudaStream_t s) {
   if (a.n == 0) return cudaSuccess;
   static bool attr_set = false;
-  const size_t smem = sizeof(InferSmem);
+  const size_t smem = infer_tc_smem_bytes();
   if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(mlp_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    cudaError_t e = cudaFuncSetAttribute(mlp_infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
   const int64_t tiles = (a.n + 127) / 128;
-  const int64_t cap = int64_t(sms) * 3;
+  const int64_t cap = 2 * int64_t(sms);
   const int grid = int(tiles < cap ? tiles : cap);
-  mlp_infer_kernel<<<grid, 128, smem, s>>>(a);
+  mlp_infer_tc_kernel<<<grid, 512, smem, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -60,7 +60,11 @@ struct MlpInferArgs {
   float* warm_amp;      // [n][warm_stride]
   int warm_stride;
   float* logits;        // optional [n][MLP_OUT] raw outputs
+  unsigned* err;        // device error word (MLP_ERR_* bits), or null
 };
+
+// Bits of the inference error word.
+constexpr unsigned MLP_ERR_TIMEOUT = 1u;  // a bounded wait on the tensor cores gave up
 
 __global__ void mlp_features_kernel(const MlpFeatArgs a);
 __global__ void mlp_targets_kernel(int64_t n, const double* amp, int amp_stride, const float* scale,
@@ -72,10 +76,10 @@ __global__ void bias_grad_kernel(int B, int C, const __nv_bfloat16* dZ, float* d
 __global__ void adam_kernel(int count, float* w, const float* g, float* m, float* v, float lr, float b1, float b2,
                             float eps, float c1, float c2);
 __global__ void pack_weights_kernel(const float* w, __nv_bfloat16* wh, __nv_bfloat16* wt, int out, int in);
-__global__ void mlp_infer_kernel(const MlpInferArgs a);
+__global__ void mlp_infer_tc_kernel(const MlpInferArgs a);
 
 cudaError_t launch_gemm(int epi, bool akc, bool bkc, const GemmArgs& p, int splits, cudaStream_t s);
 cudaError_t launch_mlp_infer(const MlpInferArgs& a, int sms, cudaStream_t s);
-size_t infer_smem_bytes();
+size_t infer_tc_smem_bytes();
 
 }  // namespace mfgb

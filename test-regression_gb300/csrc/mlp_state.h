@@ -35,6 +35,7 @@ struct MlpState {
   static constexpr int64_t kChunk = int64_t(1) << 21;
   uint16_t* warm_mask = nullptr;
   float* warm_amp = nullptr;
+  unsigned* infer_err = nullptr;  // inference error word (MLP_ERR_* bits)
 };
 
 // Host buffers of a gradient check (one forward/backward on the first batch).

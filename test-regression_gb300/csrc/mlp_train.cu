@@ -31,7 +31,7 @@ cudaError_t alloc(T** p, size_t count) {
 }  // namespace
 
 void mlp_free(MlpState& s) {
-  void* ps[] = {s.params, s.grads, s.m, s.v, s.W1h, s.W2h, s.W3h, s.W2t, s.W3t, s.warm_mask, s.warm_amp};
+  void* ps[] = {s.params, s.grads, s.m, s.v, s.W1h, s.W2h, s.W3h, s.W2t, s.W3t, s.warm_mask, s.warm_amp, s.infer_err};
   for (void* p : ps) cudaFree(p);
   s = MlpState();
 }
@@ -50,6 +50,7 @@ int mlp_init(MlpState& s, int device, int set, uint64_t seed) {
   if (e == cudaSuccess) e = alloc(&s.W3t, MLP_OUT * MLP_H);
   if (e == cudaSuccess) e = alloc(&s.warm_mask, MlpState::kChunk);
   if (e == cudaSuccess) e = alloc(&s.warm_amp, MlpState::kChunk * 10);
+  if (e == cudaSuccess) e = alloc(&s.infer_err, 1);
   if (e != cudaSuccess) {
     set_last_error("mlp_init cudaMalloc", e);
     mlp_free(s);
@@ -67,6 +68,7 @@ int mlp_init(MlpState& s, int device, int set, uint64_t seed) {
   e = cudaMemcpy(s.params, h.data(), sizeof(float) * P_COUNT, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(s.m, 0, sizeof(float) * P_COUNT);
   if (e == cudaSuccess) e = cudaMemset(s.v, 0, sizeof(float) * P_COUNT);
+  if (e == cudaSuccess) e = cudaMemset(s.infer_err, 0, sizeof(unsigned));
   if (e == cudaSuccess) e = pack_all(s, 0);
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   if (e != cudaSuccess) {
@@ -114,6 +116,7 @@ void fill_infer_args(const MlpState& s, const HostTables& tab, int intime_unused
   a->b1 = s.params + P_B1;
   a->b2 = s.params + P_B2;
   a->b3 = s.params + P_B3;
+  a->err = s.infer_err;
 }
 
 // One training run over n channels whose converged amplitudes are given.

@@ -158,8 +158,9 @@ def test_mixed_fp64_flop_counter(mf, cuda):
 
 
 def test_inference_matches_cpu_network(mf, cuda, mlp_engine):
-    """mlp_infer_kernel (BF16 mma.sync, FP32 accumulation, GELU through the
-    hardware tanh.approx.f32) against the FP64 checker network with exact tanh
+    """The inference kernel (tcgen05.mma: BF16 operands from shared memory,
+    FP32 accumulators in tensor memory; GELU through the hardware
+    tanh.approx.f32) against the FP64 checker network with exact tanh
     and the same BF16 rounding points, on the same BF16 features. The hardware
     tanh's relative error (<= 2^-10.987) moves a hidden activation by at most
     2^-12 relative, under half a BF16 ulp (2^-9), so it only flips the rounding
@@ -178,3 +179,9 @@ def test_inference_matches_cpu_network(mf, cuda, mlp_engine):
     rel = np.abs(logits.cpu().numpy() - ref) / np.maximum(1.0, np.abs(ref))
     assert rel.max() <= 2e-2, rel.max()
     assert rel.mean() <= 2e-3, rel.mean()
+    # the decode: a column is predicted where its logit exceeds -0.5
+    lg = logits.cpu().numpy()
+    want = np.zeros(B, np.uint16)
+    for k in range(10):
+        want |= (lg[:, k] > -0.5).astype(np.uint16) << k
+    assert np.array_equal(mask.cpu().numpy().view(np.uint16), want)
