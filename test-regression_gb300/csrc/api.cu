@@ -61,6 +61,23 @@ struct GraphKey {
   int warm, block, lanes;
 };
 
+// The mixed form's per-fit device workspace: the search -> judge hand-off,
+// the fix and repair queues, the persistent schedule's lists and counters,
+// and the warm start's predictions. Lane 0 is the context's own workspace;
+// mf_fit_host runs alternate chunks on lane 1 (second stream) as well.
+struct Lane {
+  uint16_t* mask = nullptr;
+  uint16_t* count = nullptr;
+  float* x = nullptr;
+  int* queue = nullptr;
+  int* fixq = nullptr;
+  unsigned* qcount = nullptr;
+  int* list = nullptr;
+  unsigned* sched = nullptr;
+  uint16_t* warm_mask = nullptr;
+  float* warm_amp = nullptr;
+};
+
 struct mf_context {
   int device = 0;
   DevConditions cond[MF_MAX_CTYPES];
@@ -104,8 +121,13 @@ struct mf_context {
   uint8_t* d_status = nullptr;
   int32_t* d_iters = nullptr;
   cudaStream_t stream = nullptr;
-  // mf_fit_host pipeline: copy-in and copy-out streams, per-chunk events
+  // mf_fit_host pipeline: copy-in and copy-out streams, per-chunk events, and
+  // a second compute stream with its own workspace (lane 1, allocated on
+  // first use)
   cudaStream_t h2d_stream = nullptr, d2h_stream = nullptr;
+  cudaStream_t stream2 = nullptr;
+  Lane lane1;
+  cudaEvent_t fork = nullptr;
   static constexpr int kHostChunks = 64;
   cudaEvent_t in_done[kHostChunks] = {}, fit_done[kHostChunks] = {};
   LaunchTimer timer;  // per-kernel launch timing (mf_profile), off by default
@@ -172,7 +194,8 @@ int fill_args(mf_context* ctx, const mf_batch* b, const mf_options* o, FitArgs* 
 
 void fill_dev_mixed(const mf_context* c, int t, DevMixed* m);
 
-int dispatch_mixed(mf_context* c, const FitArgs& a, const mf_options* o, cudaStream_t s, bool allow_graph) {
+int dispatch_mixed(mf_context* c, const FitArgs& a, const mf_options* o, cudaStream_t s, bool allow_graph,
+                   int lane) {
   if (o->compute_errors) return MF_EUNSUPPORTED;
   const bool persistent = o->schedule == MF_SCHED_PERSISTENT;
   const int block = o->block_size ? o->block_size : (persistent && c->tuned_block ? c->tuned_block : 128);
@@ -214,6 +237,21 @@ int dispatch_mixed(mf_context* c, const FitArgs& a, const mf_options* o, cudaStr
   m.sms = c->sms;
   m.ws_list = c->ws_list;
   m.ws_sched = c->ws_sched;
+  uint16_t* warm_mask = c->mlp.warm_mask;
+  float* warm_amp = c->mlp.warm_amp;
+  if (lane == 1) {
+    const Lane& L = c->lane1;
+    m.ws_mask = L.mask;
+    m.ws_count = L.count;
+    m.ws_x = L.x;
+    m.ws_queue = L.queue;
+    m.ws_fixq = L.fixq;
+    m.ws_qcount = L.qcount;
+    m.ws_list = L.list;
+    m.ws_sched = L.sched;
+    warm_mask = L.warm_mask;
+    warm_amp = L.warm_amp;
+  }
   m.blocks_per_sm = o->blocks_per_sm;
   m.list_identity = a.ctype == nullptr ? 1 : 0;
   m.judge_df = o->precision == MF_PREC_FP32 ? 1 : 0;
@@ -223,8 +261,8 @@ int dispatch_mixed(mf_context* c, const FitArgs& a, const mf_options* o, cudaStr
   if (warm) {
     fill_infer_args(c->mlp, c->tab[c->mlp.set], 0, &ia);
     ia.sample_stride = a.sample_stride;
-    ia.warm_mask = c->mlp.warm_mask;
-    ia.warm_amp = c->mlp.warm_amp;
+    ia.warm_mask = warm_mask;
+    ia.warm_amp = warm_amp;
     ia.warm_stride = 10;
   }
   const int64_t cap = warm && MlpState::kChunk < MIXED_CHUNK ? MlpState::kChunk : MIXED_CHUNK;
@@ -252,8 +290,8 @@ int dispatch_mixed(mf_context* c, const FitArgs& a, const mf_options* o, cudaStr
       ic.samples = mc.samples;
       ic.pederr = mc.pederr;
       ic.ctype = mc.ctype;
-      mc.warm_mask = c->mlp.warm_mask;
-      mc.warm_amp = c->mlp.warm_amp;
+      mc.warm_mask = warm_mask;
+      mc.warm_amp = warm_amp;
       mc.warm_stride = 10;
       mc.warm_set = c->mlp.set;
       if (tm) tm->mark(MF_K_MLP_INFER, st);
@@ -310,8 +348,9 @@ int dispatch_mixed(mf_context* c, const FitArgs& a, const mf_options* o, cudaStr
 }
 
 int dispatch_form(mf_context* c, const FitArgs& a, const mf_options* o, cudaStream_t s, bool instrumented,
-                  bool allow_graph) {
-  if (o->precision == MF_PREC_MIXED || o->precision == MF_PREC_FP32) return dispatch_mixed(c, a, o, s, allow_graph);
+                  bool allow_graph, int lane) {
+  if (o->precision == MF_PREC_MIXED || o->precision == MF_PREC_FP32)
+    return dispatch_mixed(c, a, o, s, allow_graph, lane);
   if (o->precision != MF_PREC_FP64 || o->schedule != MF_SCHED_GRID || o->warm_start != MF_WARM_NONE)
     return MF_EUNSUPPORTED;
   cudaError_t e = launch_fit_fp64(a, o->block_size, s, instrumented, &c->timer);
@@ -323,8 +362,8 @@ int dispatch_form(mf_context* c, const FitArgs& a, const mf_options* o, cudaStre
 }
 
 int dispatch(mf_context* c, const FitArgs& a, const mf_options* o, cudaStream_t s, bool instrumented,
-             bool allow_graph = true) {
-  const int rc = dispatch_form(c, a, o, s, instrumented, allow_graph);
+             bool allow_graph = true, int lane = 0) {
+  const int rc = dispatch_form(c, a, o, s, instrumented, allow_graph, lane);
   c->timer.mark(-1, s);  // end of this fit's launches
   return rc;
 }
@@ -336,6 +375,36 @@ void destroy_timer(LaunchTimer& t) {
   t.ev = nullptr;
   t.used = 0;
   t.overflow = false;
+}
+
+void free_lane(Lane& L) {
+  void* ps[] = {L.mask, L.count, L.x, L.queue, L.fixq, L.qcount, L.list, L.sched, L.warm_mask, L.warm_amp};
+  for (void* p : ps) cudaFree(p);
+  L = Lane();
+}
+
+// Lane 1 and the second compute stream of mf_fit_host (200 MB), once.
+int grow_lane1(mf_context* c) {
+  if (c->lane1.mask) return MF_OK;
+  Lane& L = c->lane1;
+  cudaError_t e = cudaMalloc(&L.mask, sizeof(uint16_t) * MIXED_CHUNK);
+  if (e == cudaSuccess) e = cudaMalloc(&L.count, sizeof(uint16_t) * MIXED_CHUNK);
+  if (e == cudaSuccess) e = cudaMalloc(&L.x, sizeof(float) * MIXED_CHUNK * KMAX);
+  if (e == cudaSuccess) e = cudaMalloc(&L.queue, sizeof(int) * MIXED_CHUNK);
+  if (e == cudaSuccess) e = cudaMalloc(&L.fixq, sizeof(int) * MIXED_CHUNK);
+  if (e == cudaSuccess) e = cudaMalloc(&L.qcount, 2 * sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMalloc(&L.list, sizeof(int) * MIXED_CHUNK * MF_MAX_CTYPES);
+  if (e == cudaSuccess) e = cudaMalloc(&L.sched, sizeof(unsigned) * SCHED_WORDS);
+  if (e == cudaSuccess) e = cudaMalloc(&L.warm_mask, sizeof(uint16_t) * MlpState::kChunk);
+  if (e == cudaSuccess) e = cudaMalloc(&L.warm_amp, sizeof(float) * MlpState::kChunk * 10);
+  if (e == cudaSuccess && !c->stream2) e = cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking);
+  if (e == cudaSuccess && !c->fork) e = cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    set_last_error("mf_fit_host: second lane", e);
+    free_lane(L);
+    return MF_ENOMEM;
+  }
+  return MF_OK;
 }
 
 void free_staging(mf_context* c) {
@@ -540,6 +609,9 @@ void mf_destroy(mf_context* c) {
   cudaFree(c->ws_qcount);
   cudaFree(c->ws_list);
   cudaFree(c->ws_sched);
+  free_lane(c->lane1);
+  if (c->stream2) cudaStreamDestroy(c->stream2);
+  if (c->fork) cudaEventDestroy(c->fork);
   destroy_timer(c->timer);
   if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
   if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
@@ -692,11 +764,46 @@ int mf_fit_count_flops(mf_context* c, const mf_batch* b, const mf_options* o, do
   return dispatch(c, a, o, (cudaStream_t)stream, true);
 }
 
-// Host-pointer fit, pipelined: the batch is cut into chunks (>= 2^20
-// channels, at most 64); the copy-in of chunk i+1 (h2d stream) and the
-// copy-out of chunk i-1 (d2h stream) run under the fit of chunk i (the
-// context stream), ordered by events. With pinned host buffers the step costs
-// about max(copies, fit) instead of their sum.
+// Chunk boundaries of a host-pointer fit: offs[0] = 0 < ... < offs[k] = n,
+// returns k. Full chunks of B = MIXED_CHUNK channels with a ramp of B/4 and
+// B/2 at both ends: only the first chunk's copy-in and the last chunk's
+// copy-out are not hidden under a fit (88 B in and 99 B out per channel at
+// ~200 GB/s each way against ~0.76 ns of fit per channel). Measured on 10M
+// warm channels (e2e ms per step): 8.74 with this rule, 8.80 with B halved,
+// 9.53 with B quartered, 9.02 without the ramp; the device fit alone 7.55.
+// Batches too small for the ramp are cut into up to eight equal chunks of at
+// least B/8.
+int host_chunks(int64_t n, int64_t* offs) {
+  constexpr int64_t B = MIXED_CHUNK, R = B / 8;
+  constexpr int64_t ramp[2] = {B / 4, B / 2};
+  constexpr int64_t ramp_sum = B / 4 + B / 2;
+  int k = 0;
+  offs[0] = 0;
+  if (n >= 2 * ramp_sum + B) {
+    for (int64_t r : ramp) offs[k + 1] = offs[k] + r, ++k;
+    const int64_t middle = n - 2 * ramp_sum;
+    int64_t parts = (middle + B - 1) / B;  // beyond the event slots the middle chunks grow past B
+    if (parts > mf_context::kHostChunks - 4) parts = mf_context::kHostChunks - 4;
+    for (int64_t p = 0; p < parts; ++p) offs[k + 1] = offs[2] + middle * (p + 1) / parts, ++k;
+    for (int j = 1; j >= 0; --j) offs[k + 1] = offs[k] + ramp[j], ++k;
+  } else {
+    int64_t parts = (n + R - 1) / R;
+    if (parts > 8) parts = 8;
+    if (parts < 1) parts = 1;
+    for (int64_t p = 0; p < parts; ++p) offs[k + 1] = n * (p + 1) / parts, ++k;
+  }
+  return k;
+}
+
+// Host-pointer fit, pipelined: the batch is cut into chunks (host_chunks); the
+// copy-in of chunk i+1 (h2d stream) and the copy-out of chunk i-1 (d2h stream)
+// run under the fit of chunk i, ordered by events. The mixed forms fit even
+// chunks on the context stream and odd chunks on a second stream with its own
+// workspace (lane 1), so neighbouring fits overlap (one chunk's queue kernels,
+// whose time is set by their slowest channels, run beside the next chunk's
+// search); chunk i + 2 reuses chunk i's lane on the same stream. The FP64 form and per-kernel profiling keep
+// one stream. With pinned host buffers the step costs about max(copies, fit)
+// instead of their sum.
 int mf_fit_host(mf_context* c, const mf_batch* hb, const mf_options* o) {
   if (!c || !hb) return MF_EINVAL;
   std::lock_guard<std::mutex> g(c->mu);
@@ -727,23 +834,32 @@ int mf_fit_host(mf_context* c, const mf_batch* hb, const mf_options* o) {
     set_last_error("mf_fit_host: stream/event setup", e);
     return MF_ECUDA;
   }
-  const int64_t min_chunk = int64_t(1) << 20;
-  int64_t chunk = (n + mf_context::kHostChunks - 1) / mf_context::kHostChunks;
-  if (chunk < min_chunk) chunk = min_chunk;
-  const int nchunks = int((n + chunk - 1) / chunk);
+  int64_t offs[mf_context::kHostChunks + 1];
+  const int nchunks = host_chunks(n, offs);
+  const bool two = nchunks > 1 && !c->timer.ev &&
+                   (o->precision == MF_PREC_MIXED || o->precision == MF_PREC_FP32);
+  if (two) {
+    rc = grow_lane1(c);
+    if (rc) return rc;
+    // the second stream starts after everything already queued on the context stream
+    e = cudaEventRecord(c->fork, c->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream2, c->fork, 0);
+  }
   const int ss = hb->sample_stride, as = hb->amp_stride;
   auto cp = [&](void* dst, const void* src, size_t bytes, cudaMemcpyKind k, cudaStream_t st) {
     if (e == cudaSuccess && src && dst && bytes) e = cudaMemcpyAsync(dst, src, bytes, k, st);
   };
   for (int i = 0; i < nchunks && e == cudaSuccess && rc == MF_OK; ++i) {
-    const int64_t off = i * chunk, m = (n - off < chunk) ? n - off : chunk;
+    const int64_t off = offs[i], m = offs[i + 1] - offs[i];
     // copy in
     cp(c->d_samples + off * ss, hb->samples + off * ss, sizeof(double) * m * ss, cudaMemcpyHostToDevice, c->h2d_stream);
     cp(c->d_pederr + off, hb->pederr + off, sizeof(double) * m, cudaMemcpyHostToDevice, c->h2d_stream);
     if (hb->ctype) cp(c->d_ctype + off, hb->ctype + off, m, cudaMemcpyHostToDevice, c->h2d_stream);
     if (e == cudaSuccess) e = cudaEventRecord(c->in_done[i], c->h2d_stream);
     // fit
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->in_done[i], 0);
+    const int lane = two ? (i & 1) : 0;
+    cudaStream_t fs = lane ? c->stream2 : c->stream;
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(fs, c->in_done[i], 0);
     if (e != cudaSuccess) break;
     mf_batch db = *hb;
     db.n = m;
@@ -759,9 +875,9 @@ int mf_fit_host(mf_context* c, const mf_batch* hb, const mf_options* o) {
     db.iters = hb->iters ? c->d_iters + off : nullptr;
     FitArgs a;
     rc = fill_args(c, &db, o, &a);
-    if (rc == MF_OK) rc = dispatch(c, a, o, c->stream, false, false);
+    if (rc == MF_OK) rc = dispatch(c, a, o, fs, false, false, lane);
     if (rc != MF_OK) break;
-    e = cudaEventRecord(c->fit_done[i], c->stream);
+    e = cudaEventRecord(c->fit_done[i], fs);
     // copy out
     if (e == cudaSuccess) e = cudaStreamWaitEvent(c->d2h_stream, c->fit_done[i], 0);
     cp(hb->amplitudes + off * as, c->d_amp + off * as, sizeof(double) * m * as, cudaMemcpyDeviceToHost, c->d2h_stream);
@@ -775,7 +891,11 @@ int mf_fit_host(mf_context* c, const mf_batch* hb, const mf_options* o) {
   }
   // drain all three streams, whatever happened above
   const cudaError_t e1 = cudaStreamSynchronize(c->h2d_stream);
-  const cudaError_t e2 = cudaStreamSynchronize(c->stream);
+  cudaError_t e2 = cudaStreamSynchronize(c->stream);
+  if (c->stream2) {
+    const cudaError_t e4 = cudaStreamSynchronize(c->stream2);
+    if (e2 == cudaSuccess) e2 = e4;
+  }
   const cudaError_t e3 = cudaStreamSynchronize(c->d2h_stream);
   if (rc != MF_OK) return rc;
   if (e == cudaSuccess) e = e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e3);
