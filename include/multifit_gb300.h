@@ -281,6 +281,12 @@ int mf_mlp_set_weights(mf_context* ctx, const float* host_params);
 /* Inference on device pointers: predicted passive set mask[n], amplitudes
  * amp[n][10] (GeV) and optionally the raw outputs logits[n][32]. */
 int mf_mlp_predict(mf_context* ctx, const mf_batch* batch, uint16_t* mask, float* amp, float* logits, void* stream);
+/* Test hook of the inference's timeout path (off by default). While enabled,
+ * every inference wait first waits, for at most 1 ms, on an mbarrier nothing
+ * arrives on: it gives up, the error is recorded (the next mf_fit_host
+ * returns MF_ETIMEOUT), the tensor-core work in flight drains, and the
+ * affected channels are fitted from a cold start (same results). */
+int mf_mlp_test_stall(mf_context* ctx, int enable);
 
 /* Host-only view of the mixed-form tables of a condition set (for checks):
  * whiten [N][N] row-major = L_R^-1 with L_R = chol(samplecor); pinv [p][N]

@@ -143,6 +143,7 @@ SIGNATURES = [
     ("mf_mlp_get_weights", C.c_int, [C.c_void_p, C.c_void_p]),
     ("mf_mlp_set_weights", C.c_int, [C.c_void_p, C.c_void_p]),
     ("mf_mlp_predict", C.c_int, [C.c_void_p, C.POINTER(MfBatch), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("mf_mlp_test_stall", C.c_int, [C.c_void_p, C.c_int]),
     ("mf_synth_conditions", C.c_int, [C.c_int, C.POINTER(MfConditions), C.POINTER(C.c_double)]),
     ("mf_synth_generate", C.c_int, [C.POINTER(MfSynthParams), C.c_int64, C.c_int64, C.c_int, C.c_void_p,
                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
@@ -452,12 +453,16 @@ def _mlp_engine_methods():
         w = np.ascontiguousarray(w, dtype=np.float32)
         _check(self.lib.mf_mlp_set_weights(self.h, w.ctypes.data), "mf_mlp_set_weights")
 
+    def mlp_test_stall(self, enable: bool):
+        """Test hook: inference waits give up after 1 ms (mf_mlp_test_stall)."""
+        _check(self.lib.mf_mlp_test_stall(self.h, 1 if enable else 0), "mf_mlp_test_stall")
+
     def mlp_predict(self, batch: MfBatch, mask_ptr, amp_ptr, logits_ptr=None, stream=None):
         _check(self.lib.mf_mlp_predict(self.h, C.byref(batch), mask_ptr, amp_ptr, logits_ptr, stream),
                "mf_mlp_predict")
 
     return dict(mlp_init=mlp_init, mlp_train=mlp_train, mlp_gradient=mlp_gradient, mlp_get_weights=mlp_get_weights,
-                mlp_set_weights=mlp_set_weights, mlp_predict=mlp_predict)
+                mlp_set_weights=mlp_set_weights, mlp_test_stall=mlp_test_stall, mlp_predict=mlp_predict)
 
 
 for _k, _v in _mlp_engine_methods().items():

@@ -218,6 +218,7 @@ int dispatch_mixed(mf_context* c, const FitArgs& a, const mf_options* o, cudaStr
   m.max_iter64 = o->max_iter_nnls > 0 ? o->max_iter_nnls : 1;
   m.tol32 = 1e-5f;
   m.eps = o->nnls_eps;
+  m.eps32 = float(o->nnls_eps);
   m.samples = a.samples;
   m.pederr = a.pederr;
   m.ctype = a.ctype;
@@ -959,6 +960,13 @@ int mf_mlp_set_weights(mf_context* c, const float* host) {
   return mlp_set_weights(c->mlp, host);
 }
 
+int mf_mlp_test_stall(mf_context* c, int enable) {
+  if (!c) return MF_EINVAL;
+  std::lock_guard<std::mutex> g(c->mu);
+  c->mlp.test_stall = enable ? 1 : 0;
+  return MF_OK;
+}
+
 int mf_mlp_predict(mf_context* c, const mf_batch* b, uint16_t* mask, float* amp, float* logits, void* stream) {
   if (!c || !b || !mask || !amp || b->n < 0 || (b->n > 0 && (!b->samples || !b->pederr))) return MF_EINVAL;
   if (!c->mlp.ready) return MF_ENOTRAINED;
@@ -1136,6 +1144,7 @@ extern "C" int mf_fit_noalloc(mf_context* c, const mf_batch* b, const mf_options
   m.max_iter64 = o->max_iter_nnls > 0 ? o->max_iter_nnls : 1;
   m.tol32 = 1e-5f;
   m.eps = o->nnls_eps;
+  m.eps32 = float(o->nnls_eps);
   m.samples = a.samples;
   m.pederr = a.pederr;
   m.ctype = a.ctype;

@@ -138,6 +138,7 @@ struct MixedArgs {
   int max_iter32, max_iter64;
   float tol32;
   double eps;
+  float eps32;  // eps rounded to float (the double-float judge's KKT tolerance)
   const double* samples;
   const double* pederr;
   const uint8_t* ctype;

@@ -457,16 +457,21 @@ __device__ __forceinline__ bool whiten64(const MixedArgs& a, const DevMixed& T, 
 
 // Outputs of a judged channel: amplitudes, chi2, in-time amplitude, active
 // mask (support of x), status, counters, FP64 flops.
+// A finite double, decided on its exponent bits (no FP64 instruction).
+__device__ __forceinline__ bool finite64(double v) {
+  return ((__double2hiint(v) >> 20) & 0x7ff) != 0x7ff;
+}
+
 template <int N, int K>
 __device__ __forceinline__ void store_outputs(const MixedArgs& a, const DevMixed& T, int64_t ch, const double* x,
                                               double chi2, bool bad, bool converged, int adds, int solves, int f64) {
   double* out = a.amplitudes + ch * a.amp_stride;
-  bool finite = isfinite(chi2);
+  bool finite = finite64(chi2);
   uint16_t support = 0;
 #pragma unroll
   for (int k = 0; k < K; ++k) {
     out[k] = x[k];
-    finite = finite && isfinite(x[k]);
+    finite = finite && finite64(x[k]);
     if (pos64(x[k])) support |= uint16_t(1u << k);
   }
   for (int k = K; k < a.amp_stride && k < KMAX; ++k) out[k] = 0.;
@@ -666,10 +671,6 @@ __device__ __forceinline__ void df_fma(float& hi, float& lo, float ah, float al,
   df_acc(hi, lo, p, e);
 }
 
-// A finite double, decided on its exponent bits (no FP64 instruction).
-__device__ __forceinline__ bool finite64(double v) {
-  return ((__double2hiint(v) >> 20) & 0x7ff) != 0x7ff;
-}
 
 template <int N, int K>
 __device__ __forceinline__ void judge_df_body(const MixedArgs& a, const DevMixed& T, int64_t ch, unsigned* qcount,
@@ -679,6 +680,11 @@ __device__ __forceinline__ void judge_df_body(const MixedArgs& a, const DevMixed
   const double* in = a.samples + ch * a.sample_stride;
   const double sig = a.pederr[ch];
   bool bad = !finite64(sig) || !pos64(sig);
+  float sgh, sgl;  // pederr as a float pair, its square as another
+  split64(sig, sgh, sgl);
+  float s2h, s2l;
+  two_prod(sgh, sgh, s2h, s2l);
+  s2l = fmaf(2.f * sgh, sgl, s2l);
   float sh[N], sl[N];
 #pragma unroll
   for (int i = 0; i < N; ++i) {
@@ -765,7 +771,7 @@ __device__ __forceinline__ void judge_df_body(const MixedArgs& a, const DevMixed
       for (int i = 0; i < N; ++i)
         if (i >= T.gfz[k]) e[i] = fmaf(fabsf(T.G32[k * N + i]), ek, e[i]);
     }
-    const float tol = float(a.eps * sig * sig);
+    const float tol = a.eps32 * s2h;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
       float w = 0.f, mag = 0.f, werr = 0.f;
@@ -797,7 +803,18 @@ __device__ __forceinline__ void judge_df_body(const MixedArgs& a, const DevMixed
   double x[K];
 #pragma unroll
   for (int k = 0; k < K; ++k) x[k] = double(xh[k]) + double(xl[k]);
-  const double chi2 = (double(ch2) + double(cl2)) / (sig * sig);
+  // chi2 / pederr^2 in double-float: q1 = c / s2 rounded, then the remainder
+  // c - q1 s2 (exact leading difference) divided once more (~2^-46 relative)
+  double chi2;
+  if (!bad) {
+    const float q1 = __fdiv_rn(ch2, s2h);
+    float p, e;
+    two_prod(q1, s2h, p, e);
+    const float rem = __fadd_rn(__fsub_rn(ch2, p), __fsub_rn(cl2, fmaf(q1, s2l, e)));
+    chi2 = double(q1) + double(__fdiv_rn(rem, s2h));
+  } else {
+    chi2 = (double(ch2) + double(cl2)) / (sig * sig);
+  }
   store_outputs<N, K>(a, T, ch, x, chi2, bad, true, int(cnt & 255u), int(cnt >> 8) + 1, K + 4);
 }
 

@@ -61,6 +61,7 @@ struct MlpInferArgs {
   int warm_stride;
   float* logits;        // optional [n][MLP_OUT] raw outputs
   unsigned* err;        // device error word (MLP_ERR_* bits), or null
+  int test_stall;       // wait first on an mbarrier nothing arrives on (timeout test)
 };
 
 // Bits of the inference error word.

@@ -36,6 +36,7 @@ struct MlpState {
   uint16_t* warm_mask = nullptr;
   float* warm_amp = nullptr;
   unsigned* infer_err = nullptr;  // inference error word (MLP_ERR_* bits)
+  int test_stall = 0;             // mf_mlp_test_stall
 };
 
 // Host buffers of a gradient check (one forward/backward on the first batch).

@@ -42,6 +42,7 @@ constexpr int TILE = 128;             // channels per tile = MMA M = TMEM lanes
 constexpr int kThreads = 512;         // four warpgroups, 32 columns of every layer each
 constexpr uint32_t kTmemCols = 256;   // per slot: D of every layer (layer 3 uses its first 32 columns)
 constexpr uint64_t kWaitNs = 200000000ull;  // 0.2 s: an MMA round takes ~1 us
+constexpr uint64_t kTestWaitNs = 1000000ull;  // the timeout test's wait: 1 ms
 
 extern __shared__ __align__(128) unsigned char tc_smem_raw[];
 
@@ -53,6 +54,7 @@ struct TcSmem {
   float b1[MLP_H], b2[MLP_H], b3[MLP_OUT];
   float scale[2][2][TILE];   // |y| of each slot's channels, features -> decode (by pair parity)
   unsigned long long bar[2]; // MMA completion per slot
+  unsigned long long never;  // nothing arrives on it (the timeout test's wait)
   uint32_t tmem;             // TMEM base written by tcgen05.alloc
 };
 
@@ -192,10 +194,11 @@ __global__ void __launch_bounds__(kThreads, 2) mlp_infer_tc_kernel(const MlpInfe
     S.b2[e] = a.b2[e];
   }
   if (tid < MLP_OUT) S.b3[tid] = a.b3[tid];
-  const uint32_t bar0 = smem_u32(&S.bar[0]), bar1 = smem_u32(&S.bar[1]);
+  const uint32_t bar0 = smem_u32(&S.bar[0]), bar1 = smem_u32(&S.bar[1]), never = smem_u32(&S.never);
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0) : "memory");
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar1) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(never) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -244,7 +247,7 @@ __global__ void __launch_bounds__(kThreads, 2) mlp_infer_tc_kernel(const MlpInfe
   };
   // everyone waits for slot s's last commit; false (for every thread) if it gave up
   auto wait = [&](int s) -> bool {
-    const bool ok = mbar_wait(slot_bar(s), phase[s], kWaitNs);
+    const bool ok = a.test_stall ? mbar_wait(never, 0u, kTestWaitNs) : mbar_wait(slot_bar(s), phase[s], kWaitNs);
     const bool all_ok = __syncthreads_and(ok);
     if (all_ok) {
       phase[s] ^= 1u;

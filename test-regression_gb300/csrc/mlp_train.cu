@@ -117,6 +117,7 @@ void fill_infer_args(const MlpState& s, const HostTables& tab, int intime_unused
   a->b2 = s.params + P_B2;
   a->b3 = s.params + P_B3;
   a->err = s.infer_err;
+  a->test_stall = s.test_stall;
 }
 
 // One training run over n channels whose converged amplitudes are given.
