@@ -1,6 +1,6 @@
-// Mixed-precision multifit: an FP32 active-set search and an FP64 judge, as
-// two kernels, started cold or from the passive sets and amplitudes the
-// warm-start MLP predicted.
+// Mixed-precision multifit: an FP32 active-set search and an FP64 (or
+// double-float) judge in separate kernels, started cold or from the passive
+// sets and amplitudes the warm-start MLP predicted.
 //
 // With an amplitude-independent covariance the whitened problem of a channel
 // is min ||G x - y||^2 with the condition set's shared G = L_R^-1 P and
@@ -12,28 +12,33 @@
 //     gradient w = G^T y - H x, solve the passive set, step back and drop
 //     columns that go non-positive -- from an empty set or the predicted one;
 //     writes the passive mask and the FP32 amplitudes of each channel.
+//   screen_kernel  (cold starts; FP32, branch-free): the residual of the FP32
+//     solution in double-float and the KKT test of every inactive column; a
+//     channel with provably violating columns is queued for the fix.
 //   judge_kernel   (FP64 -- or, for MF_PREC_FP32, the same steps in double-float
-//     FP32 arithmetic; lean, branch-free: every lane the same FP64
-//     instructions): y in FP64, the FP64 solve on the FP32 passive set, the
-//     FP64 residual, chi2 = ||y - G x||^2 / pederr^2, and the KKT test
+//     FP32 arithmetic; lean, branch-free: every lane the same instructions):
+//     y, the solve on the passive set through the operator table, the
+//     residual, chi2 = ||y - G x||^2 / pederr^2, and the KKT test
 //     max w < eps * pederr^2 (the reference's absolute eps on the
 //     pederr-scaled gradient, PulseChiSqSNNLS.cpp:242) screened in FP32 with
-//     a rounding bound. A channel whose amplitudes are positive but whose
-//     columns provably violate the test is queued for
+//     a rounding bound. On warm starts a channel whose amplitudes are positive
+//     but whose columns provably violate the test is queued for the fix;
 //   fix_kernel     (FP32, compacted): the FNNLS step with those columns and a
-//     double-float screen of the new set, then
+//     double-float screen of the new set, then (warm starts)
 //   judge_fixed_kernel: the judge again, on the fixed channels only. Every
 //     other rejected channel is queued for
 //   repair_kernel  (FP64): the FNNLS loop in FP64 to the FP64 KKT point, so
 //     the result is the FP64 KKT point whatever the FP32 search found.
+// Order per set: cold search, screen, fix, judge, repair; warm search, judge,
+// fix, judge_fixed, repair (launch_set).
 //
-// Why two kernels: on this GPU an FP64 warp instruction costs the full pipe
-// time whatever the number of active lanes, and FP64 results have long
-// latency. In one kernel the FP32 search set the register budget (168), so
-// only three warps per scheduler were resident and the dependent FP64 chains
-// of the judge were latency-bound (the judge took ~6x its pipe time). Apart,
-// the judge runs convergent at high occupancy; the hand-off costs ~124 bytes
-// per channel of HBM traffic.
+// Why separate kernels: on this GPU an FP64 warp instruction costs the full
+// pipe time whatever the number of active lanes, and FP64 results have long
+// latency. With the search in the same kernel its register budget (168) left
+// three warps per scheduler and the judge's dependent FP64 chains were
+// latency-bound (~6x its pipe time). Apart, the judge runs convergent at high
+// occupancy, and the queue kernels run their rare channels in full warps; the
+// hand-off costs ~124 bytes per channel of HBM traffic.
 //
 // The covariance does not depend on the amplitudes (no fullpulsecov), so the
 // outer chi2 loop of Minimize (multifit_cpu/src/PulseChiSqSNNLS.cpp:149-166)
