@@ -534,7 +534,7 @@ def run_ours(args, world, rank, local):
             "vs_baseline": None,
             "dtype": {"fp64": "f64", "mixed": "f32+f64", "fp32": "f32 (double-float judge; f64 repair)",
                       "warm": "f32 (double-float judge; f64 repair; bf16 MLP)"}[args.form],
-            "data": "synthetic (seeded Philox generator; BASELINE shapes and distributions)",
+            "data": "synthetic (seeded Philox generator; the workload's shapes and value distributions)",
             "config": {
                 "workload": wl,
                 "description": WORKLOAD_DESC.get(wl, wl),
@@ -735,7 +735,7 @@ def run_reference(args, world, rank):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
-        "data": "synthetic (seeded Philox generator; BASELINE shapes and distributions)",
+        "data": "synthetic (seeded Philox generator; the workload's shapes and value distributions)",
         "config": {"workload": args.workload, "description": WORKLOAD_DESC.get(args.workload, args.workload),
                    "form": "reference multifit_cpu path (oracle port: Eigen absent, reference not buildable)",
                    "max_iter_nnls": args.max_iter, "nnls_start": ["reference", "support"][args.start]},
