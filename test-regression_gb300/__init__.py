@@ -22,6 +22,9 @@ import numpy as np
 
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG_DIR, "_build", "libmultifit_gb300.so")
+# loaded by path under the name multifit_gb300: make it a package so that its
+# submodules (rootio, ecal_data_io) import as multifit_gb300.<name>
+__path__ = [PKG_DIR]
 
 MAX_SAMPLES = 10
 MAX_PULSES = 10
