@@ -1,0 +1,99 @@
+"""The C++ reader of the reference's data files (include/multifit_gb300_io.hpp,
+driven by tests/cpp/rootio_check.cpp) on the CPU: its zlib decoder against
+Python's zlib over every compression level and strategy, and its reading of
+the reference's files against the fixture the Python reader made
+(tests/golden/replay_mysample_100.npz), bit for bit."""
+import os
+import struct
+import subprocess
+import zlib
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden", "replay_mysample_100.npz")
+DATA = os.path.join(os.environ.get("MULTIFIT_REFERENCE_ROOT", "/root/reference"), "data")
+SAMPLE_100 = os.path.join(DATA, "mysample_100_0.000_0.000_10_25.00_10.00_0.00_1.000_1.00_CRRC43_0.00_slew_1.00.root")
+SAMPLE_1000 = os.path.join(DATA,
+                           "mysample_1000_0.000_0.000_10_25.00_10.00_0.00_1.000_1.00_CRRC43_0.00_slew_1.00.root")
+SHAPE = os.path.join(DATA, "EmptyFile.root")
+needs_data = pytest.mark.skipif(not (os.path.exists(SAMPLE_100) and os.path.exists(SHAPE)),
+                                reason="the reference's data files are absent")
+
+
+@pytest.fixture(scope="module")
+def exe(tmp_path_factory):
+    out = str(tmp_path_factory.mktemp("rootio") / "rootio_check")
+    for extra in ((), ("-funsigned-char",)):  # plain char is unsigned on Arm
+        subprocess.run(["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror", *extra, "-I",
+                        os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "cpp", "rootio_check.cpp"),
+                        "-o", out], check=True, capture_output=True)
+    return out
+
+
+def run(exe, *args):
+    return subprocess.run([exe, *map(str, args)], capture_output=True, text=True)
+
+
+def test_inflate_matches_zlib(exe, tmp_path):
+    rng = np.random.default_rng(7)
+    datas = [b"", b"x", b"abcabcabcabc" * 3, rng.bytes(70_000), bytes(100_000), b"0123456789" * 5000,
+             np.cumsum(rng.standard_normal(20_000)).astype(">f8").tobytes(),
+             rng.integers(0, 4, 50_000, dtype=np.uint8).tobytes()]
+    strategies = (zlib.Z_DEFAULT_STRATEGY, zlib.Z_FILTERED, zlib.Z_HUFFMAN_ONLY, zlib.Z_RLE, zlib.Z_FIXED)
+    path = tmp_path / "streams.bin"
+    n = 0
+    with open(path, "wb") as f:
+        for d in datas:
+            for level in range(10):
+                for strategy in strategies:
+                    c = zlib.compressobj(level, zlib.DEFLATED, 15, 9, strategy)
+                    z = c.compress(d) + c.flush()
+                    f.write(struct.pack("<QQ", len(d), len(z)) + z + d)
+                    n += 1
+    r = run(exe, "inflate", path)
+    assert r.returncode == 0 and r.stdout.strip() == f"ok {n}", r.stdout
+
+
+def test_inflate_rejects_corrupt_stream(exe, tmp_path):
+    d = b"the quick brown fox " * 200
+    z = bytearray(zlib.compress(d, 6))
+    z[-1] ^= 1  # Adler-32
+    path = tmp_path / "bad.bin"
+    path.write_bytes(struct.pack("<QQ", len(d), len(z)) + bytes(z) + d)
+    r = run(exe, "inflate", path)
+    assert r.returncode == 2 and "Adler-32" in r.stdout
+
+
+@needs_data
+def test_cpp_reader_matches_python_reader_fixture(exe, tmp_path):
+    g = dict(np.load(GOLDEN))
+    out = tmp_path / "dump.bin"
+    r = run(exe, "dump", SAMPLE_100, SHAPE, out)
+    assert r.returncode == 0, r.stdout
+    b = out.read_bytes()
+    n = struct.unpack_from("=q", b, 0)[0]
+    assert n == 100
+    f = np.frombuffer(b, dtype=np.float64, offset=8, count=n * 10 + n + 19 + 100 + 100 + 3)
+    p = 0
+    for name, size, shape in (("samples", n * 10, (n, 10)), ("truth", n, (n,)), ("fullpulse", 19, (19,)),
+                              ("noisecor", 100, (10, 10)), ("P", 100, (10, 10)), ("tail", 3, (3,))):
+        arr = f[p:p + size].reshape(shape)
+        if name == "P":
+            arr = arr.reshape(10, 10).T  # column-major
+        assert np.array_equal(arr, g[name]), name
+        p += size
+    npts, srt = struct.unpack_from("=qq", b, 8 + 8 * p)
+    assert npts == int(g["graph_points"]) and bool(srt) == bool(g["graph_sorted"])
+
+
+@needs_data
+def test_cpp_reader_errors(exe):
+    if os.path.exists(SAMPLE_1000):
+        r = run(exe, "expect-error", SAMPLE_1000, "Samples", "samples", "not closed")
+        assert r.returncode == 0, r.stdout
+    r = run(exe, "expect-error", SAMPLE_100, "Samples", "no_such_branch", "no baskets")
+    assert r.returncode == 0, r.stdout
+    r = run(exe, "patch-compression", SAMPLE_100, "samples")
+    assert r.returncode == 0, r.stdout
