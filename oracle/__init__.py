@@ -17,41 +17,87 @@ import numpy as np
 from . import build_oracle
 
 _lib = None
+_lib_sep = None
 _ref = None
+_ref_ocl = {}
 
 KMAX = 10
 
 dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 
 
+def _bind(L):
+    L.oracle_cholesky.argtypes = [dp, dp, C.c_int, C.c_int]
+    L.oracle_forward.argtypes = [dp, C.c_int, dp, dp, C.c_int]
+    L.oracle_backward.argtypes = [dp, C.c_int, dp, dp, C.c_int]
+    L.oracle_rc_addition.argtypes = [dp, dp, C.c_int, dp, dp, C.c_int]
+    L.oracle_inbetween_removal.argtypes = [dp, dp, C.c_int, dp, dp, C.c_int, C.c_int]
+    L.oracle_swap_sym.argtypes = [dp, C.c_int, C.c_int, C.c_int, C.c_int]
+    L.oracle_inplace_fnnls.argtypes = [dp, dp, dp, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int,
+                                       np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")]
+    L.oracle_fit_batch.restype = C.c_int
+    L.oracle_fit_batch.argtypes = [C.c_int64, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
+                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
+                                   C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
+                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_void_p, C.c_void_p]
+    L.oracle_kkt_violation.restype = C.c_double
+    L.oracle_kkt_violation.argtypes = [dp, dp, dp, C.c_int, C.c_int]
+    L.oracle_nnls_bruteforce.restype = C.c_double
+    L.oracle_nnls_bruteforce.argtypes = [dp, dp, C.c_int, C.c_int, dp]
+    L.oracle_nnls_lawson_hanson.restype = C.c_int
+    L.oracle_nnls_lawson_hanson.argtypes = [dp, dp, C.c_int, C.c_int, dp, C.c_int]
+    L.oracle_hardware_threads.restype = C.c_int
+    return L
+
+
 def lib():
     global _lib
     if _lib is None:
-        path = build_oracle.build_oracle()
-        L = C.CDLL(path)
-        L.oracle_cholesky.argtypes = [dp, dp, C.c_int, C.c_int]
-        L.oracle_forward.argtypes = [dp, C.c_int, dp, dp, C.c_int]
-        L.oracle_backward.argtypes = [dp, C.c_int, dp, dp, C.c_int]
-        L.oracle_rc_addition.argtypes = [dp, dp, C.c_int, dp, dp, C.c_int]
-        L.oracle_inbetween_removal.argtypes = [dp, dp, C.c_int, dp, dp, C.c_int, C.c_int]
-        L.oracle_swap_sym.argtypes = [dp, C.c_int, C.c_int, C.c_int, C.c_int]
-        L.oracle_inplace_fnnls.argtypes = [dp, dp, dp, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int,
-                                           np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")]
-        L.oracle_fit_batch.restype = C.c_int
-        L.oracle_fit_batch.argtypes = [C.c_int64, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
-                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
-                                       C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
-                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
-                                       C.c_void_p, C.c_void_p]
-        L.oracle_kkt_violation.restype = C.c_double
-        L.oracle_kkt_violation.argtypes = [dp, dp, dp, C.c_int, C.c_int]
-        L.oracle_nnls_bruteforce.restype = C.c_double
-        L.oracle_nnls_bruteforce.argtypes = [dp, dp, C.c_int, C.c_int, dp]
-        L.oracle_nnls_lawson_hanson.restype = C.c_int
-        L.oracle_nnls_lawson_hanson.argtypes = [dp, dp, C.c_int, C.c_int, dp, C.c_int]
-        L.oracle_hardware_threads.restype = C.c_int
-        _lib = L
+        _lib = _bind(C.CDLL(build_oracle.build_oracle()))
     return _lib
+
+
+def lib_separate():
+    """The oracle built with each product and sum of its FMA expressions
+    rounded separately (the build compared with the reference's plain-C FNNLS)."""
+    global _lib_sep
+    if _lib_sep is None:
+        _lib_sep = _bind(C.CDLL(build_oracle.build_oracle_separate()))
+    return _lib_sep
+
+
+def ref_ocl(bits: int = 64):
+    """The reference's OpenCL FNNLS (multifit_ocl/device/regression_inplace_fnnls.cl)
+    compiled as C, FP64 (bits=64) or as written in FP32 (bits=32); None where
+    the reference tree is absent."""
+    if bits not in _ref_ocl:
+        paths = build_oracle.build_ref_ocl()
+        if paths is None:
+            return None
+        for b, path in paths.items():
+            L = C.CDLL(path)
+            L.ref_ocl_inplace_fnnls.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_uint]
+            L.ref_ocl_data_type_bytes.restype = C.c_int
+            _ref_ocl[b] = L
+    return _ref_ocl[bits]
+
+
+def ref_ocl_inplace_fnnls(A: np.ndarray, b: np.ndarray, x0: np.ndarray | None = None, eps: float = 1e-11,
+                          max_iter: int = 1000, bits: int = 64) -> np.ndarray:
+    """The reference's OpenCL FNNLS on one 10x10 problem (warm x0 as its
+    final_s starts from x); returns x in the kernel's data type."""
+    L = ref_ocl(bits)
+    if L is None:
+        raise RuntimeError("the reference tree is needed for the OpenCL FNNLS")
+    dt = np.float64 if bits == 64 else np.float32
+    A = np.ascontiguousarray(A, dtype=dt)  # row-major, as the kernel indexes it
+    if A.shape != (10, 10):
+        raise ValueError("the OpenCL kernel is fixed at 10 x 10")
+    bb = np.ascontiguousarray(b, dtype=dt).copy()
+    x = np.zeros(10, dtype=dt) if x0 is None else np.ascontiguousarray(x0, dtype=dt).copy()
+    L.ref_ocl_inplace_fnnls(A.ctypes.data, bb.ctypes.data, x.ctypes.data, eps, max_iter)
+    return x
 
 
 def ref():
@@ -79,15 +125,16 @@ def hardware_threads() -> int:
 
 
 def inplace_fnnls(A: np.ndarray, b: np.ndarray, x0: np.ndarray | None = None, eps: float = 1e-11,
-                  max_iter: int = 1000, variant: int = 0, start: int = 0):
-    """FNNLS on a whitened problem. A: (N, K). Returns (x, stats dict)."""
+                  max_iter: int = 1000, variant: int = 0, start: int = 0, separate_rounding: bool = False):
+    """FNNLS on a whitened problem. A: (N, K). Returns (x, stats dict).
+    separate_rounding: use the build that rounds each product and sum."""
     A = np.asarray(A, dtype=np.float64)
     N, K = A.shape
     Acm = np.ascontiguousarray(A.T)  # column-major flat
     x = np.zeros(K) if x0 is None else np.array(x0, dtype=np.float64)
     st = np.zeros(5, dtype=np.int32)
-    lib().oracle_inplace_fnnls(Acm.ravel(), np.ascontiguousarray(b, dtype=np.float64), x, N, K, eps, max_iter,
-                               variant, start, st)
+    (lib_separate() if separate_rounding else lib()).oracle_inplace_fnnls(
+        Acm.ravel(), np.ascontiguousarray(b, dtype=np.float64), x, N, K, eps, max_iter, variant, start, st)
     return x, {"outer": int(st[0]), "inner": int(st[1]), "converged": int(st[2]), "passive": int(st[3]),
                "mask": int(st[4])}
 

@@ -12,6 +12,17 @@
   ``avoid-fma-max-bits`` heuristic off), which is the oracle's canonical
   order; the tests check that claim bit for bit.
 
+* ``oracle/_build/liboracle_sep.so``: the same restatement built with
+  ``ORACLE_SEPARATE_ROUNDING`` (each product and sum of an FMA expression
+  rounded on its own), for the pin below.
+* ``oracle/_ref/libref_ocl_fnnls_f64.so`` / ``_f32.so``: the reference's own
+  plain-C twin of the incremental-Cholesky FNNLS, the OpenCL kernel source
+  ``multifit_ocl/device/regression_inplace_fnnls.cl``, compiled unmodified as
+  C through ref_ocl_fnnls_driver.c with ``-ffp-contract=off`` (the source's
+  own roundings): once with its ``data_type`` float as written and once with
+  float mapped to double. Built only where the reference tree exists. The
+  FP64 build equals liboracle_sep.so's incremental FNNLS bit for bit.
+
 The rest of the reference path (inplace_fnnls, PulseChiSqSNNLS) includes
 Eigen, which the reference does not vendor and which is absent here, so it is
 not built.
@@ -30,7 +41,10 @@ REF_OUT = os.path.join(HERE, "_ref")
 REFERENCE_ROOT = os.environ.get("MULTIFIT_REFERENCE_ROOT", "/root/reference")
 
 ORACLE_LIB = os.path.join(BUILD, "liboracle.so")
+ORACLE_SEP_LIB = os.path.join(BUILD, "liboracle_sep.so")
 REF_LIB = os.path.join(REF_OUT, "libref_linalgebra.so")
+REF_OCL_LIBS = {64: os.path.join(REF_OUT, "libref_ocl_fnnls_f64.so"),
+                32: os.path.join(REF_OUT, "libref_ocl_fnnls_f32.so")}
 
 
 def _fma_flag() -> list[str]:
@@ -48,16 +62,43 @@ def _stale(target: str, sources: list[str]) -> bool:
     return any(os.path.getmtime(s) > t for s in sources)
 
 
-def build_oracle(force: bool = False) -> str:
+def _build_oracle_lib(target: str, defines: list[str], force: bool) -> str:
     src = os.path.join(HERE, "multifit_oracle.cpp")
-    if force or _stale(ORACLE_LIB, [src, __file__]):
+    if force or _stale(target, [src, __file__]):
         os.makedirs(BUILD, exist_ok=True)
-        tmp = ORACLE_LIB + ".tmp"
-        cmd = ["g++", "-std=c++17", "-O3", "-ffp-contract=off", "-fPIC", "-shared", "-pthread",
+        tmp = target + ".tmp"
+        cmd = ["g++", "-std=c++17", "-O3", "-ffp-contract=off", "-fPIC", "-shared", "-pthread", *defines,
                src, "-o", tmp]
         subprocess.check_call(cmd)
-        os.replace(tmp, ORACLE_LIB)
-    return ORACLE_LIB
+        os.replace(tmp, target)
+    return target
+
+
+def build_oracle(force: bool = False) -> str:
+    return _build_oracle_lib(ORACLE_LIB, [], force)
+
+
+def build_oracle_separate(force: bool = False) -> str:
+    return _build_oracle_lib(ORACLE_SEP_LIB, ["-DORACLE_SEPARATE_ROUNDING"], force)
+
+
+def build_ref_ocl(force: bool = False) -> dict | None:
+    """The reference's OpenCL FNNLS compiled as C, {64: path, 32: path}, or
+    None where the reference tree is absent."""
+    dev = os.path.join(REFERENCE_ROOT, "multifit_ocl", "device")
+    cl = os.path.join(dev, "regression_inplace_fnnls.cl")
+    if not os.path.exists(cl):
+        return None
+    src = os.path.join(HERE, "ref_ocl_fnnls_driver.c")
+    for bits, target in REF_OCL_LIBS.items():
+        if force or _stale(target, [src, __file__]):
+            os.makedirs(REF_OUT, exist_ok=True)
+            tmp = target + ".tmp"
+            cmd = ["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fPIC", "-shared",
+                   *(["-DMF_REF_OCL_DOUBLE"] if bits == 64 else []), "-I", dev, "-x", "c", src, "-o", tmp, "-lm"]
+            subprocess.check_call(cmd)
+            os.replace(tmp, target)
+    return dict(REF_OCL_LIBS)
 
 
 def build_ref(force: bool = False) -> str | None:
@@ -79,6 +120,8 @@ def main() -> int:
     force = "--force" in sys.argv
     print(build_oracle(force))
     print(build_ref(force) or "reference tree absent: oracle/_ref not built")
+    print(build_oracle_separate(force))
+    print(build_ref_ocl(force) or "reference tree absent: OpenCL FNNLS not built")
     return 0
 
 

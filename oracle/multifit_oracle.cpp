@@ -62,7 +62,15 @@ struct Flops {
   inline void op(double k = 1) { v += k; }
 };
 
+// Every a*b + c of the canonical order is one fused multiply-add. Built with
+// ORACLE_SEPARATE_ROUNDING, the same expressions round the product and the sum
+// separately (the file is compiled -ffp-contract=off): that build is the one
+// compared bit for bit with the reference's plain-C FNNLS compiled likewise.
+#ifdef ORACLE_SEPARATE_ROUNDING
+inline double FMA(double a, double b, double c) { return a * b + c; }
+#else
 inline double FMA(double a, double b, double c) { return std::fma(a, b, c); }
+#endif
 
 // ---------------------------------------------------------------------------
 // linalgebra restatement (row-major square storage of leading dimension ld)
