@@ -435,8 +435,10 @@ class RootFile {
     const int32_t n = detail::i32(d, p);
     p += 4;
     for (std::vector<double>* arr : {&g.x, &g.y}) {
-      const uint8_t present = d.at(p++);
+      if (p >= d.size()) throw FormatError(path_ + ": " + path + ": record ends before its arrays");
+      const uint8_t present = d[p++];
       if (!present) continue;
+      if (n < 0 || p + 8 * size_t(n) > d.size()) throw FormatError(path_ + ": " + path + ": array runs past the record");
       arr->resize(size_t(n));
       for (int32_t i = 0; i < n; ++i) (*arr)[size_t(i)] = detail::value<double>(d, p + 8 * size_t(i));
       p += 8 * size_t(n);
@@ -499,7 +501,8 @@ class RootFile {
   }
 
   std::string tstring(size_t& p) const {
-    size_t n = data_.at(p++);
+    if (p >= data_.size()) throw FormatError(path_ + ": string runs past the file");
+    size_t n = data_[p++];
     if (n == 255) {
       n = size_t(detail::i32(data_, p));
       p += 4;

@@ -35,6 +35,7 @@ supported and raise. Nothing here runs on the GPU.
 """
 from __future__ import annotations
 
+import functools
 import lzma
 import os
 import struct
@@ -49,6 +50,22 @@ IS_SORTED_X = 1 << 14  # TGraph::kIsSortedX in TObject::fBits
 
 class RootFormatError(ValueError):
     """The file is not a ROOT file this reader can decode, or it is damaged."""
+
+
+def _checked(fn):
+    """Reports a damaged record as RootFormatError, whatever low-level error
+    (short buffer, bad index, corrupt compressed block) decoding it hit."""
+
+    @functools.wraps(fn)
+    def wrapper(*args, **kwargs):
+        try:
+            return fn(*args, **kwargs)
+        except (RootFormatError, KeyError):
+            raise
+        except (struct.error, IndexError, ValueError, zlib.error, lzma.LZMAError) as e:
+            raise RootFormatError(f"malformed record ({type(e).__name__}: {e})") from e
+
+    return wrapper
 
 
 @dataclass
@@ -115,6 +132,7 @@ def _skip_named_and_attributes(buf, what: str):
 class RootFile:
     """Read-only view of a ROOT file held in memory."""
 
+    @_checked
     def __init__(self, source):
         if isinstance(source, (bytes, bytearray, memoryview)):
             self.path = "<bytes>"
@@ -147,6 +165,7 @@ class RootFile:
         self.top = self._dir_record(self.begin + self.nbytes_name)
 
     # -- records -------------------------------------------------------------
+    @_checked
     def read_key(self, pos: int) -> Key:
         d = self.data
         if pos < 0 or pos + 18 > len(d):
@@ -166,6 +185,8 @@ class RootFile:
 
     def _dir_record(self, pos: int) -> dict:
         d = self.data
+        if not 0 <= pos <= len(d) - 18:
+            raise RootFormatError(f"{self.path}: directory record at {pos} outside the file")
         version, _c, _m, nbytes_keys, nbytes_name = struct.unpack_from(">hIIii", d, pos)
         p = pos + 18
         if version > 1000:
@@ -191,6 +212,7 @@ class RootFile:
             p = k.header_end
         return keys
 
+    @_checked
     def keys(self, directory: str = "") -> list[Key]:
         """Keys of a directory ("" = top, "A/B" = nested)."""
         rec = self.top
@@ -207,17 +229,19 @@ class RootFile:
             raise KeyError(f"{self.path}: no object named {name!r}")
         return max(hits, key=lambda k: k.cycle)
 
+    @_checked
     def get_key(self, path: str) -> Key:
         """Key of the highest cycle of ``dir/.../name``."""
         parts = [s for s in path.split("/") if s]
         return self._find(self.keys("/".join(parts[:-1])), parts[-1])
 
+    @_checked
     def payload(self, key: Key) -> bytes:
         """The record's object bytes, decompressed (ObjLen bytes)."""
         start = key.seek_key + key.keylen
+        if key.seek_key < 0 or key.keylen < 0 or key.nbytes < key.keylen or key.seek_key + key.nbytes > len(self.data):
+            raise RootFormatError(f"{self.path}: record {key.name} lies outside the file")
         raw = self.data[start:key.seek_key + key.nbytes]
-        if key.seek_key + key.nbytes > len(self.data):
-            raise RootFormatError(f"{self.path}: record {key.name} runs past the end of the file")
         if not key.compressed:
             return raw
         out = []
@@ -253,7 +277,7 @@ class RootFile:
         pos = self.begin
         stop = len(self.data)
         while pos + 4 <= stop:
-            (n,) = struct.unpack_from(">i", self.data, pos)
+            (n,) = struct.unpack_from(">i", self.data, pos)  # in range: pos + 4 <= stop
             if n < 0:
                 pos -= n
                 continue
@@ -264,12 +288,14 @@ class RootFile:
             pos += n
 
     # -- objects -------------------------------------------------------------
+    @_checked
     def tree(self, path: str) -> "Tree":
         key = self.get_key(path)
         if key.class_name != "TTree":
             raise RootFormatError(f"{self.path}: {path} is a {key.class_name}, not a TTree")
         return Tree(self, key)
 
+    @_checked
     def graph(self, path: str):
         """(fX, fY, fBits) of a TGraph."""
         key = self.get_key(path)
@@ -296,6 +322,7 @@ class RootFile:
 class Tree:
     """Branch columns of one TTree, gathered from its basket keys."""
 
+    @_checked
     def __init__(self, f: RootFile, key: Key):
         self.file = f
         self.key = key
@@ -336,8 +363,11 @@ class Tree:
             raise RootFormatError(f"{self.file.path}: basket of {b.key.name}: {cnt} offsets for {b.nev_buf} entries")
         offs = np.frombuffer(buf, dtype=">i4", count=b.nev_buf, offset=data_len + 4).astype(np.int64) - kl
         ends = np.append(offs[1:], data_len)
+        if b.nev_buf and (offs[0] < 0 or (ends < offs).any() or ends[-1] > data_len):
+            raise RootFormatError(f"{self.file.path}: basket of {b.key.name}: entry offsets out of order or range")
         return list(zip(offs.tolist(), ends.tolist()))
 
+    @_checked
     def array(self, name: str, dtype) -> np.ndarray:
         """A branch of one fixed-size value per entry (a leaf such as
         ``x/D``, ``x/F``, ``x/I``); ``dtype`` is the value's numpy type,
@@ -355,6 +385,7 @@ class Tree:
             parts.append(np.frombuffer(buf, dtype=dt, count=b.nev_buf))
         return np.concatenate(parts).astype(dt.newbyteorder("="))
 
+    @_checked
     def vectors(self, name: str, dtype=np.float64) -> list[np.ndarray]:
         """A ``std::vector<T>`` branch (entries of varying length): one
         numpy array per entry."""

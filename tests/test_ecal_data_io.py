@@ -198,3 +198,29 @@ def test_oracle_replay_reproduces_fixture(oracle, eio, gold):
         assert oracle.kkt_violation(A, b, gold["kkt_amplitudes"][i]) < 1e-8
     # the reference start reaches the same points on this file
     assert np.array_equal(gold["ref_active_mask"], gold["kkt_active_mask"])
+
+
+@needs_data
+def test_reader_mutated_files_fail_cleanly(rootio):
+    """Random byte changes in the data files: every read either returns or
+    raises RootFormatError / KeyError (a name no longer found)."""
+    rng = np.random.default_rng(3)
+    for path in (SAMPLE_100, SHAPE):
+        orig = bytearray(open(path, "rb").read())
+        for _ in range(300):
+            d = bytearray(orig)
+            for _ in range(int(rng.integers(1, 9))):
+                d[int(rng.integers(len(d)))] = int(rng.integers(256))
+            try:
+                f = rootio.RootFile(bytes(d))
+                list(f.walk())
+                for k in f.keys():
+                    if k.class_name == "TTree":
+                        t = f.tree(k.name)
+                        t.array("amplitudeTruth", np.float64)
+                        t.vectors("samples")
+                    elif k.class_name.startswith("TDirectory"):
+                        f.graph(k.name + "/grPulseShape")
+                        f.tree(k.name + "/Tail").array("timeMin", np.float32)
+            except (rootio.RootFormatError, KeyError):
+                pass
