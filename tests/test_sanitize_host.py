@@ -63,3 +63,71 @@ def test_reader_fuzz_under_sanitizers(exe, which):
     if not os.path.exists(FILES[which]):
         pytest.skip("the reference's data files are absent")
     run(exe, "rootio-fuzz", FILES[which], 800, 17 + which)
+
+
+SAN_DIR = os.path.join(ROOT, "test-regression_gb300", "_build", "asan")
+CSRC = os.path.join(ROOT, "test-regression_gb300", "csrc")
+
+
+def _nvcc():
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    return None
+
+
+@pytest.fixture(scope="module")
+def engine_host_exe():
+    """The engine's sources with host-side sanitizers (device code as PTX
+    only, since no GPU runs it), cached under _build/asan, linked with
+    tests/cpp/sanitize_engine_host.cpp."""
+    import concurrent.futures as cf
+
+    nvcc = _nvcc()
+    if nvcc is None:
+        pytest.skip("nvcc absent")
+    os.makedirs(SAN_DIR, exist_ok=True)
+    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(ROOT, "include", "multifit_gb300.h")]
+    newest = max(os.path.getmtime(d) for d in deps)
+    srcs = sorted(f for f in os.listdir(CSRC) if f.endswith(".cu"))
+
+    def compile_one(src):
+        obj = os.path.join(SAN_DIR, src.replace(".cu", ".o"))
+        if os.path.exists(obj) and os.path.getmtime(obj) >= newest:
+            return obj
+        cmd = [nvcc, "-gencode", "arch=compute_103a,code=compute_103a", "-O1", "-g", "-std=c++17",
+               "-Xcompiler", "-fPIC", "-Xcompiler", "-fsanitize=address", "-Xcompiler", "-fsanitize=undefined",
+               "-Xcompiler", "-fno-sanitize-recover=all", "-Xcompiler", "-fno-omit-frame-pointer",
+               "-I", os.path.join(ROOT, "include"), "-I", CSRC, *(["--fmad=false"] if src == "fit_fp64.cu" else []),
+               "-c", os.path.join(CSRC, src), "-o", obj + ".tmp"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr[-2000:]
+        os.replace(obj + ".tmp", obj)
+        return obj
+
+    with cf.ThreadPoolExecutor(max_workers=len(srcs)) as ex:
+        objs = list(ex.map(compile_one, srcs))
+    exe = os.path.join(SAN_DIR, "sanitize_engine_host")
+    cuda_lib = os.path.join(os.path.dirname(os.path.dirname(nvcc)), "lib64")
+    cmd = ["g++", "-std=c++17", "-O1", "-g", "-fsanitize=address,undefined", "-fno-sanitize-recover=all",
+           "-fno-omit-frame-pointer", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+           os.path.join(ROOT, "tests", "cpp", "sanitize_engine_host.cpp"), *objs, "-L", cuda_lib, "-lcudart",
+           "-lpthread", f"-Wl,-rpath,{cuda_lib}", "-o", exe]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    return exe
+
+
+def test_engine_host_code_under_sanitizers(engine_host_exe, cuda_absent):
+    """Argument checks, the pulse-matrix rule, all 1023 + 255 operator tables,
+    the host generator and the device entry points' error paths (no GPU)."""
+    run(engine_host_exe)
+
+
+@pytest.fixture(scope="module")
+def cuda_absent():
+    # with a GPU present the driver's device entry points would run kernels
+    # from a sanitizer build; this test is for the host paths only
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present: the host-only driver is meant for machines without one")
