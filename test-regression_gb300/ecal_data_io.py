@@ -171,16 +171,21 @@ class ecal_data_io:  # noqa: N801 -- the reference's class name
 
 def h01_summary(d: np.ndarray, lo: float = H01_RANGE[0], hi: float = H01_RANGE[1]) -> dict:
     """Mean, RMS and entry count of (reco - truth) as a fixed-range histogram
-    reports them: fills outside [lo, hi) count as entries but not in the
-    moments; RMS = sqrt(|sum(x^2)/n - mean^2|)."""
+    reports them: each fill inside [lo, hi) adds to the running sums of x and
+    x^2 in fill order (fills outside count as entries only); mean = sum x / n,
+    RMS = sqrt(|sum x^2 / n - mean^2|)."""
     d = np.asarray(d, dtype=np.float64)
-    inr = d[(d >= lo) & (d < hi)]
-    if inr.size == 0:
+    sw = sx = sx2 = 0.0
+    for v in d.tolist():
+        if lo <= v < hi:
+            sw += 1.0
+            sx += v
+            sx2 += v * v
+    if sw == 0:
         return {"mean": 0.0, "rms": 0.0, "entries": int(d.size), "in_range": 0}
-    sw = float(inr.size)
-    mean = float(inr.sum()) / sw
-    rms = math.sqrt(abs(float((inr * inr).sum()) / sw - mean * mean))
-    return {"mean": mean, "rms": rms, "entries": int(d.size), "in_range": int(inr.size)}
+    mean = sx / sw
+    rms = math.sqrt(abs(sx2 / sw - mean * mean))
+    return {"mean": mean, "rms": rms, "entries": int(d.size), "in_range": int(sw)}
 
 
 def replay_arrays(engine, samples: np.ndarray, truth: np.ndarray, fullpulse: np.ndarray, noisecor: np.ndarray,
