@@ -319,6 +319,33 @@ class RootFile:
         return arrays[0], arrays[1], bits
 
 
+    @_checked
+    def th1_stats(self, path: str) -> dict:
+        """Fill statistics of a 1-D histogram (TH1D/TH1F/TH1I): after the
+        class header, TH1's header, TNamed and the three attribute bases come
+        fNcells, the three axes (skipped by their byte counts), fBarOffset,
+        fBarWidth, then fEntries, fTsumw, fTsumw2, fTsumwx, fTsumwx2.
+        Returns those with mean = sumwx / sumw and rms = sqrt(|sumwx2 / sumw -
+        mean^2|), as TH1::GetMean / GetRMS report them."""
+        key = self.get_key(path)
+        if not key.class_name.startswith("TH1"):
+            raise RootFormatError(f"{self.path}: {path} is a {key.class_name}, not a 1-D histogram")
+        buf = self.payload(key)
+        p = 12  # the class's and TH1's byte counts and versions
+        for base in ("TNamed", "TAttLine", "TAttFill", "TAttMarker"):
+            p = _skip_streamed(buf, p, f"{path} {base}")
+        (ncells,) = struct.unpack_from(">i", buf, p)
+        p += 4
+        for axis in ("fXaxis", "fYaxis", "fZaxis"):
+            p = _skip_streamed(buf, p, f"{path} {axis}")
+        p += 4  # fBarOffset, fBarWidth
+        entries, sumw, sumw2, sumwx, sumwx2 = struct.unpack_from(">5d", buf, p)
+        mean = sumwx / sumw if sumw else 0.0
+        rms = float(np.sqrt(abs(sumwx2 / sumw - mean * mean))) if sumw else 0.0
+        return {"ncells": ncells, "entries": entries, "sumw": sumw, "sumw2": sumw2, "sumwx": sumwx,
+                "sumwx2": sumwx2, "mean": mean, "rms": rms}
+
+
 class Tree:
     """Branch columns of one TTree, gathered from its basket keys."""
 

@@ -224,3 +224,30 @@ def test_reader_mutated_files_fail_cleanly(rootio):
                         f.tree(k.name + "/Tail").array("timeMin", np.float32)
             except (rootio.RootFormatError, KeyError):
                 pass
+
+
+OUTPUT_CPU = os.path.join(os.path.dirname(DATA), "analysis", "output_cpu.root")
+
+
+@pytest.mark.skipif(not os.path.exists(OUTPUT_CPU), reason="the reference's analysis output is absent")
+def test_reader_reference_output_histograms(rootio):
+    """The reference's own multifit_cpu output (analysis/output_cpu.root): its
+    Duration histogram holds the 10 batch times of the 65,536-channel run
+    whose mean, 277.7 ms, is the last entry of analysis/cpu_i7-4770K_gpu_V100/
+    multifit_cpu.csv; h01 (reco - true in-time amplitude) and reco_ampl were
+    filled once per channel and iteration. Its input (a -13 ns shifted sample
+    file) is not in the reference tree, so the physics numbers are recorded,
+    not replayed."""
+    f = rootio.RootFile(OUTPUT_CPU)
+    assert {k.name for k in f.keys()} == {"RecoAndSim", "h01", "reco_ampl", "Duration"}
+    dur = f.th1_stats("Duration")
+    assert dur["entries"] == 10 and dur["ncells"] == 102
+    assert round(dur["mean"], 6) == 277.7
+    h = f.th1_stats("h01")
+    assert h["entries"] == 655_360 == 10 * 65_536 and h["ncells"] == 1002
+    reco = f.th1_stats("reco_ampl")
+    assert reco["entries"] == h["entries"]
+    # reco = truth + dA with truth = 10 GeV for every channel: the moments agree
+    assert abs(reco["mean"] - 10.0 - h["mean"]) < 1e-9 and abs(reco["rms"] - h["rms"]) < 1e-8
+    assert abs(h["mean"]) < 0.01 and 0.02 < h["rms"] < 0.04
+    assert f.tree("RecoAndSim").entries == 0  # the tree record holds no entries
