@@ -1,6 +1,8 @@
 """Helpers shared by the GPU tests: device buffers (torch as plumbing),
 synthetic workloads generated on the device, and the oracle run on the same
 bytes."""
+import os
+
 import numpy as np
 
 FIELDS = ("amplitudes", "chi2", "intime", "errors", "active_mask", "status", "iters")
@@ -95,3 +97,19 @@ def assert_bitwise(gpu, ref, fields=("amplitudes", "chi2", "active_mask", "statu
         g = gpu["iters"] if sel is None else gpu["iters"][sel]
         r = pack_iters(ref["iters"] if sel is None else ref["iters"][sel])
         assert np.array_equal(g, r), "iteration counters differ"
+
+
+def reference_data_dir():
+    """The reference tree's data/ directory (the tree the oracle recipe
+    compiles from), for the CPU tests of the data-file readers; they skip
+    where it is absent."""
+    from oracle import build_oracle
+
+    return os.path.join(build_oracle.REFERENCE_ROOT, "data")
+
+
+def replay_data_dir():
+    """A directory holding the reference's data files for the GPU replay
+    tests, only when the user names one in MULTIFIT_REPLAY_DATA (the GPU
+    tests read no default location); None otherwise."""
+    return os.environ.get("MULTIFIT_REPLAY_DATA") or None

@@ -40,8 +40,9 @@ spec.loader.exec_module(mf)
 import multifit_gb300.ecal_data_io as eio  # noqa: E402
 import multifit_gb300.rootio as rootio  # noqa: E402
 
-REFERENCE_ROOT = os.environ.get("MULTIFIT_REFERENCE_ROOT", "/root/reference")
-DATA = os.path.join(REFERENCE_ROOT, "data")
+from oracle import build_oracle  # noqa: E402
+
+DATA = os.path.join(build_oracle.REFERENCE_ROOT, "data")
 SAMPLE_FILE = "mysample_100_0.000_0.000_10_25.00_10.00_0.00_1.000_1.00_CRRC43_0.00_slew_1.00.root"
 SHAPE_FILE = "EmptyFile.root"
 OUT = os.path.join(HERE, "replay_mysample_100.npz")

@@ -11,8 +11,10 @@ import struct
 import numpy as np
 import pytest
 
+from _helpers import reference_data_dir
+
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "replay_mysample_100.npz")
-DATA = os.path.join(os.environ.get("MULTIFIT_REFERENCE_ROOT", "/root/reference"), "data")
+DATA = reference_data_dir()
 SAMPLE_100 = os.path.join(DATA, "mysample_100_0.000_0.000_10_25.00_10.00_0.00_1.000_1.00_CRRC43_0.00_slew_1.00.root")
 SAMPLE_1000 = os.path.join(DATA,
                            "mysample_1000_0.000_0.000_10_25.00_10.00_0.00_1.000_1.00_CRRC43_0.00_slew_1.00.root")

@@ -1,18 +1,20 @@
 """The reference driver's run() in C++ against the engine
 (tests/cpp/replay_driver.cpp: include/multifit_gb300_io.hpp reads the data
 files, mfgb::PulseChiSqSNNLS / mfgb::BatchFitter fit them). It compiles and
-links here; on a GPU with the reference's data files present it reproduces
-the oracle's fits and physics check of tests/golden/replay_mysample_100.npz
-bit for bit."""
+links here; on a GPU, with MULTIFIT_REPLAY_DATA naming a directory that holds
+the reference's two data files, it reproduces the oracle's fits and physics
+check of tests/golden/replay_mysample_100.npz bit for bit."""
 import os
 import subprocess
 
 import numpy as np
 import pytest
 
+from _helpers import replay_data_dir
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(ROOT, "tests", "golden", "replay_mysample_100.npz")
-DATA = os.path.join(os.environ.get("MULTIFIT_REFERENCE_ROOT", "/root/reference"), "data")
+DATA = replay_data_dir() or ""
 SAMPLE_100 = os.path.join(DATA, "mysample_100_0.000_0.000_10_25.00_10.00_0.00_1.000_1.00_CRRC43_0.00_slew_1.00.root")
 SHAPE = os.path.join(DATA, "EmptyFile.root")
 
@@ -39,8 +41,8 @@ def test_replay_driver_compiles_and_links(mf, tmp_path, extra):
 @pytest.mark.gpu
 @pytest.mark.parametrize("batch", [0, 1])
 def test_replay_driver_reproduces_oracle(mf, cuda, tmp_path, batch):
-    if not (os.path.exists(SAMPLE_100) and os.path.exists(SHAPE)):
-        pytest.skip("the reference's data files are absent")
+    if not (DATA and os.path.exists(SAMPLE_100) and os.path.exists(SHAPE)):
+        pytest.skip("MULTIFIT_REPLAY_DATA does not name a directory with the reference's data files")
     g = dict(np.load(GOLDEN))
     exe = build(mf, tmp_path)
     r = subprocess.run([exe, SAMPLE_100, SHAPE, "0", str(batch)], capture_output=True, text=True, timeout=300)

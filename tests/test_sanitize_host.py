@@ -13,8 +13,10 @@ import zlib
 import numpy as np
 import pytest
 
+from _helpers import reference_data_dir
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-DATA = os.path.join(os.environ.get("MULTIFIT_REFERENCE_ROOT", "/root/reference"), "data")
+DATA = reference_data_dir()
 FILES = [os.path.join(DATA, "mysample_100_0.000_0.000_10_25.00_10.00_0.00_1.000_1.00_CRRC43_0.00_slew_1.00.root"),
          os.path.join(DATA, "EmptyFile.root")]
 ENV = dict(os.environ, ASAN_OPTIONS="detect_leaks=1:abort_on_error=1", UBSAN_OPTIONS="print_stacktrace=1")
