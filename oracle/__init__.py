@@ -10,7 +10,6 @@ checker or the timed CPU baseline -- never on the engine's path.
 from __future__ import annotations
 
 import ctypes as C
-import os
 
 import numpy as np
 
