@@ -193,7 +193,8 @@ def replay_arrays(engine, samples: np.ndarray, truth: np.ndarray, fullpulse: np.
     """The driver's fit loop and physics check on channels already read:
     samples (n, 10), true in-time amplitudes (n,), the driver's fullpulse (19,)
     and noise correlation (10, 10). Fits on the GPU (the engine's FP64 form
-    unless ``options`` says otherwise; error calculation off)."""
+    unless ``options`` says otherwise; error calculation off). Replaces the
+    engine's condition set 0 with the driver's."""
     mf = sys.modules[__package__]
     samples = np.ascontiguousarray(samples, dtype=np.float64)
     n = samples.shape[0]

@@ -130,7 +130,8 @@ def _skip_named_and_attributes(buf, what: str):
 
 
 class RootFile:
-    """Read-only view of a ROOT file held in memory."""
+    """Read-only view of a ROOT file, read whole into memory (the multifit
+    data files are a few MB)."""
 
     @_checked
     def __init__(self, source):
