@@ -253,3 +253,33 @@ def test_reader_reference_output_histograms(rootio):
     assert abs(reco["mean"] - 10.0 - h["mean"]) < 1e-9 and abs(reco["rms"] - h["rms"]) < 1e-8
     assert abs(h["mean"]) < 0.01 and 0.02 < h["rms"] < 0.04
     assert f.tree("RecoAndSim").entries == 0  # the tree record holds no entries
+
+
+def test_reader_compressed_record_blocks(rootio):
+    """A record split into several compressed blocks, zlib and LZMA (each block:
+    2-letter algorithm, method byte, 3-byte little-endian compressed and
+    uncompressed sizes, then the stream), inflated back to its ObjLen bytes."""
+    import lzma
+    import zlib
+
+    rng = np.random.default_rng(4)
+    parts = [np.cumsum(rng.standard_normal(3000)).astype(">f8").tobytes(), b"multifit" * 700, bytes(5000)]
+
+    def block(alg, raw):
+        z = zlib.compress(raw, 6) if alg == b"ZL" else lzma.compress(raw, format=lzma.FORMAT_XZ)
+        return alg + b"\x08" + len(z).to_bytes(3, "little") + len(raw).to_bytes(3, "little") + z
+
+    body = block(b"ZL", parts[0]) + block(b"XZ", parts[1]) + block(b"ZL", parts[2])
+    keylen = 40
+    data = bytes(keylen) + body
+    rf = rootio.RootFile.__new__(rootio.RootFile)
+    rf.path, rf.data = "<blocks>", data
+    objlen = sum(len(p) for p in parts)
+    key = rootio.Key(0, len(data), 4, objlen, keylen, 1, 0, 0, "TBasket", "b", "t", keylen)
+    assert rf.payload(key) == b"".join(parts)
+    bad = rootio.Key(0, len(data), 4, objlen + 1, keylen, 1, 0, 0, "TBasket", "b", "t", keylen)
+    with pytest.raises(rootio.RootFormatError):
+        rf.payload(bad)
+    rf.data = bytes(keylen) + b"L4" + body[2:]
+    with pytest.raises(rootio.RootFormatError, match="not supported"):
+        rf.payload(key)
