@@ -186,7 +186,8 @@ int mf_fit_count_flops(mf_context* ctx, const mf_batch* batch, const mf_options*
  *  - n > MF_NOALLOC_MAX_CHANNELS: MF_EINVAL, mf_last_error says why.
  *  - The context's device must be current. The first call on a device
  *    resolves the scratch address (cudaGetSymbolAddress): make it before any
- *    stream capture on that device begins.
+ *    stream capture on that device begins. The address is kept for the life
+ *    of the process: do not cudaDeviceReset a device between calls.
  *  - One scratch per device: calls that overlap on a device (other streams,
  *    threads or contexts) race on it; serialise them.
  *  - The only scratch words that must start at zero (the two queue counters)

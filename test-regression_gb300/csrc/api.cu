@@ -1079,7 +1079,8 @@ unsigned char* g_noalloc_ptr[kMaxDevices] = {};
 
 // Address of this device's scratch, resolved once per device (the device must
 // be current). The first call on a device resolves it; make that call before
-// any stream capture on the device begins.
+// any stream capture on the device begins. The address is cached for the
+// process: a cudaDeviceReset between calls would leave it stale.
 int noalloc_scratch(int device, unsigned char** out) {
   if (device < 0 || device >= kMaxDevices) return MF_EINVAL;
   std::lock_guard<std::mutex> g(g_noalloc_mu);
