@@ -14,6 +14,10 @@
 //   rootio_check expect-error <file> <tree> <branch> <substring>
 //       reading the branch must throw a FormatError whose message contains the
 //       substring.
+//   rootio_check branches <file> <out.bin>
+//       the Samples tree's amplitudeTruth and samples branches: writes
+//       i64 entries, entries f64 truth values, then per entry i64 length and
+//       that many f64 samples; or exits 3 with the FormatError message.
 //   rootio_check patch-compression <file> <branch>
 //       the branch's first basket with its "ZL" block tag changed to "L4" must
 //       be refused.
@@ -97,6 +101,27 @@ int expect_error(const char* path, const char* tree, const char* branch, const c
   return 1;
 }
 
+int branches(const char* path, const char* out_path) {
+  try {
+    const mfgb::rootio::RootFile f(path);
+    const mfgb::rootio::Tree t = f.tree("Samples");
+    const std::vector<double> truth = t.array<double>("amplitudeTruth");
+    const std::vector<std::vector<double>> vecs = t.vectors<double>("samples");
+    std::ofstream o(out_path, std::ios::binary);
+    put(o, int64_t(truth.size()));
+    for (double v : truth) put(o, v);
+    put(o, int64_t(vecs.size()));
+    for (const auto& v : vecs) {
+      put(o, int64_t(v.size()));
+      for (double x : v) put(o, x);
+    }
+  } catch (const mfgb::rootio::FormatError& e) {
+    std::printf("error: %s\n", e.what());
+    return 3;
+  }
+  return 0;
+}
+
 int patch_compression(const char* path, const char* branch) {
   std::vector<uint8_t> d = read_all(path);
   const mfgb::rootio::RootFile f(d, path);
@@ -128,10 +153,11 @@ int main(int argc, char** argv) {
     if (mode == "dump" && argc == 5) return dump(argv[2], argv[3], argv[4]);
     if (mode == "expect-error" && argc == 6) return expect_error(argv[2], argv[3], argv[4], argv[5]);
     if (mode == "patch-compression" && argc == 4) return patch_compression(argv[2], argv[3]);
+    if (mode == "branches" && argc == 4) return branches(argv[2], argv[3]);
   } catch (const std::exception& e) {
     std::printf("exception: %s\n", e.what());
     return 2;
   }
-  std::fprintf(stderr, "usage: rootio_check inflate|dump|expect-error|patch-compression ...\n");
+  std::fprintf(stderr, "usage: rootio_check inflate|dump|expect-error|patch-compression|branches ...\n");
   return 2;
 }
