@@ -411,6 +411,21 @@ def run_ours(args, world, rank, local):
         bms = max_over_ranks(sum(bts) / len(bts), world, device=dev)
         baseline = {"form": "plain-fp64 drop-in (reference start, max_iter 10)", "value": n * world / (bms * 1e-3),
                     "ms_per_step": bms, "speedup_of_form": (n * world / (step_ms_max * 1e-3)) / (n * world / (bms * 1e-3))}
+        # the form against multifit_cpu's own result: `amp` now holds the plain FP64
+        # fit with multifit_cpu's settings (reference start, max_iter 10)
+        torch.cuda.synchronize()
+        err_c = (form_amp - amp).abs().amax(dim=1) / amp.abs().amax(dim=1).clamp_min(1e-300)
+        d_chi2 = (chi2 - form_chi2) / form_chi2.abs().clamp_min(1.0)
+        vs_cpu = {"reference": "plain FP64 GPU kernel with multifit_cpu's settings (reference start, max_iter 10; "
+                               "bit-identical to the oracle)",
+                  "channels": n,
+                  "frac_within_1e-5": float((err_c <= 1e-5).double().mean().item()),
+                  "frac_within_1e-4": float((err_c <= 1e-4).double().mean().item()),
+                  "support_identical_frac": float((form_mask == mask).double().mean().item()),
+                  "chi2_multifit_cpu_above_frac": float((d_chi2 > 1e-9).double().mean().item()),
+                  "chi2_multifit_cpu_below_frac": float((d_chi2 < -1e-9).double().mean().item()),
+                  "chi2_note": "(chi2_cpu - chi2_form) / max(chi2_form, 1) beyond +-1e-9: where multifit_cpu's "
+                               "chi2 is above, it stopped short of the NNLS optimum the form returns"}
         # accuracy of the form against the plain FP64 kernel run to KKT convergence, whole batch on the GPU
         eng.fit_device(batch, mf.default_options(max_iter_nnls=1000, nnls_start=mf.START_SUPPORT),
                        stream.cuda_stream)
@@ -427,7 +442,8 @@ def run_ours(args, world, rank, local):
                     "chi2_rel_err_median": float(chi2_err.median().item()) if chi2_err.numel() else None,
                     "chi2_rel_err_max": float(chi2_err.max().item()) if chi2_err.numel() else None,
                     "chi2_note": "|chi2 - chi2_ref| / max(chi2_ref, 1) on channels whose active sets agree",
-                    "active_set_identical_frac": float(same.double().mean().item())}
+                    "active_set_identical_frac": float(same.double().mean().item()),
+                    "vs_multifit_cpu": vs_cpu}
         amp.copy_(form_amp)
         mask.copy_(form_mask)
         chi2.copy_(form_chi2)
@@ -502,6 +518,7 @@ def run_ours(args, world, rank, local):
     # that waited on someone else's host-memory traffic says nothing of the engine
     e2e_sorted = sorted(e2e_times)
     e2e_s = max_over_ranks(e2e_sorted[len(e2e_sorted) // 2], world, device=dev)
+    e2e_mean_s = max_over_ranks(sum(e2e_times) / len(e2e_times), world, device=dev)
     h2d = n * (10 * 8 + 8 + (1 if mixed else 0))
     d2h = n * (10 * 8 + 8 + 8 + 2 + 1)
 
@@ -520,7 +537,7 @@ def run_ours(args, world, rank, local):
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
-            cpu = cpu_baseline(mf, args, p, budget_s=args.cpu_seconds)
+            cpu = cpu_baseline(args, wl, n, budget_s=args.cpu_seconds)
         out = {
             "metric": METRIC,
             "value": value,
@@ -535,15 +552,11 @@ def run_ours(args, world, rank, local):
             "dtype": {"fp64": "f64", "mixed": "f32+f64", "fp32": "f32 (double-float judge; f64 repair)",
                       "warm": "f32 (double-float judge; f64 repair; bf16 MLP)"}[args.form],
             "data": "synthetic (seeded Philox generator; the workload's shapes and value distributions)",
-            "config": {
-                "workload": wl,
-                "description": WORKLOAD_DESC.get(wl, wl),
-                "channels_per_gpu": n,
+            "config": workload_config(args, wl, n, world),
+            "engine": {
                 "form": FORM_DESC[args.form],
                 "max_iter_nnls": opt.max_iter_nnls,
                 "nnls_start": ["reference", "support"][opt.nnls_start] if args.form == "fp64" else "KKT-converged",
-                "l2": "flushed between steps (256 MB write)",
-                "parallelism": f"replicas x{world}",
                 "schedule": ["grid", "persistent work-stealing"][opt.schedule],
                 "launch_shape": {"block_size": opt.block_size or "tuned/default",
                                  "channels_per_warp": opt.channels_per_warp or "tuned/default"},
@@ -554,6 +567,7 @@ def run_ours(args, world, rank, local):
             "e2e": {"value": n * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "entry": "mf_fit_host (pinned host buffers, pipelined copies)",
                     "statistic": "median step wall time",
+                    "value_mean": n * world / e2e_mean_s, "ms_mean": e2e_mean_s * 1e3,
                     "step_ms": {"median": e2e_s * 1e3, "min": e2e_sorted[0] * 1e3, "max": e2e_sorted[-1] * 1e3,
                                 "mean": sum(e2e_times) / len(e2e_times) * 1e3}},
             "roofline": roof,
@@ -649,79 +663,137 @@ def kernel_rooflines(mf, eng, kernels, args, n, ctype, plain_flops, form_fp64_fl
     return out
 
 
-def cpu_baseline(mf, args, p, budget_s: float = 3.0):
-    """The oracle (a port of the reference's CPU path) on the host cores over a
-    bounded sample of the same workload."""
-    sys.path.insert(0, ROOT)
-    import numpy as np
+def reference_fit_setting(args):
+    """(max_iter_nnls, nnls start, label) of the fit both arms compute: the
+    warm/mixed/FP32 forms return each channel's NNLS optimum (KKT point), which
+    the reference path reaches with max_iter 1000 and the support start; the
+    FP64 form is timed with the settings given on the command line."""
+    if args.form == "fp64":
+        return args.max_iter, args.start, ("multifit_cpu literal (reference start, max_iter %d)" % args.max_iter
+                                           if args.start == 0 else "support start, max_iter %d" % args.max_iter)
+    return 1000, 1, "NNLS to KKT convergence (support start, max_iter 1000)"
 
-    import oracle
 
-    nt = oracle.hardware_threads()
-    ecal, _ = mf.synth_conditions(mf.SYNTH_ECAL)
-    P, R, bxs, _ = mf.conditions_arrays(ecal)
-    m = 20_000
-    d = mf.synth_generate_host(p, 0, m, with_truth=False)
-    t0 = time.perf_counter()
-    oracle.fit_batch(d["samples"], d["pederr"], P, R, bxs, max_iter_nnls=args.max_iter, start=args.start,
-                     nthreads=nt)
-    dt = time.perf_counter() - t0
-    rate = m / dt
-    m2 = int(min(p.n, max(m, rate * budget_s)))
-    if m2 > m:
-        d = mf.synth_generate_host(p, 0, m2, with_truth=False)
+def workload_config(args, wl: str, n: int, world: int) -> dict:
+    """The `config` both arms print: the workload and the fit it asks for,
+    nothing that depends on which arm runs it."""
+    _, _, fit = reference_fit_setting(args)
+    return {"workload": wl, "description": WORKLOAD_DESC.get(wl, wl), "channels_per_step": n, "fit": fit,
+            "l2": "inputs (88 B/channel) exceed every cache; the GPU arm also flushes its L2 between steps "
+                  "(256 MB write)",
+            "parallelism": f"replicas x{world}"}
+
+
+class CpuReference:
+    """The reference's CPU path on this host: the oracle restatement of
+    multifit_cpu's fit (oracle/, C++), fed by the oracle's own seeded
+    generator. Loads nothing of the engine."""
+
+    def __init__(self, wl: str, n: int):
+        sys.path.insert(0, ROOT)
+        import numpy as np
+
+        import oracle
+
+        self.oracle, self.np = oracle, np
+        self.nt = oracle.hardware_threads()
+        self.wl, self.n = wl, n
+        sets = [0, 1] if oracle.WORKLOADS[wl].get("hcal_fraction", 0.0) > 0 else [0]
+        self.conds = {t: oracle.synth_conditions(t) for t in sets}
+        d = oracle.synth_generate(wl, 0, n)
+        # channels of each condition set in contiguous arrays (the fits are per set)
+        self.parts = {}
+        for t in sets:
+            sel = np.nonzero(d["ctype"] == t)[0]
+            self.parts[t] = (np.ascontiguousarray(d["samples"][sel]), np.ascontiguousarray(d["pederr"][sel]))
+
+    def fit(self, max_iter: int, start: int, nthreads: int = 0, m: int | None = None) -> float:
+        """Fits the first m channels of every set; returns the wall seconds."""
         t0 = time.perf_counter()
-        oracle.fit_batch(d["samples"], d["pederr"], P, R, bxs, max_iter_nnls=args.max_iter, start=args.start,
-                         nthreads=nt)
-        dt = time.perf_counter() - t0
-        m = m2
-        rate = m / dt
-    return {"value": rate, "unit": UNIT, "cores": nt, "kind": "port",
-            "sample": f"first {m} channels of the workload, ECAL set, all {nt} host threads, {dt:.2f} s"}
+        for t, (s, pe) in self.parts.items():
+            k = s.shape[0] if m is None else min(s.shape[0], m)
+            if k == 0:
+                continue
+            P, R, bxs, _ = self.conds[t]
+            self.oracle.fit_batch(s[:k], pe[:k], P, R, bxs, max_iter_nnls=max_iter, start=start,
+                                  nthreads=nthreads or self.nt)
+        return time.perf_counter() - t0
+
+    def channels(self, m: int | None) -> int:
+        return sum(s.shape[0] if m is None else min(s.shape[0], m) for s, _ in self.parts.values())
+
+    def rate(self, max_iter: int, start: int, nthreads: int, budget_s: float, cap: int | None = None) -> dict:
+        """Channels/s on a sample sized to about budget_s of work (a probe of
+        2,000 channels per thread first)."""
+        probe = min(self.n, 2000 * nthreads)
+        dt = self.fit(max_iter, start, nthreads, probe)
+        per = dt / max(self.channels(probe), 1)
+        m = int(min(self.n, cap or self.n, max(probe, budget_s / max(per, 1e-12))))
+        dt = self.fit(max_iter, start, nthreads, m)
+        c = self.channels(m)
+        return {"value": c / dt, "unit": UNIT, "threads": nthreads, "channels": c, "seconds": dt}
+
+
+def cpu_baseline(args, wl: str, n: int, budget_s: float = 10.0) -> dict:
+    """The reference's CPU path (oracle port) on the host cores over a bounded
+    sample of the same workload: all threads and one thread (the reference
+    driver's own setting, multifit_cpu/src/multifit.cpp:196-227), for the fit
+    the timed form computes and for multifit_cpu's literal settings."""
+    mi, st, fit = reference_fit_setting(args)
+    ref = CpuReference(wl, min(n, 2_000_000))
+    allt = ref.rate(mi, st, ref.nt, budget_s * 0.4)
+    one = ref.rate(mi, st, 1, budget_s * 0.2)
+    lit_all = ref.rate(10, 0, ref.nt, budget_s * 0.25)
+    lit_one = ref.rate(10, 0, 1, budget_s * 0.15)
+    return {"value": allt["value"], "unit": UNIT, "cores": ref.nt, "kind": "port",
+            "sample": f"first {allt['channels']} channels of {wl}, {fit}, all {ref.nt} host threads, "
+                      f"{allt['seconds']:.2f} s",
+            "one_thread": one,
+            "multifit_cpu_settings": {"fit": "reference start, max_iter 10", "all_threads": lit_all,
+                                      "one_thread": lit_one}}
 
 
 def run_reference(args, world, rank):
+    """The reference arm: the reference's CPU implementation of the path (the
+    oracle port; the reference itself needs Eigen, absent here) on all host
+    threads, over the same workload, channel count and fit as the GPU arm,
+    with inputs from the oracle's own generator. Nothing of the engine is
+    loaded. Rank 0 alone runs it."""
     if rank != 0:
         return None
-    build_pkg()
-    mf = load_pkg()
+    wl = args.workload or ("ecal-1m-pu2" if args.form == "fp64" else "warm-eval-10m")
     sys.path.insert(0, ROOT)
     import oracle
 
-    nt = oracle.hardware_threads()
-    args.workload = args.workload or ("ecal-1m-pu2" if args.form == "fp64" else "warm-eval-10m")
-    p = mf.WORKLOADS[args.workload]()
-    mixed = p.hcal_fraction > 0
-    conds = {0: mf.synth_conditions(mf.SYNTH_ECAL)[0]}
-    if mixed:
-        conds[1] = mf.synth_conditions(mf.SYNTH_HCAL)[0]
-    # size one step to about args.cpu_seconds of work on all cores
-    probe = 20_000
-    d = mf.synth_generate_host(p, 0, probe, with_truth=False)
-
-    def fit(d):
-        for t, c in conds.items():
-            sel = d["ctype"] == t
-            if not sel.any():
-                continue
-            P, R, bxs, _ = mf.conditions_arrays(c)
-            oracle.fit_batch(d["samples"][sel], d["pederr"][sel], P, R, bxs, max_iter_nnls=args.max_iter,
-                             start=args.start, nthreads=nt)
-
-    t0 = time.perf_counter()
-    fit(d)
-    rate = probe / (time.perf_counter() - t0)
-    per_step_s = min(args.cpu_seconds, 120.0 / (args.steps + args.warmup))
-    m = int(min(p.n, max(probe, rate * per_step_s)))
-    d = mf.synth_generate_host(p, 0, m, with_truth=False)
+    n = int(getattr(args, "channels", 0) or oracle.WORKLOADS[wl]["n"])
+    mi, st, fit = reference_fit_setting(args)
+    ref = CpuReference(wl, n)
+    # a step fits every channel unless that would take longer than the step cap:
+    # then the first m channels of each set, stated in the line
+    probe_dt = ref.fit(mi, st, ref.nt, min(n, 20_000))
+    est = probe_dt / max(ref.channels(min(n, 20_000)), 1) * ref.channels(None)
+    cap_s = getattr(args, "ref_step_cap_s", 8.0)
+    m = None if est <= cap_s else max(1000, int(n * cap_s / est))
     for _ in range(args.warmup):
-        fit(d)
+        ref.fit(mi, st, ref.nt, m)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        fit(d)
+        ref.fit(mi, st, ref.nt, m)
     dt = (time.perf_counter() - t0) / args.steps
-    value = m / dt
-    sample = f"first {m} channels of {args.workload} per step, all {nt} host threads"
+    c = ref.channels(m)
+    value = c / dt
+    sample = (f"all {c} channels of {wl} per step" if m is None else f"first {c} of {n} channels of {wl} per step")
+    sample += f", {fit}, all {ref.nt} host threads"
+    # multifit_cpu's literal settings on the same channels, and one thread
+    lit_steps = max(1, min(3, args.steps))
+    t0 = time.perf_counter()
+    for _ in range(lit_steps):
+        ref.fit(10, 0, ref.nt, m)
+    lit = {"fit": "multifit_cpu literal (reference start, max_iter 10)", "value": c * lit_steps /
+           (time.perf_counter() - t0), "unit": UNIT, "threads": ref.nt, "channels": c, "steps": lit_steps}
+    budget = getattr(args, "cpu_seconds", 10.0)
+    one = ref.rate(mi, st, 1, budget * 0.5, cap=n)
+    lit_one = ref.rate(10, 0, 1, budget * 0.5, cap=n)
     out = {
         "impl": "reference",
         "metric": METRIC,
@@ -736,10 +808,13 @@ def run_reference(args, world, rank):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded Philox generator; the workload's shapes and value distributions)",
-        "config": {"workload": args.workload, "description": WORKLOAD_DESC.get(args.workload, args.workload),
-                   "form": "reference multifit_cpu path (oracle port: Eigen absent, reference not buildable)",
-                   "max_iter_nnls": args.max_iter, "nnls_start": ["reference", "support"][args.start]},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nt, "kind": "port", "sample": sample},
+        "config": workload_config(args, wl, n, world),
+        "implementation": {"path": "the reference's multifit_cpu fit, restated in C++ (oracle/; the reference "
+                                   "needs Eigen, absent here)",
+                           "generator": "oracle/synth_oracle.cpp (the engine library is not loaded)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": ref.nt, "kind": "port", "sample": sample,
+                         "one_thread": one,
+                         "multifit_cpu_settings": {"all_threads": lit, "one_thread": lit_one}},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out), flush=True)
@@ -765,7 +840,9 @@ def main(argv=None):
     ap.add_argument("--max-iter", type=int, default=10)
     ap.add_argument("--start", type=int, default=0, choices=[0, 1])
     ap.add_argument("--cpu-seconds", type=float, default=10.0,
-                    help="CPU work of the cpu_baseline sample; the reference arm's steps share ~2 minutes")
+                    help="CPU work of the cpu_baseline sample and of the reference arm's one-thread legs")
+    ap.add_argument("--ref-step-cap-s", type=float, default=8.0,
+                    help="reference arm: a step fits every channel unless that takes longer than this")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-parity", action="store_true")
     args = ap.parse_args(argv)

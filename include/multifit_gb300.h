@@ -121,7 +121,8 @@ typedef struct mf_options {
   int32_t schedule;       /* enum mf_schedule */
   int32_t warm_start;     /* enum mf_warm */
   int32_t compute_errors; /* 1: MINOS-like in-time uncertainty (DoFit, PulseChiSqSNNLS.cpp:75-146) */
-  int32_t block_size;     /* threads per block; 0 = tuned default */
+  int32_t block_size;     /* threads per block, a multiple of 32; grid schedule at most 128, persistent
+                             at most 512 (MF_EINVAL beyond); 0 = tuned default */
   int32_t blocks_per_sm;  /* persistent schedule: cap on resident blocks per SM; 0 = the occupancy limit */
   int32_t channels_per_warp; /* persistent schedule, FP32 search: 1, 2, 4, 8 or 32 channels per warp
                                 (32 / that many lanes per channel); 0 = tuned (mf_autotune) or 32 */

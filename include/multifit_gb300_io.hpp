@@ -142,10 +142,14 @@ constexpr uint8_t kDistExtra[30] = {0, 0, 0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 6,
 // RFC 1951 3.2.7: order in which the code-length code lengths are sent
 constexpr uint8_t kClOrder[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
 
-inline void inflate_block(BitReader& br, const Huffman& lit, const Huffman& dist, std::vector<uint8_t>& out) {
+// Output beyond `limit` bytes (the block's declared inflated size) is an
+// error at once, so a damaged stream cannot grow memory past what it declares.
+inline void inflate_block(BitReader& br, const Huffman& lit, const Huffman& dist, std::vector<uint8_t>& out,
+                          size_t limit) {
   for (;;) {
     const int sym = lit.decode(br);
     if (sym < 256) {
+      if (out.size() >= limit) throw FormatError("zlib: output exceeds the declared size");
       out.push_back(uint8_t(sym));
     } else if (sym == 256) {
       return;
@@ -157,6 +161,7 @@ inline void inflate_block(BitReader& br, const Huffman& lit, const Huffman& dist
       if (di >= 30) throw FormatError("zlib: invalid distance code");
       const size_t d = kDistBase[di] + br.bits(kDistExtra[di]);
       if (d > out.size()) throw FormatError("zlib: distance before the start of the data");
+      if (len > limit - out.size()) throw FormatError("zlib: output exceeds the declared size");
       const size_t from = out.size() - d;
       for (size_t i = 0; i < len; ++i) {  // byte by byte: the copy may overlap its own output
         const uint8_t c = out[from + i];
@@ -166,7 +171,8 @@ inline void inflate_block(BitReader& br, const Huffman& lit, const Huffman& dist
   }
 }
 
-/* Inflates one zlib stream (2-byte header, DEFLATE blocks, Adler-32). */
+/* Inflates one zlib stream (2-byte header, DEFLATE blocks, Adler-32) whose
+ * inflated size is at most `expected` bytes (FormatError beyond). */
 inline std::vector<uint8_t> zlib_inflate(const uint8_t* p, size_t n, size_t expected) {
   if (n < 6) throw FormatError("zlib: stream too short");
   const unsigned cmf = p[0], flg = p[1];
@@ -194,9 +200,10 @@ inline std::vector<uint8_t> zlib_inflate(const uint8_t* p, size_t n, size_t expe
       const unsigned len = br.byte() | (unsigned(br.byte()) << 8);
       const unsigned nlen = br.byte() | (unsigned(br.byte()) << 8);
       if ((len ^ 0xffffu) != nlen) throw FormatError("zlib: stored block length check failed");
+      if (len > expected - out.size()) throw FormatError("zlib: output exceeds the declared size");
       for (unsigned i = 0; i < len; ++i) out.push_back(br.byte());
     } else if (type == 1) {
-      inflate_block(br, fixed_lit, fixed_dist, out);
+      inflate_block(br, fixed_lit, fixed_dist, out, expected);
     } else if (type == 2) {
       const int hlit = int(br.bits(5)) + 257, hdist = int(br.bits(5)) + 1, hclen = int(br.bits(4)) + 4;
       if (hlit > 286 || hdist > 30) throw FormatError("zlib: bad dynamic block counts");
@@ -230,7 +237,7 @@ inline std::vector<uint8_t> zlib_inflate(const uint8_t* p, size_t n, size_t expe
       Huffman lit, dist;
       lit.build(lens, hlit);
       dist.build(lens + hlit, hdist);
-      inflate_block(br, lit, dist, out);
+      inflate_block(br, lit, dist, out, expected);
     } else {
       throw FormatError("zlib: reserved block type");
     }

@@ -47,6 +47,13 @@ def _bind(L):
     L.oracle_nnls_lawson_hanson.restype = C.c_int
     L.oracle_nnls_lawson_hanson.argtypes = [dp, dp, C.c_int, C.c_int, dp, C.c_int]
     L.oracle_hardware_threads.restype = C.c_int
+    L.oracle_synth_conditions.restype = C.c_int
+    L.oracle_synth_conditions.argtypes = [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_void_p, C.c_void_p,
+                                          C.c_void_p, C.POINTER(C.c_double)]
+    L.oracle_synth_generate.restype = C.c_int
+    L.oracle_synth_generate.argtypes = [C.c_uint64, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                        C.c_double, C.c_int64, C.c_int64, C.c_int, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_void_p, C.c_int, C.c_int]
     return L
 
 
@@ -174,6 +181,57 @@ def fit_batch(samples: np.ndarray, pederr: np.ndarray, P: np.ndarray, R: np.ndar
     if rc != 0:
         raise ValueError(f"oracle_fit_batch rc={rc}")
     return out
+
+
+# Seeded synthetic workloads (the benchmark configurations): seed, channels,
+# in-time amplitude law and range, pileup mean per out-of-time BX (negative:
+# drawn per channel uniform in [0, -mean]), hit energy mean, HCAL fraction.
+SYNTH_ECAL, SYNTH_HCAL = 0, 1
+WORKLOADS = {
+    "ecal-10k-pu0.5": dict(seed=1, n=10_000, intime_log=False, lo=1.0, hi=100.0, pileup_mean=0.5),
+    "ecal-1m-pu2": dict(seed=2, n=1_000_000, intime_log=False, lo=1.0, hi=100.0, pileup_mean=2.0),
+    "ecal-10m-logamp-pu4": dict(seed=3, n=10_000_000, intime_log=True, lo=0.1, hi=1000.0, pileup_mean=4.0),
+    "mixed-10m-ecal-hcal": dict(seed=4, n=10_000_000, intime_log=False, lo=1.0, hi=100.0, pileup_mean=-8.0,
+                                hcal_fraction=0.4),
+    "warm-train-5m": dict(seed=5, n=5_000_000, intime_log=True, lo=0.1, hi=1000.0, pileup_mean=4.0),
+    "warm-eval-10m": dict(seed=6, n=10_000_000, intime_log=True, lo=0.1, hi=1000.0, pileup_mean=4.0),
+}
+
+
+def synth_conditions(kind: int):
+    """(P (N,K), R (N,N), bxs (K,), sigma) of a synthetic condition set: the
+    ECAL 10x10 set as the reference driver builds it, or the HCAL 8x8 set."""
+    N, K = C.c_int(), C.c_int()
+    P = np.zeros(KMAX * KMAX)
+    R = np.zeros(KMAX * KMAX)
+    bx = np.zeros(KMAX, dtype=np.int8)
+    sg = C.c_double()
+    if lib().oracle_synth_conditions(kind, C.byref(N), C.byref(K), P.ctypes.data, R.ctypes.data, bx.ctypes.data,
+                                     C.byref(sg)):
+        raise ValueError(f"unknown synthetic condition set {kind}")
+    n, k = N.value, K.value
+    return (P[: n * k].reshape(k, n).T.copy(), R[: n * n].reshape(n, n).T.copy(), bx[:k].copy(), sg.value)
+
+
+def synth_generate(workload, first: int, count: int, stride: int = 10, with_truth: bool = False,
+                   nthreads: int = 0) -> dict:
+    """Channels [first, first + count) of a seeded workload (a WORKLOADS name
+    or a dict of its parameters) on the host cores: samples, pederr, ctype and
+    optionally the true amplitudes."""
+    w = dict(WORKLOADS[workload]) if isinstance(workload, str) else dict(workload)
+    hit_mean = w.get("hit_mean", 1.0)
+    hcal = w.get("hcal_fraction", 0.0)
+    samples = np.zeros((count, stride))
+    pederr = np.zeros(count)
+    ctype = np.zeros(count, dtype=np.uint8)
+    truth = np.zeros((count, KMAX)) if with_truth else None
+    rc = lib().oracle_synth_generate(int(w["seed"]), int(w["intime_log"]), float(w["lo"]), float(w["hi"]),
+                                     float(w["pileup_mean"]), float(hit_mean), float(hcal), first, count, stride,
+                                     samples.ctypes.data, pederr.ctypes.data, ctype.ctypes.data,
+                                     truth.ctypes.data if with_truth else None, KMAX, nthreads)
+    if rc:
+        raise ValueError("oracle_synth_generate: bad arguments")
+    return {"samples": samples, "pederr": pederr, "ctype": ctype, "truth": truth}
 
 
 def kkt_violation(A, b, x) -> float:

@@ -1,8 +1,9 @@
 """Build recipe for the CPU oracle (test infrastructure).
 
 * ``oracle/_build/liboracle.so``: the C++17 FP64 restatement of the reference
-  path (multifit_oracle.cpp), built with ``-ffp-contract=off`` so that only its
-  explicit ``std::fma`` calls fuse. Built on every machine.
+  path (multifit_oracle.cpp) and the seeded synthetic-channel generator
+  (synth_oracle.cpp), built with ``-ffp-contract=off`` so that only explicit
+  ``std::fma`` calls fuse. Built on every machine.
 * ``oracle/_ref/libref_linalgebra.so``: the reference project's own
   header-only linear-algebra primitives (``linalgebra/interface/*.hpp``),
   compiled in place from the reference tree with a small driver
@@ -62,12 +63,12 @@ def _stale(target: str, sources: list[str]) -> bool:
 
 
 def _build_oracle_lib(target: str, defines: list[str], force: bool) -> str:
-    src = os.path.join(HERE, "multifit_oracle.cpp")
-    if force or _stale(target, [src, __file__]):
+    srcs = [os.path.join(HERE, "multifit_oracle.cpp"), os.path.join(HERE, "synth_oracle.cpp")]
+    if force or _stale(target, [*srcs, __file__]):
         os.makedirs(BUILD, exist_ok=True)
         tmp = target + ".tmp"
         cmd = ["g++", "-std=c++17", "-O3", "-ffp-contract=off", "-fPIC", "-shared", "-pthread", *defines,
-               src, "-o", tmp]
+               *srcs, "-o", tmp]
         subprocess.check_call(cmd)
         os.replace(tmp, target)
     return target

@@ -150,6 +150,12 @@ int check_options(const mf_options* o) {
   const int cpw = o->channels_per_warp;
   if (cpw != 0 && cpw != 1 && cpw != 2 && cpw != 4 && cpw != 8 && cpw != 32) return MF_EINVAL;
   if (o->schedule == MF_SCHED_PERSISTENT && o->block_size > 512) return MF_EINVAL;
+  // the grid schedule's kernels are compiled for at most 128 threads a block
+  if (o->schedule == MF_SCHED_GRID && o->block_size > 128) {
+    std::snprintf(g_last_error, sizeof(g_last_error),
+                  "block_size %d: the grid schedule takes at most 128 threads a block", o->block_size);
+    return MF_EINVAL;
+  }
   return MF_OK;
 }
 
@@ -1116,7 +1122,11 @@ extern "C" int mf_fit_noalloc(mf_context* c, const mf_batch* b, const mf_options
     return MF_EINVAL;
   }
   for (int t = 0; t < a.n_ctypes; ++t)
-    if (!c->tab_ok[t]) return MF_EUNSUPPORTED;
+    if (!c->tab_ok[t]) {
+      std::snprintf(g_last_error, sizeof(g_last_error),
+                    "mf_fit_noalloc: condition set %d has no passive-set tables (shape or pulse covariance)", t);
+      return MF_EUNSUPPORTED;
+    }
   int cur = -1;
   cudaError_t e = cudaGetDevice(&cur);
   if (e != cudaSuccess) {

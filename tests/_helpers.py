@@ -99,17 +99,21 @@ def assert_bitwise(gpu, ref, fields=("amplitudes", "chi2", "active_mask", "statu
         assert np.array_equal(g, r), "iteration counters differ"
 
 
+COMMITTED_DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_data")
+
+
 def reference_data_dir():
     """The reference tree's data/ directory (the tree the oracle recipe
-    compiles from), for the CPU tests of the data-file readers; they skip
-    where it is absent."""
+    compiles from) where it exists, else the two data files committed under
+    tests/golden/reference_data/ (made by tests/golden/make_reference_data.py)."""
     from oracle import build_oracle
 
-    return os.path.join(build_oracle.REFERENCE_ROOT, "data")
+    d = os.path.join(build_oracle.REFERENCE_ROOT, "data")
+    return d if os.path.isdir(d) else COMMITTED_DATA
 
 
 def replay_data_dir():
-    """A directory holding the reference's data files for the GPU replay
-    tests, only when the user names one in MULTIFIT_REPLAY_DATA (the GPU
-    tests read no default location); None otherwise."""
-    return os.environ.get("MULTIFIT_REPLAY_DATA") or None
+    """The directory of the reference's data files for the GPU replay tests:
+    MULTIFIT_REPLAY_DATA where the user names one, else the committed copies
+    under tests/golden/reference_data/."""
+    return os.environ.get("MULTIFIT_REPLAY_DATA") or COMMITTED_DATA

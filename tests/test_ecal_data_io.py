@@ -283,3 +283,21 @@ def test_reader_compressed_record_blocks(rootio):
     rf.data = bytes(keylen) + b"L4" + body[2:]
     with pytest.raises(rootio.RootFormatError, match="not supported"):
         rf.payload(key)
+
+
+def test_committed_data_files_are_the_references():
+    """tests/golden/reference_data/ holds the reference's files unchanged."""
+    import hashlib
+
+    from _helpers import COMMITTED_DATA
+
+    want = {"mysample_100_0.000_0.000_10_25.00_10.00_0.00_1.000_1.00_CRRC43_0.00_slew_1.00.root":
+            "12bd30188d1f5084b7fa0bc795fb7483823acc78846cc2e01ee5143c45cd10b8",
+            "EmptyFile.root": "e771768a1b1d5b55cadaccce00aabe507a2949dac136904381ce3cf6d0cbe3a9"}
+    for name, digest in want.items():
+        data = open(os.path.join(COMMITTED_DATA, name), "rb").read()
+        assert hashlib.sha256(data).hexdigest() == digest, name
+        ref = os.path.join(DATA, name)
+        if DATA != COMMITTED_DATA and os.path.exists(ref):
+            assert open(ref, "rb").read() == data, name
+

@@ -18,7 +18,7 @@ from _helpers import replay_data_dir
 pytestmark = pytest.mark.gpu
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "replay_mysample_100.npz")
-DATA = replay_data_dir() or ""
+DATA = replay_data_dir()
 SAMPLE_100 = os.path.join(DATA, "mysample_100_0.000_0.000_10_25.00_10.00_0.00_1.000_1.00_CRRC43_0.00_slew_1.00.root")
 SHAPE = os.path.join(DATA, "EmptyFile.root")
 AMP_TOL = 1e-4  # normwise relative amplitude error of the mixed and FP32 forms
@@ -82,10 +82,10 @@ def test_replay_mixed_forms_within_bounds_of_kkt_fits(mf, cuda, eio, gold, prec)
 
 
 @pytest.mark.skipif(not (DATA and os.path.exists(SAMPLE_100) and os.path.exists(SHAPE)),
-                    reason="MULTIFIT_REPLAY_DATA does not name a directory with the reference's data files")
+                    reason="the reference's data files are absent")
 def test_replay_from_the_root_file(mf, cuda, eio, gold):
-    """With MULTIFIT_REPLAY_DATA naming a directory that holds the two data
-    files: read, condition and fit end to end."""
+    """The two data files (committed copies, or MULTIFIT_REPLAY_DATA's):
+    read, condition and fit end to end."""
     eng = mf.Engine(0)
     r = eio.replay(eng, SAMPLE_100, SHAPE)
     assert np.array_equal(r["samples"], gold["samples"])

@@ -1,9 +1,10 @@
 """The reference driver's run() in C++ against the engine
 (tests/cpp/replay_driver.cpp: include/multifit_gb300_io.hpp reads the data
 files, mfgb::PulseChiSqSNNLS / mfgb::BatchFitter fit them). It compiles and
-links here; on a GPU, with MULTIFIT_REPLAY_DATA naming a directory that holds
-the reference's two data files, it reproduces the oracle's fits and physics
-check of tests/golden/replay_mysample_100.npz bit for bit."""
+links here; on a GPU, on the reference's two data files (the copies committed
+under tests/golden/reference_data/, or a directory MULTIFIT_REPLAY_DATA
+names), it reproduces the oracle's fits and physics check of
+tests/golden/replay_mysample_100.npz bit for bit."""
 import os
 import subprocess
 
@@ -14,7 +15,7 @@ from _helpers import replay_data_dir
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(ROOT, "tests", "golden", "replay_mysample_100.npz")
-DATA = replay_data_dir() or ""
+DATA = replay_data_dir()
 SAMPLE_100 = os.path.join(DATA, "mysample_100_0.000_0.000_10_25.00_10.00_0.00_1.000_1.00_CRRC43_0.00_slew_1.00.root")
 SHAPE = os.path.join(DATA, "EmptyFile.root")
 
@@ -42,7 +43,7 @@ def test_replay_driver_compiles_and_links(mf, tmp_path, extra):
 @pytest.mark.parametrize("batch", [0, 1])
 def test_replay_driver_reproduces_oracle(mf, cuda, tmp_path, batch):
     if not (DATA and os.path.exists(SAMPLE_100) and os.path.exists(SHAPE)):
-        pytest.skip("MULTIFIT_REPLAY_DATA does not name a directory with the reference's data files")
+        pytest.skip("the reference's data files are absent")
     g = dict(np.load(GOLDEN))
     exe = build(mf, tmp_path)
     r = subprocess.run([exe, SAMPLE_100, SHAPE, "0", str(batch)], capture_output=True, text=True, timeout=300)

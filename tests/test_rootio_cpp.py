@@ -69,6 +69,20 @@ def test_inflate_rejects_corrupt_stream(exe, tmp_path):
     assert r.returncode == 2 and "Adler-32" in r.stdout
 
 
+@pytest.mark.parametrize("level", [0, 1, 6, 9])
+def test_inflate_stops_at_the_declared_size(exe, tmp_path, level):
+    """A stream that inflates to more than its record declares is refused as
+    soon as its output passes the declared size (stored, literal and
+    back-reference output alike), not after it has been decoded whole."""
+    d = b"0123456789" * 20_000 + bytes(range(256)) * 40
+    z = zlib.compress(d, level)
+    declared = len(d) // 3
+    path = tmp_path / "over.bin"
+    path.write_bytes(struct.pack("<QQ", declared, len(z)) + z + d[:declared])
+    r = run(exe, "inflate", path)
+    assert r.returncode == 2 and "exceeds the declared size" in r.stdout, r.stdout
+
+
 @needs_data
 def test_cpp_reader_matches_python_reader_fixture(exe, tmp_path):
     g = dict(np.load(GOLDEN))
