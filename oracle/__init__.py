@@ -106,6 +106,70 @@ def ref_ocl_inplace_fnnls(A: np.ndarray, b: np.ndarray, x0: np.ndarray | None = 
     return x
 
 
+_ref_dofit = None
+
+
+def ref_dofit_lib():
+    """The reference's multifit_cpu fit (PulseChiSqSNNLS.cpp + inplace_fnnls.cu
+    over the Eigen shim), or None where the reference tree is absent."""
+    global _ref_dofit
+    if _ref_dofit is None:
+        path = build_oracle.build_ref_dofit()
+        if path is None:
+            return None
+        L = C.CDLL(path)
+        L.ref_dofit_batch.restype = C.c_int
+        L.ref_dofit_batch.argtypes = [C.c_long, C.c_int] + [C.c_void_p] * 6 + [C.c_int] + [C.c_void_p] * 4
+        _ref_dofit = L
+    return _ref_dofit
+
+
+def fullpulse_of(P: np.ndarray, bxs) -> np.ndarray:
+    """The 19-sample fullpulse that the reference's sliding-window rule
+    (multifit_cpu/src/PulseChiSqSNNLS.cpp:49-62) turns into the 10 x K pulse
+    matrix P; raises if P is not of that form."""
+    P = np.asarray(P, dtype=np.float64)
+    fp = np.zeros(19)
+    seen = np.zeros(19, dtype=bool)
+    for k, bx in enumerate(np.asarray(bxs, dtype=np.int64)):
+        first = max(0, int(bx) + 3)
+        for i in range(P.shape[0]):
+            if i < first:
+                if P[i, k] != 0:
+                    raise ValueError("P is not a sliding window of one fullpulse")
+                continue
+            j = i + 4 - int(bx)
+            if not 0 <= j < 19 or (seen[j] and fp[j] != P[i, k]):
+                raise ValueError("P is not a sliding window of one fullpulse")
+            fp[j], seen[j] = P[i, k], True
+    return fp
+
+
+def ref_dofit(samples, pederr, R, bxs, fullpulse, fullpulsecov=None, compute_errors: bool = False) -> dict:
+    """The reference's own PulseChiSqSNNLS::DoFit on each channel (N = 10):
+    X(), ChiSq(), the in-time Errors() entry and DoFit's return value."""
+    L = ref_dofit_lib()
+    if L is None:
+        raise RuntimeError("the reference tree is needed for the reference DoFit")
+    s = np.ascontiguousarray(samples, dtype=np.float64)
+    n = s.shape[0]
+    if s.shape[1] != 10:
+        raise ValueError("the reference fit is fixed at 10 samples")
+    bx = np.ascontiguousarray(bxs, dtype=np.int8)
+    K = bx.shape[0]
+    Rcm = np.ascontiguousarray(np.asarray(R, dtype=np.float64).T)
+    fp = np.ascontiguousarray(fullpulse, dtype=np.float64)
+    F = None if fullpulsecov is None else np.ascontiguousarray(np.asarray(fullpulsecov, dtype=np.float64).T)
+    pe = np.ascontiguousarray(pederr, dtype=np.float64)
+    out = {"amplitudes": np.zeros((n, K)), "chi2": np.zeros(n), "errors": np.zeros(n), "ok": np.zeros(n, np.int32)}
+    rc = L.ref_dofit_batch(n, K, s.ctypes.data, Rcm.ctypes.data, pe.ctypes.data, bx.ctypes.data, fp.ctypes.data,
+                           F.ctypes.data if F is not None else None, int(compute_errors), out["amplitudes"].ctypes.data,
+                           out["chi2"].ctypes.data, out["errors"].ctypes.data, out["ok"].ctypes.data)
+    if rc:
+        raise ValueError(f"ref_dofit_batch rc={rc}")
+    return out
+
+
 def ref():
     """The reference's own linalgebra primitives, or None where the reference tree is absent."""
     global _ref

@@ -24,9 +24,23 @@
   float mapped to double. Built only where the reference tree exists. The
   FP64 build equals liboracle_sep.so's incremental FNNLS bit for bit.
 
-The rest of the reference path (inplace_fnnls, PulseChiSqSNNLS) includes
-Eigen, which the reference does not vendor and which is absent here, so it is
-not built.
+* ``oracle/_ref/libref_dofit.so``: the reference's own multifit_cpu fit,
+  ``multifit_cpu/src/PulseChiSqSNNLS.cpp`` (DoFit, Minimize, updateCov, NNLS,
+  ComputeChiSq, ComputeApproxUncertainty) and ``nnls/src/inplace_fnnls.cu``,
+  compiled unmodified through ref_dofit_driver.cpp. Both include Eigen, which
+  the reference does not vendor and which is absent here: ``eigen_shim/``
+  provides the small part of its API they use, with the oracle's canonical
+  arithmetic order, and ``eigen_shim_stubs/`` an empty stand-in for the
+  vendored Eigen NNLS module the fit includes but never calls. Built with
+  ``-O3 -ffp-contract=fast`` (and FMA on x86) so that gcc fuses the
+  accumulations written in the reference's own loops (transpose_multiply's
+  ``+=``), as the oracle does; ``-fsigned-char`` because the fit keeps its
+  BX offsets in plain char. Built only where the reference tree exists.
+
+The reference tree is read from MULTIFIT_REFERENCE_ROOT, by default the
+location this recipe was written against; where it is absent, every _ref
+library is skipped and the tests fall back on the committed outputs in
+tests/golden/.
 """
 from __future__ import annotations
 
@@ -43,6 +57,7 @@ REFERENCE_ROOT = os.environ.get("MULTIFIT_REFERENCE_ROOT", "/root/reference")
 ORACLE_LIB = os.path.join(BUILD, "liboracle.so")
 ORACLE_SEP_LIB = os.path.join(BUILD, "liboracle_sep.so")
 REF_LIB = os.path.join(REF_OUT, "libref_linalgebra.so")
+REF_DOFIT_LIB = os.path.join(REF_OUT, "libref_dofit.so")
 REF_OCL_LIBS = {64: os.path.join(REF_OUT, "libref_ocl_fnnls_f64.so"),
                 32: os.path.join(REF_OUT, "libref_ocl_fnnls_f32.so")}
 
@@ -116,12 +131,33 @@ def build_ref(force: bool = False) -> str | None:
     return REF_LIB
 
 
+def build_ref_dofit(force: bool = False) -> str | None:
+    """The reference's multifit_cpu fit compiled over the Eigen shim, or None
+    where the reference tree is absent."""
+    src_cpp = os.path.join(REFERENCE_ROOT, "multifit_cpu", "src", "PulseChiSqSNNLS.cpp")
+    if not os.path.exists(src_cpp):
+        return None
+    shim = os.path.join(HERE, "eigen_shim", "Eigen", "Dense")
+    stub = os.path.join(HERE, "eigen_shim_stubs", "nnls", "interface", "eigen_nnls.h")
+    drv = os.path.join(HERE, "ref_dofit_driver.cpp")
+    if force or _stale(REF_DOFIT_LIB, [drv, shim, stub, __file__]):
+        os.makedirs(REF_OUT, exist_ok=True)
+        tmp = REF_DOFIT_LIB + ".tmp"
+        cmd = ["g++", "-std=c++17", "-O3", "-ffp-contract=fast", *_fma_flag(), "-fsigned-char", "-Wno-unknown-pragmas",
+               "-fPIC", "-shared", "-I", os.path.join(HERE, "eigen_shim"), "-iquote",
+               os.path.join(HERE, "eigen_shim_stubs"), "-I", REFERENCE_ROOT, drv, "-o", tmp]
+        subprocess.check_call(cmd)
+        os.replace(tmp, REF_DOFIT_LIB)
+    return REF_DOFIT_LIB
+
+
 def main() -> int:
     force = "--force" in sys.argv
     print(build_oracle(force))
     print(build_ref(force) or "reference tree absent: oracle/_ref not built")
     print(build_oracle_separate(force))
     print(build_ref_ocl(force) or "reference tree absent: OpenCL FNNLS not built")
+    print(build_ref_dofit(force) or "reference tree absent: reference DoFit not built")
     return 0
 
 

@@ -71,3 +71,29 @@ def test_mixed_form_within_bounds_of_kkt_fixture(mf, cuda, name, prec):
     if name != "edge":
         assert (diff[ok] == 0).all()
     eng.close()
+
+
+@pytest.mark.parametrize("errors", [0, 1])
+@pytest.mark.parametrize("name", ["c0", "logamp", "warm", "fpc", "edge"])
+def test_fp64_kernel_reproduces_reference_dofit(mf, cuda, name, errors):
+    """The FP64 drop-in against the reference's own multifit_cpu fit
+    (PulseChiSqSNNLS.cpp + inplace_fnnls.cu compiled over the oracle's Eigen
+    shim; outputs in tests/golden/dofit_ref.npz): bit for bit, with the
+    reference's settings (reference start, max_iter 10) and errors off or on."""
+    g = dict(np.load(os.path.join(GOLDEN, "dofit_ref.npz")))
+    F = g["fullpulsecov"] if bool(g[f"{name}_has_fpc"]) else None
+    eng = mf.Engine(0)
+    eng.set_conditions(0, mf.make_conditions(g["P"], g["R"], g["bxs"], fullpulsecov=F))
+    s = g[f"{name}_samples"]
+    n = s.shape[0]
+    db = DeviceBatch(mf, cuda, n)
+    db.samples[:n] = cuda.from_numpy(s).cuda()
+    db.pederr[:n] = cuda.from_numpy(g[f"{name}_pederr"]).cuda()
+    cuda.cuda.synchronize()
+    eng.fit_device(db.batch, mf.default_options(compute_errors=errors))
+    o = db.outputs_host()
+    assert np.array_equal(o["amplitudes"], g[f"{name}_e{errors}_amplitudes"])
+    assert np.array_equal(o["chi2"], g[f"{name}_e{errors}_chi2"])
+    if errors:
+        assert np.array_equal(o["errors"], g[f"{name}_e{errors}_errors"], equal_nan=True)
+    eng.close()
