@@ -173,7 +173,26 @@ FORM_DESC = {
     "fp32": "FP32: FP32 active-set search + double-float screen and judge (FP32 error-free transforms), "
             "FP64 repair of the rare rejects, KKT-converged",
     "warm": "learned warm start: BF16 tensor-core MLP + the FP32 form (double-float judge) to KKT",
+    "fp32-cov": "per-channel FP32 form (a pulse covariance makes the covariance amplitude-dependent): each "
+                "Minimize's outer loop in FP32, then FP64 from its result (one FP64 covariance factor, refinement "
+                "solve and chi2 when the FP32 fit was right), KKT-converged",
 }
+# the pulse covariance of the fp32-cov workload: 1e-4 exp(-|i-j| / 3) over the
+# template's samples 7..18 of the 19-sample fullpulse (a pulse-shape jitter)
+FPC_SCALE, FPC_LENGTH = 1e-4, 3.0
+
+
+def pulse_covariance():
+    import numpy as np
+
+    F = np.zeros((19, 19))
+    idx = np.arange(7, 19)
+    F[np.ix_(idx, idx)] = FPC_SCALE * np.exp(-np.abs(np.subtract.outer(idx, idx)) / FPC_LENGTH)
+    return F
+
+
+def default_workload(form: str) -> str:
+    return {"fp64": "ecal-1m-pu2", "fp32-cov": "ecal-1m-pu2"}.get(form, "warm-eval-10m")
 # useful FLOPs of one warm-start prediction: 12 inputs -> 128 -> 128 -> 20
 # outputs, 2 per multiply-add (the network pads to 16 inputs and 32 outputs)
 MLP_FLOPS_PER_CHANNEL = 2 * (12 * 128 + 128 * 128 + 128 * 20)
@@ -193,6 +212,8 @@ def form_options(mf, args, mixed_sets=False):
         return mf.default_options(precision=mf.PREC_MIXED, max_iter_nnls=1000, schedule=sched)
     if args.form == "fp32":
         return mf.default_options(precision=mf.PREC_FP32, max_iter_nnls=1000, schedule=sched)
+    if args.form == "fp32-cov":
+        return mf.default_options(precision=mf.PREC_FP32, max_iter_nnls=1000)
     return mf.default_options(precision=mf.PREC_FP32, warm_start=mf.WARM_MLP, max_iter_nnls=1000, schedule=sched)
 
 
@@ -283,12 +304,15 @@ def run_ours(args, world, rank, local):
     build_pkg()
     mf = load_pkg()
     eng = mf.Engine(local)
-    wl = args.workload or ("ecal-1m-pu2" if args.form == "fp64" else "warm-eval-10m")
+    wl = args.workload or default_workload(args.form)
     p = mf.WORKLOADS[wl]()
     n = int(args.channels or p.n)
     p.n = n
     mixed = p.hcal_fraction > 0
     ecal, _ = mf.synth_conditions(mf.SYNTH_ECAL)
+    if args.form == "fp32-cov":
+        P, R, bxs, _ = mf.conditions_arrays(ecal)
+        ecal = mf.make_conditions(P, R, bxs, fullpulsecov=pulse_covariance())
     eng.set_conditions(0, ecal)
     if mixed:
         hcal, _ = mf.synth_conditions(mf.SYNTH_HCAL)
@@ -466,13 +490,13 @@ def run_ours(args, world, rank, local):
             sel = np.nonzero(ct == t)[0]
             if sel.size == 0:
                 continue
-            P, R, bxs, _ = mf.conditions_arrays(cond)
+            P, R, bxs, F = mf.conditions_arrays(cond)
             if args.form == "fp64":
-                ref = oracle.fit_batch(inp_s[sel], inp_p[sel], P, R, bxs, max_iter_nnls=args.max_iter,
+                ref = oracle.fit_batch(inp_s[sel], inp_p[sel], P, R, bxs, fullpulsecov=F, max_iter_nnls=args.max_iter,
                                        start=args.start)
                 ok = ok and bool(np.array_equal(a_gpu[sel, : P.shape[1]], ref["amplitudes"]))
             else:
-                ref = oracle.fit_batch(inp_s[sel], inp_p[sel], P, R, bxs, max_iter_nnls=1000, start=1)
+                ref = oracle.fit_batch(inp_s[sel], inp_p[sel], P, R, bxs, fullpulsecov=F, max_iter_nnls=1000, start=1)
                 r = ref["amplitudes"]
                 e = np.abs(a_gpu[sel, : P.shape[1]] - r).max(axis=1) / np.maximum(np.abs(r).max(axis=1), 1e-300)
                 worst = max(worst, float(e.max())) if sel.size else worst
@@ -550,7 +574,8 @@ def run_ours(args, world, rank, local):
             "scaling": "weak",
             "vs_baseline": None,
             "dtype": {"fp64": "f64", "mixed": "f32+f64", "fp32": "f32 (double-float judge; f64 repair)",
-                      "warm": "f32 (double-float judge; f64 repair; bf16 MLP)"}[args.form],
+                      "warm": "f32 (double-float judge; f64 repair; bf16 MLP)",
+                      "fp32-cov": "f32 outer loop; f64 final iteration"}[args.form],
             "data": "synthetic (seeded Philox generator; the workload's shapes and value distributions)",
             "config": workload_config(args, wl, n, world),
             "engine": {
@@ -626,6 +651,8 @@ def kernel_rooflines(mf, eng, kernels, args, n, ctype, plain_flops, form_fp64_fl
         mean_s = total / launches * 1e-3
         if name == "fit_fp64_kernel":
             work, bound, peak, unit = plain_flops / per_step, "fp64", fp64_peak, "TFLOP/s"
+        elif name == "fit_cov_kernel":  # its FP64 phase's counted flops (the FP32 phase is not FP64 work)
+            work, bound, peak, unit = form_fp64_flops / per_step, "fp64", fp64_peak, "TFLOP/s"
         elif name == "judge_kernel" and df_form:
             work, bound, peak, unit = judge_df / per_step, "fp32", fp32_peak, "TFLOP/s"
         elif name == "judge_kernel":
@@ -678,10 +705,13 @@ def workload_config(args, wl: str, n: int, world: int) -> dict:
     """The `config` both arms print: the workload and the fit it asks for,
     nothing that depends on which arm runs it."""
     _, _, fit = reference_fit_setting(args)
-    return {"workload": wl, "description": WORKLOAD_DESC.get(wl, wl), "channels_per_step": n, "fit": fit,
-            "l2": "inputs (88 B/channel) exceed every cache; the GPU arm also flushes its L2 between steps "
-                  "(256 MB write)",
-            "parallelism": f"replicas x{world}"}
+    cfg = {"workload": wl, "description": WORKLOAD_DESC.get(wl, wl), "channels_per_step": n, "fit": fit,
+           "l2": "inputs (88 B/channel) exceed every cache; the GPU arm also flushes its L2 between steps "
+                 "(256 MB write)",
+           "parallelism": f"replicas x{world}"}
+    if args.form == "fp32-cov":
+        cfg["fullpulsecov"] = f"{FPC_SCALE:g} exp(-|i-j|/{FPC_LENGTH:g}) over fullpulse samples 7..18"
+    return cfg
 
 
 class CpuReference:
@@ -689,13 +719,14 @@ class CpuReference:
     multifit_cpu's fit (oracle/, C++), fed by the oracle's own seeded
     generator. Loads nothing of the engine."""
 
-    def __init__(self, wl: str, n: int):
+    def __init__(self, wl: str, n: int, fullpulsecov=None):
         sys.path.insert(0, ROOT)
         import numpy as np
 
         import oracle
 
         self.oracle, self.np = oracle, np
+        self.fpc = fullpulsecov
         self.nt = oracle.hardware_threads()
         self.wl, self.n = wl, n
         sets = [0, 1] if oracle.WORKLOADS[wl].get("hcal_fraction", 0.0) > 0 else [0]
@@ -715,8 +746,8 @@ class CpuReference:
             if k == 0:
                 continue
             P, R, bxs, _ = self.conds[t]
-            self.oracle.fit_batch(s[:k], pe[:k], P, R, bxs, max_iter_nnls=max_iter, start=start,
-                                  nthreads=nthreads or self.nt)
+            self.oracle.fit_batch(s[:k], pe[:k], P, R, bxs, fullpulsecov=self.fpc if t == 0 else None,
+                                  max_iter_nnls=max_iter, start=start, nthreads=nthreads or self.nt)
         return time.perf_counter() - t0
 
     def channels(self, m: int | None) -> int:
@@ -740,7 +771,7 @@ def cpu_baseline(args, wl: str, n: int, budget_s: float = 10.0) -> dict:
     driver's own setting, multifit_cpu/src/multifit.cpp:196-227), for the fit
     the timed form computes and for multifit_cpu's literal settings."""
     mi, st, fit = reference_fit_setting(args)
-    ref = CpuReference(wl, min(n, 2_000_000))
+    ref = CpuReference(wl, min(n, 2_000_000), pulse_covariance() if args.form == "fp32-cov" else None)
     allt = ref.rate(mi, st, ref.nt, budget_s * 0.4)
     one = ref.rate(mi, st, 1, budget_s * 0.2)
     lit_all = ref.rate(10, 0, ref.nt, budget_s * 0.25)
@@ -761,13 +792,13 @@ def run_reference(args, world, rank):
     loaded. Rank 0 alone runs it."""
     if rank != 0:
         return None
-    wl = args.workload or ("ecal-1m-pu2" if args.form == "fp64" else "warm-eval-10m")
+    wl = args.workload or default_workload(args.form)
     sys.path.insert(0, ROOT)
     import oracle
 
     n = int(getattr(args, "channels", 0) or oracle.WORKLOADS[wl]["n"])
     mi, st, fit = reference_fit_setting(args)
-    ref = CpuReference(wl, n)
+    ref = CpuReference(wl, n, pulse_covariance() if args.form == "fp32-cov" else None)
     # a step fits every channel unless that would take longer than the step cap:
     # then the first m channels of each set, stated in the line
     probe_dt = ref.fit(mi, st, ref.nt, min(n, 20_000))
@@ -827,13 +858,14 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--form", choices=["warm", "fp32", "mixed", "fp64"], default="warm")
+    ap.add_argument("--form", choices=["warm", "fp32", "mixed", "fp64", "fp32-cov"], default="warm")
     ap.add_argument("--schedule", choices=["auto", "grid", "persistent"], default="auto",
                     help="auto: persistent work stealing for workloads of several condition sets "
                          "(mixed/warm forms), else grid")
     ap.add_argument("--autotune", action="store_true",
                     help="sweep the persistent schedule's launch shape on the workload first (untimed)")
-    ap.add_argument("--workload", default="", help="default: warm-eval-10m (warm/mixed), ecal-1m-pu2 (fp64)")
+    ap.add_argument("--workload", default="",
+                    help="default: warm-eval-10m (warm/fp32/mixed), ecal-1m-pu2 (fp64, fp32-cov)")
     ap.add_argument("--train-channels", type=int, default=0)
     ap.add_argument("--train-epochs", type=int, default=3)
     ap.add_argument("--channels", type=int, default=0, help="override the workload's channel count")

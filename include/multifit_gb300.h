@@ -65,7 +65,15 @@ enum mf_channel_status {
   MF_CH_BADINPUT = 8       /* non-finite sample or pederr, or bad condition index */
 };
 
-/* Arithmetic of the fit. */
+/* Arithmetic of the fit. MF_PREC_MIXED and MF_PREC_FP32 return each channel's
+ * NNLS optimum (KKT point) within 1e-4 of the FP64 fit run to convergence.
+ * They fit through the passive-set tables of a condition set when it has them
+ * (no pulse covariance, N = K = 10 or 8) and errors are off; otherwise the
+ * whole batch takes the per-channel form: each Minimize runs its outer chi2
+ * loop in FP32 (covariance, Cholesky, whitening, FNNLS), then continues in
+ * FP64 from that result (one FP64 covariance factor, refinement solve and
+ * chi2 when the FP32 fit was right; more FP64 iterations when not), on the
+ * grid schedule and from a cold start. */
 enum mf_precision {
   MF_PREC_FP64 = 0,  /* plain FP64, bit-identical to the CPU oracle's canonical order */
   MF_PREC_MIXED = 1, /* FP32 search and screen; FP64 refinement solve, residual and chi2 (the judge) */
@@ -228,7 +236,8 @@ enum mf_kernel_kind {
   MF_K_REJUDGE = 6,   /* judge_fixed_kernel / judge_fixed_persist: the judge of the channels the fix changed */
   MF_K_FIX = 7,       /* fix_kernel / fix_persist: FP32 FNNLS step of the channels queued for it */
   MF_K_SCREEN = 8,    /* screen_kernel / screen_persist: FP32 double-float KKT screen (cold starts) */
-  MF_K_COUNT = 9
+  MF_K_FIT_COV = 9,   /* fit_cov_kernel: per-channel form (pulse covariance, errors, shapes without tables) */
+  MF_K_COUNT = 10
 };
 /* enable != 0 creates the context's event pool (and clears it); 0 frees it. */
 int mf_profile(mf_context* ctx, int enable);

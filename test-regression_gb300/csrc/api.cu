@@ -89,6 +89,7 @@ struct mf_context {
   double* d_pinv64[MF_MAX_CTYPES] = {nullptr, nullptr};
   float* d_pinv32[MF_MAX_CTYPES] = {nullptr, nullptr};
   float* d_pinv32lo[MF_MAX_CTYPES] = {nullptr, nullptr};
+  float* d_pinv2[MF_MAX_CTYPES] = {nullptr, nullptr};
   MlpState mlp;
   int sms = 152;
   // mixed-form hand-off workspace (MIXED_CHUNK channels), allocated with the tables
@@ -354,8 +355,30 @@ int dispatch_mixed(mf_context* c, const FitArgs& a, const mf_options* o, cudaStr
   return MF_OK;
 }
 
+// The mixed and FP32 precisions fit a batch through the passive-set tables
+// when every condition set it uses has them and no errors are asked for;
+// otherwise (a pulse covariance makes the covariance depend on the channel's
+// amplitudes, the MINOS-like errors refit with a constrained column, or a
+// shape has no tables) through the per-channel form, on the grid schedule
+// and from a cold start (the learned warm start seeds the table search only).
+bool per_channel_form(const mf_context* c, const FitArgs& a, const mf_options* o) {
+  if (o->compute_errors) return true;
+  for (int t = 0; t < a.n_ctypes; ++t)
+    if (!c->tab_ok[t]) return true;
+  return false;
+}
+
 int dispatch_form(mf_context* c, const FitArgs& a, const mf_options* o, cudaStream_t s, bool instrumented,
                   bool allow_graph, int lane) {
+  if ((o->precision == MF_PREC_MIXED || o->precision == MF_PREC_FP32) && per_channel_form(c, a, o)) {
+    const int block = o->block_size && o->block_size <= 128 ? o->block_size : 128;
+    const cudaError_t e = launch_fit_cov(a, block, s, instrumented, &c->timer);
+    if (e != cudaSuccess) {
+      set_last_error("per-channel fit launch", e);
+      return MF_ECUDA;
+    }
+    return MF_OK;
+  }
   if (o->precision == MF_PREC_MIXED || o->precision == MF_PREC_FP32)
     return dispatch_mixed(c, a, o, s, allow_graph, lane);
   if (o->precision != MF_PREC_FP64 || o->schedule != MF_SCHED_GRID || o->warm_start != MF_WARM_NONE)
@@ -440,7 +463,9 @@ void free_tables(mf_context* c, int t) {
   cudaFree(c->d_pinv64[t]);
   cudaFree(c->d_pinv32[t]);
   cudaFree(c->d_pinv32lo[t]);
+  cudaFree(c->d_pinv2[t]);
   c->d_pinv32lo[t] = nullptr;
+  c->d_pinv2[t] = nullptr;
   c->d_offset[t] = nullptr;
   c->d_pinv64[t] = nullptr;
   c->d_pinv32[t] = nullptr;
@@ -464,11 +489,14 @@ int upload_tables(mf_context* c, int t) {
   if (e == cudaSuccess) e = cudaMalloc(&c->d_pinv64[t], sizeof(double) * np);
   if (e == cudaSuccess) e = cudaMalloc(&c->d_pinv32[t], sizeof(float) * np);
   if (e == cudaSuccess) e = cudaMalloc(&c->d_pinv32lo[t], sizeof(float) * np);
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_pinv2[t], sizeof(float) * h.pinv2.size());
   if (e == cudaSuccess) e = cudaMemcpy(c->d_offset[t], h.offset.data(), sizeof(int) * no, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(c->d_pinv64[t], h.pinv64.data(), sizeof(double) * np, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(c->d_pinv32[t], h.pinv32.data(), sizeof(float) * np, cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
     e = cudaMemcpy(c->d_pinv32lo[t], h.pinv32lo.data(), sizeof(float) * np, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(c->d_pinv2[t], h.pinv2.data(), sizeof(float) * h.pinv2.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess && !c->ws_mask) {
     e = cudaMalloc(&c->ws_mask, sizeof(uint16_t) * MIXED_CHUNK);
     if (e == cudaSuccess) e = cudaMalloc(&c->ws_count, sizeof(uint16_t) * MIXED_CHUNK);
@@ -514,6 +542,7 @@ void fill_dev_mixed(const mf_context* c, int t, DevMixed* m) {
   m->pinv64 = c->d_pinv64[t];
   m->pinv32 = c->d_pinv32[t];
   m->pinv32lo = c->d_pinv32lo[t];
+  m->pinv2 = c->d_pinv2[t];
 }
 
 int grow_staging(mf_context* c, int64_t n, int ss, int as) {

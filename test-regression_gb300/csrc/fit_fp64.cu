@@ -17,480 +17,20 @@
 // The FP64 pipe of the GB300 issues about 1/58 of the FP32 rate, so this
 // kernel is bound by FP64 instructions; integer, shared-memory and local
 // traffic hide under them.
-#include <cfloat>
-
-#include "mf_internal.h"
+#include "fit_core.cuh"
 
 namespace mfgb {
 namespace {
 
-struct Flop {
-  double v;
-  __device__ __forceinline__ void fma(double k) { v += 2 * k; }
-  __device__ __forceinline__ void op(double k) { v += k; }
-};
-
-template <bool COUNT>
-struct Counter {
-  Flop f{0};
-  __device__ __forceinline__ void fma(double k) {
-    if (COUNT) f.fma(k);
-  }
-  __device__ __forceinline__ void op(double k) {
-    if (COUNT) f.op(k);
-  }
-};
-
-// linalgebra/interface/cholesky.hpp:8-38 (rows [r0, r1) of a row-major factor)
-template <bool C>
-__device__ __forceinline__ void chol_rows(const double* M, double* L, int ld, int r0, int r1, Counter<C>& f) {
-  for (int i = r0; i < r1; ++i) {
-    double sumsq = 0;
-    for (int j = 0; j < i; ++j) {
-      double s2 = 0;
-      for (int k = 0; k < j; ++k) s2 = fma(L[i * ld + k], L[j * ld + k], s2);
-      const double v = (M[i * ld + j] - s2) / L[j * ld + j];
-      L[i * ld + j] = v;
-      sumsq = fma(v, v, sumsq);
-      f.fma(j + 1);
-      f.op(2);
-    }
-    L[i * ld + i] = sqrt(M[i * ld + i] - sumsq);
-    f.op(2);
-  }
-}
-
-// linalgebra/interface/substitution.hpp:10-26
-template <bool C>
-__device__ __forceinline__ void fwd(const double* L, int ld, const double* b, double* y, int n, Counter<C>& f) {
-  for (int i = 0; i < n; ++i) {
-    double t = b[i];
-    for (int j = 0; j < i; ++j) t = fma(-L[i * ld + j], y[j], t);
-    y[i] = t / L[i * ld + i];
-    f.fma(i);
-    f.op(1);
-  }
-}
-
-// linalgebra/interface/substitution.hpp:34-50 (L^T x = y)
-template <bool C>
-__device__ __forceinline__ void bwd(const double* L, int ld, const double* y, double* x, int n, Counter<C>& f) {
-  for (int i = n - 1; i >= 0; --i) {
-    double t = y[i];
-    for (int j = i + 1; j < n; ++j) t = fma(-L[j * ld + i], x[j], t);
-    x[i] = t / L[i * ld + i];
-    f.fma(n - 1 - i);
-    f.op(1);
-  }
-}
-
-// linalgebra/interface/fused_cholesky_substitution.hpp:18-59
-template <bool C>
-__device__ __forceinline__ void rc_add(const double* M, double* L, int ld, const double* b, double* y, int view,
-                                       Counter<C>& f) {
-  const int row = view - 1;
-  double sum = 0, total = b[row];
-  for (int col = 0; col < row; ++col) {
-    double s2 = 0;
-    for (int j = 0; j < col; ++j) s2 = fma(L[row * ld + j], L[col * ld + j], s2);
-    const double v = (M[row * ld + col] - s2) / L[col * ld + col];
-    total = fma(-v, y[col], total);
-    sum = fma(v, v, sum);
-    L[row * ld + col] = v;
-    f.fma(col + 3);
-    f.op(2);
-  }
-  const double d = sqrt(M[row * ld + row] - sum);
-  L[row * ld + row] = d;
-  y[row] = total / d;
-  f.op(3);
-}
-
-// linalgebra/interface/fused_cholesky_substitution.hpp:64-102
-template <bool C>
-__device__ __forceinline__ void inbetween_removal(const double* M, double* L, int ld, const double* b, double* y,
-                                                  int pos, int view, Counter<C>& f) {
-  for (int i = pos; i < view; ++i) {
-    double sumsq = 0, total = b[i];
-    for (int j = 0; j < i; ++j) {
-      double s2 = 0;
-      for (int k = 0; k < j; ++k) s2 = fma(L[i * ld + k], L[j * ld + k], s2);
-      const double v = (M[i * ld + j] - s2) / L[j * ld + j];
-      L[i * ld + j] = v;
-      total = fma(-v, y[j], total);
-      sumsq = fma(v, v, sumsq);
-      f.fma(j + 2);
-      f.op(2);
-    }
-    const double d = sqrt(M[i * ld + i] - sumsq);
-    L[i * ld + i] = d;
-    y[i] = total / d;
-    f.op(3);
-  }
-}
-
-__device__ __forceinline__ void swap_d(double& a, double& b) {
-  const double t = a;
-  a = b;
-  b = t;
-}
-
-__device__ __forceinline__ void swap_sym(double* M, int ld, int n, int a, int b) {
-  if (a == b) return;
-  for (int k = 0; k < n; ++k) swap_d(M[k * ld + a], M[k * ld + b]);
-  for (int k = 0; k < n; ++k) swap_d(M[a * ld + k], M[b * ld + k]);
-}
-
-struct FnnlsOut {
-  int outer, inner, converged;
-  uint16_t mask;
-};
-
-// FNNLS, nnls/src/inplace_fnnls.cu:72-233 with the incremental factor.
-// A: N x K column-major, b: N, x: K warm start in / solution out.
-// start 0: the reference's start (empty passive set, warm x);
-// start 1: passive set seeded with the support of the warm x (ascending).
-template <int NT, int KT, bool C>
-__device__ void fnnls(const double* A, const double* b, double* x, int N, int K, double eps, int max_iter,
-                      int start, FnnlsOut& o, Counter<C>& f) {
-  if (NT > 0) N = NT;
-  if (KT > 0) K = KT;
-  double AtA[KMAX * KMAX], Atb[KMAX], s[KMAX], L[KMAX * KMAX], y[KMAX];
-  int8_t perm[KMAX];
-  const int ld = KMAX;
-  for (int i = 0; i < K; ++i) {
-    for (int j = i; j < K; ++j) {
-      double acc = 0;
-      for (int k = 0; k < N; ++k) acc = fma(A[i * N + k], A[j * N + k], acc);
-      AtA[j * ld + i] = acc;
-      AtA[i * ld + j] = acc;
-      f.fma(N);
-    }
-  }
-  for (int i = 0; i < K; ++i) {
-    double acc = 0;
-    for (int k = 0; k < N; ++k) acc = fma(A[i * N + k], b[k], acc);
-    Atb[i] = acc;
-    f.fma(N);
-  }
-  for (int i = 0; i < K; ++i) perm[i] = int8_t(i);
-
-  int nP = 0, outer = 0, inner = 0, converged = 0;
-
-  auto swap_in = [&](int p, int q) {
-    swap_sym(AtA, ld, K, p, q);
-    swap_d(Atb[p], Atb[q]);
-    swap_d(x[p], x[q]);
-    const int8_t t = perm[p];
-    perm[p] = perm[q];
-    perm[q] = t;
-  };
-
-  // inner loop; `added` rows were just appended to the passive block
-  auto inner_loop = [&](int added) {
-    int inner_iteration = 0, position_removed = -1;
-    while (nP > 0) {
-      ++inner;
-      if (nP == 1) {
-        const double l00 = sqrt(AtA[0]);
-        L[0] = l00;
-        y[0] = Atb[0] / l00;
-        position_removed = -1;
-        f.op(2);
-      } else if (inner_iteration == 0) {
-        for (int r = nP - added + 1; r <= nP; ++r) {
-          if (r == 1) {
-            const double l00 = sqrt(AtA[0]);
-            L[0] = l00;
-            y[0] = Atb[0] / l00;
-            f.op(2);
-          } else {
-            rc_add(AtA, L, ld, Atb, y, r, f);
-          }
-        }
-      } else {
-        inbetween_removal(AtA, L, ld, Atb, y, position_removed, nP, f);
-      }
-      bwd(L, ld, y, s, nP, f);
-
-      double smin = s[0];
-      for (int i = 1; i < nP; ++i) smin = (s[i] < smin) ? s[i] : smin;
-      if (smin > 0.) {
-        for (int i = 0; i < nP; ++i) x[i] = s[i];
-        break;
-      }
-      double alpha = DBL_MAX;
-      int alpha_idx = 0;
-      for (int i = 0; i < nP; ++i) {
-        if (s[i] <= 0.) {
-          const double ratio = x[i] / (x[i] - s[i]);
-          f.op(2);
-          if (ratio < alpha) {
-            alpha = ratio;
-            alpha_idx = i;
-          }
-        }
-      }
-      if (alpha == DBL_MAX) {
-        for (int i = 0; i < nP; ++i) x[i] = s[i];
-        break;
-      }
-      for (int i = 0; i < nP; ++i) x[i] = fma(alpha, s[i] - x[i], x[i]);
-      f.fma(nP);
-      f.op(nP);
-      x[alpha_idx] = 0;
-      --nP;
-      swap_in(nP, alpha_idx);
-      position_removed = alpha_idx;
-      ++inner_iteration;
-    }
-  };
-
-  if (start == 1) {
-    // columns with x_k > 0 and a non-zero whitened norm (the MINOS refits
-    // zero the in-time column and hold its amplitude fixed)
-    for (int k = 0; k < K; ++k)
-      if (x[k] > 0. && AtA[k * ld + k] > 0.) swap_in(nP++, k);
-    if (nP > 0) inner_loop(nP);
-  }
-
-  for (int iter = 0; iter < max_iter; ++iter) {
-    if (nP == K) {
-      converged = 1;
-      break;
-    }
-    int imax = nP;
-    double wmax = 0;
-    for (int i = nP; i < K; ++i) {
-      double acc = 0;
-      for (int j = 0; j < K; ++j) acc = fma(AtA[i * ld + j], x[j], acc);
-      const double w = Atb[i] - acc;
-      f.fma(K);
-      f.op(1);
-      if (i == nP || w > wmax) {
-        wmax = w;
-        imax = i;
-      }
-    }
-    if (wmax < eps) {
-      converged = 1;
-      break;
-    }
-    ++outer;
-    swap_in(nP, imax);
-    ++nP;
-    inner_loop(1);
-  }
-  double xo[KMAX];
-  for (int i = 0; i < K; ++i) xo[perm[i]] = x[i];
-  uint16_t mask = 0;
-  for (int i = 0; i < nP; ++i) mask |= uint16_t(1u << perm[i]);
-  for (int i = 0; i < K; ++i) x[i] = xo[i];
-  o.outer += outer;
-  o.inner += inner;
-  o.converged = converged;
-  o.mask = mask;
-}
-
-// Per-channel state of PulseChiSqSNNLS (multifit_cpu/interface/PulseChiSqSNNLS.h:44-58).
-struct FitState {
-  double samp[KMAX];
-  double amp[KMAX];
-  double P[KMAX * KMAX];  // column-major N x K
-  double LC[KMAX * KMAX]; // row-major lower factor of the covariance, ld = KMAX
-  double chisq;
-  FnnlsOut st;
-  int outer_iters;
-  int outer_maxed;
-};
-
-// updateCov, multifit_cpu/src/PulseChiSqSNNLS.cpp:169-194
-template <int NT, int KT, bool C>
-__device__ void update_cov(const DevConditions& c, int N, int K, double pederr, FitState& S, Counter<C>& f) {
-  double M[KMAX * KMAX];
-  const double ped2 = pederr * pederr;
-  f.op(1);
-  for (int i = 0; i < N; ++i)
-    for (int j = 0; j <= i; ++j) M[i * KMAX + j] = ped2 * c.R[j * N + i];
-  f.op(N * (N + 1) / 2);
-  if (c.has_fpc) {
-    const int NF = N + 9;
-    for (int k = 0; k < K; ++k) {
-      if (S.amp[k] == 0.) continue;
-      const int bx = c.bxs[k];
-      const int first = bx + 3 > 0 ? bx + 3 : 0;
-      const int offset = 7 - 3 - bx;
-      const double ampsq = S.amp[k] * S.amp[k];
-      const int ns = N - first;
-      for (int a = 0; a < ns; ++a)
-        for (int cc = 0; cc <= a; ++cc) {
-          const int i = first + a, j = first + cc;
-          M[i * KMAX + j] = fma(ampsq, c.fpc[(j + offset) * NF + (i + offset)], M[i * KMAX + j]);
-        }
-      f.op(1);
-      f.fma(ns * (ns + 1) / 2);
-    }
-  }
-  chol_rows(M, S.LC, KMAX, 0, N, f);
-}
-
-// ComputeChiSq, multifit_cpu/src/PulseChiSqSNNLS.cpp:196-200
-template <bool C>
-__device__ double compute_chisq(int N, int K, const FitState& S, Counter<C>& f) {
-  double r[KMAX], z[KMAX];
-  for (int i = 0; i < N; ++i) {
-    double acc = 0;
-    for (int k = 0; k < K; ++k) acc = fma(S.P[k * N + i], S.amp[k], acc);
-    r[i] = acc - S.samp[i];
-  }
-  f.fma(N * K);
-  f.op(N);
-  fwd(S.LC, KMAX, r, z, N, f);
-  double c = 0;
-  for (int i = 0; i < N; ++i) c = fma(z[i], z[i], c);
-  f.fma(N);
-  return c;
-}
-
-// NNLS + Minimize, multifit_cpu/src/PulseChiSqSNNLS.cpp:149-166, 219-273.
-// `lanes` = the lanes of the warp that run this call together. The outer
-// iterations are warp-uniform (a ballot at the loop head), and the lanes
-// reconverge after the divergent FNNLS: on this GPU an FP64 warp instruction
-// costs the full pipe time whatever the number of active lanes, so the
-// covariance factor, the whitening and chi2 must be issued once for all lanes
-// rather than once per group of lanes that left FNNLS together.
-template <int NT, int KT, bool C>
-__device__ void minimize(const DevConditions& c, const DevOptions& o, int N, int K, double pederr, FitState& S,
-                         Counter<C>& f, unsigned lanes) {
-  bool done = false;
-  for (int it = 0;; ++it) {
-    const bool run = !done && it < o.max_iter_outer;
-    const unsigned act = __ballot_sync(lanes, run);
-    if (act == 0u) break;
-    if (!run) continue;
-    update_cov<NT, KT>(c, N, K, pederr, S, f);
-    double A[KMAX * KMAX], b[KMAX];
-    for (int k = 0; k < K; ++k) fwd(S.LC, KMAX, S.P + k * N, A + k * N, N, f);
-    fwd(S.LC, KMAX, S.samp, b, N, f);
-    fnnls<NT, KT>(A, b, S.amp, N, K, o.nnls_eps, o.max_iter_nnls, o.nnls_start, S.st, f);
-    __syncwarp(act);
-    const double now = compute_chisq(N, K, S, f);
-    const double delta = now - S.chisq;
-    f.op(1);
-    S.chisq = now;
-    ++S.outer_iters;
-    if (fabs(delta) < o.dchi2_tol) done = true;
-  }
-  if (!done) S.outer_maxed = 1;
-}
-
-// ComputeApproxUncertainty, multifit_cpu/src/PulseChiSqSNNLS.cpp:202-207
-template <bool C>
-__device__ double approx_uncertainty(int N, const FitState& S, int k, Counter<C>& f) {
-  double z[KMAX];
-  fwd(S.LC, KMAX, S.P + k * N, z, N, f);
-  double n2 = 0;
-  for (int i = 0; i < N; ++i) n2 = fma(z[i], z[i], n2);
-  f.fma(N);
-  f.op(2);
-  return 1. / sqrt(n2);
-}
-
-// DoFit, multifit_cpu/src/PulseChiSqSNNLS.cpp:21-147
+// DoFit with the FP64 Minimize: the plain drop-in.
 template <int NT, int KT, bool C>
 __device__ void dofit(const FitArgs& a, const DevConditions& c, int64_t ch, unsigned lanes) {
   const int N = NT > 0 ? NT : c.N;
   const int K = KT > 0 ? KT : c.K;
   Counter<C> f;
-  FitState S;
-  const double* in = a.samples + ch * a.sample_stride;
-  const double pederr = a.pederr[ch];
-  bool bad = !isfinite(pederr);
-  for (int i = 0; i < N; ++i) {
-    S.samp[i] = in[i];
-    bad = bad || !isfinite(S.samp[i]);
-  }
-  for (int k = 0; k < K; ++k)
-    for (int i = 0; i < N; ++i) S.P[k * N + i] = c.P[k * N + i];
-  for (int k = 0; k < K; ++k) S.amp[k] = 0.;
-  S.chisq = 0.;
-  S.st = FnnlsOut{0, 0, 0, 0};
-  S.outer_iters = 0;
-  S.outer_maxed = 0;
-
-  minimize<NT, KT>(c, a.opt, N, K, pederr, S, f, lanes);
-  const FnnlsOut main_st = S.st;
-  const int main_outer = S.outer_iters;
-  const int main_maxed = S.outer_maxed;
-  double ampmin[KMAX];
-  for (int k = 0; k < K; ++k) ampmin[k] = S.amp[k];
-  double err = 0.;
-
-  if (a.opt.compute_errors && c.intime_col >= 0) {
-    const int kin = c.intime_col;
-    const double approxerr = approx_uncertainty(N, S, kin, f);
-    const double chisq0 = S.chisq;
-    const double x0 = ampmin[kin];
-    double pulse_in[KMAX];
-    for (int i = 0; i < N; ++i) {
-      pulse_in[i] = S.P[kin * N + i];
-      S.P[kin * N + i] = 0.;
-    }
-    const double xplus = x0 + approxerr;
-    S.amp[kin] = xplus;
-    for (int i = 0; i < N; ++i) S.samp[i] = fma(-xplus, pulse_in[i], in[i]);
-    minimize<NT, KT>(c, a.opt, N, K, pederr, S, f, lanes);
-    const double chip = compute_chisq(N, K, S, f);
-    const double sigmaplus = fabs(xplus - x0) / sqrt(chip - chisq0);
-    const bool lower = x0 / sigmaplus > 0.5;
-    const unsigned lanes2 = __ballot_sync(lanes, lower);
-    if (lower) {
-      const double xminus = (x0 - approxerr) > 0. ? (x0 - approxerr) : 0.;
-      S.amp[kin] = xminus;
-      for (int i = 0; i < N; ++i) S.samp[i] = fma(-xminus, pulse_in[i], in[i]);
-      minimize<NT, KT>(c, a.opt, N, K, pederr, S, f, lanes2);
-      const double chim = compute_chisq(N, K, S, f);
-      const double sigmaminus = fabs(xminus - x0) / sqrt(chim - chisq0);
-      err = 0.5 * (sigmaplus + sigmaminus);
-    } else {
-      err = sigmaplus;
-    }
-    S.chisq = chisq0;
-  }
-
-  double* out = a.amplitudes + ch * a.amp_stride;
-  bool finite = isfinite(S.chisq);
-  for (int k = 0; k < K; ++k) {
-    out[k] = ampmin[k];
-    finite = finite && isfinite(ampmin[k]);
-  }
-  for (int k = K; k < a.amp_stride && k < KMAX; ++k) out[k] = 0.;
-  a.chi2[ch] = S.chisq;
-  if (a.intime) a.intime[ch] = c.intime_col >= 0 ? ampmin[c.intime_col] : 0.;
-  if (a.errors) a.errors[ch] = err;
-  if (a.active_mask) {
-    // support of X(): the last FNNLS call restarts from an empty passive set
-    // and usually stops at once, so its passive set is not the fitted set
-    uint16_t support = 0;
-    for (int k = 0; k < K; ++k)
-      if (ampmin[k] > 0.) support |= uint16_t(1u << k);
-    a.active_mask[ch] = support;
-  }
-  if (a.status) {
-    uint8_t st = 0;
-    if (!main_st.converged) st |= CH_NNLS_MAXITER;
-    if (main_maxed) st |= CH_OUTER_MAXITER;
-    if (!finite) st |= CH_NONFINITE;
-    if (bad) st |= CH_BADINPUT;
-    a.status[ch] = st;
-  }
-  if (a.iters) {
-    const int o8 = main_outer < 255 ? main_outer : 255;
-    const int fo = main_st.outer < 4095 ? main_st.outer : 4095;
-    const int fi = main_st.inner < 4095 ? main_st.inner : 4095;
-    a.iters[ch] = o8 | (fo << 8) | (fi << 20);
-  }
-  if (C && a.flops) a.flops[ch] = f.f.v;
+  dofit_with<NT, KT, C>(a, c, ch, lanes, f, [&](FitState<double>& S, double pederr, unsigned ln) {
+    minimize<NT, KT>(c, a.opt, N, K, pederr, S, f, ln);
+  });
 }
 
 // One launch per condition set (lanes of other sets idle); out-of-range set

@@ -82,6 +82,9 @@ struct LaunchTimer {
   }
 };
 
+// Per-channel form of the mixed and FP32 precisions (fit_cov.cu): FP32 outer
+// loop, then FP64 from its result.
+cudaError_t launch_fit_cov(const FitArgs& a, int block, cudaStream_t s, bool instrumented, LaunchTimer* tm);
 cudaError_t launch_fit_fp64(const FitArgs& a, int block, cudaStream_t s, bool instrumented,
                             LaunchTimer* tm = nullptr);
 
@@ -104,6 +107,7 @@ struct HostTables {
   std::vector<double> pinv64;
   std::vector<float> pinv32;
   std::vector<float> pinv32lo;        // pinv64 = pinv32 + pinv32lo to ~2^-48
+  std::vector<float> pinv2;           // element e as the pair (pinv32[e], pinv32lo[e]) at [2e], [2e + 1]
 };
 int build_mixed_tables(const DevConditions& c, HostTables* t);
 
@@ -127,6 +131,7 @@ struct DevMixed {
   const double* pinv64;
   const float* pinv32;
   const float* pinv32lo;
+  const float* pinv2;  // (hi, lo) pairs; a row of an even N starts on 16 bytes
 };
 
 struct MixedArgs {

@@ -706,7 +706,8 @@ __device__ __forceinline__ void judge_df_body(const MixedArgs& a, const DevMixed
     }
   }
   // x = G_S^+ y through the table's float pairs (rows outside the set read the
-  // zero row), with dx[k] = sum_i |G^+_ki y_i|, the scale of x_k's round-off
+  // zero row), with dx[k] = sum_i |G^+_ki y_i|, the scale of x_k's round-off.
+  // A row's (hi, lo) pairs come two elements per 16-byte load when N is even.
   float xh[K], xl[K], dx[K];
   {
     const int off = __ldg(T.offset + m);
@@ -717,11 +718,24 @@ __device__ __forceinline__ void judge_df_body(const MixedArgs& a, const DevMixed
       const int row = inset ? off + r * N : T.zero_row;
       r += inset ? 1 : 0;
       float hi = 0.f, lo = 0.f, mag = 0.f;
+      if constexpr (N % 2 == 0) {
+        const float4* rp = reinterpret_cast<const float4*>(T.pinv2 + 2 * row);
 #pragma unroll
-      for (int i = 0; i < N; ++i) {
-        const float ph = __ldg(T.pinv32 + row + i);
-        df_fma(hi, lo, ph, __ldg(T.pinv32lo + row + i), yh[i], yl[i]);
-        mag = fmaf(fabsf(ph), fabsf(yh[i]), mag);
+        for (int i = 0; i < N; i += 2) {
+          const float4 q = __ldg(rp + i / 2);
+          df_fma(hi, lo, q.x, q.y, yh[i], yl[i]);
+          mag = fmaf(fabsf(q.x), fabsf(yh[i]), mag);
+          df_fma(hi, lo, q.z, q.w, yh[i + 1], yl[i + 1]);
+          mag = fmaf(fabsf(q.z), fabsf(yh[i + 1]), mag);
+        }
+      } else {
+        const float2* rp = reinterpret_cast<const float2*>(T.pinv2 + 2 * row);
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          const float2 q = __ldg(rp + i);
+          df_fma(hi, lo, q.x, q.y, yh[i], yl[i]);
+          mag = fmaf(fabsf(q.x), fabsf(yh[i]), mag);
+        }
       }
       xh[k] = hi;
       xl[k] = lo;

@@ -167,6 +167,14 @@ int build_mixed_tables(const DevConditions& c, HostTables* t) {
       t->pinv32lo[t->offset[m] + e] = float(pinv[e] - ld(t->pinv32[t->offset[m] + e]));
     }
   }
+  // the same operators as (hi, lo) pairs, for the double-float solve: with N
+  // even every row (offset[m] + r N elements, 8 bytes each) starts on a
+  // 16-byte boundary, so a row is N / 2 16-byte loads
+  t->pinv2.assign(2 * size_t(total + N), 0.0f);
+  for (int e = 0; e < total + N; ++e) {
+    t->pinv2[2 * size_t(e)] = t->pinv32[e];
+    t->pinv2[2 * size_t(e) + 1] = t->pinv32lo[e];
+  }
   return MF_OK;
 }
 

@@ -99,22 +99,6 @@ def test_mixed_matches_fp64_gpu_path(mf, cuda, prec):
     eng.close()
 
 
-def test_mixed_rejects_unsupported(mf, cuda):
-    eng = mf.Engine(0)
-    cond, _ = mf.synth_conditions(mf.SYNTH_ECAL)
-    eng.set_conditions(0, cond)
-    s = np.zeros((2, 10))
-    with pytest.raises(mf.MultifitError):
-        eng.fit_host(s, np.full(2, 0.044), options=mf.default_options(precision=mf.PREC_MIXED, compute_errors=1))
-    P, R, bxs, _ = mf.conditions_arrays(cond)
-    F = np.zeros((19, 19))
-    F[7:, 7:] = 1e-6
-    eng.set_conditions(0, mf.make_conditions(P, R, bxs, F))
-    with pytest.raises(mf.MultifitError):
-        eng.fit_host(s, np.full(2, 0.044), options=mf.default_options(precision=mf.PREC_MIXED))
-    eng.close()
-
-
 def test_profile_counts_and_times_every_launch(mf, cuda):
     """mf_profile: one record per kernel launch on the fit's stream, with
     positive device times, for the mixed form on two condition sets and for
