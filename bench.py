@@ -173,9 +173,9 @@ FORM_DESC = {
     "fp32": "FP32: FP32 active-set search + double-float screen and judge (FP32 error-free transforms), "
             "FP64 repair of the rare rejects, KKT-converged",
     "warm": "learned warm start: BF16 tensor-core MLP + the FP32 form (double-float judge) to KKT",
-    "fp32-cov": "per-channel FP32 form (a pulse covariance makes the covariance amplitude-dependent): each "
-                "Minimize's outer loop in FP32, then FP64 from its result (one FP64 covariance factor, refinement "
-                "solve and chi2 when the FP32 fit was right), KKT-converged",
+    "fp32-cov": "per-channel form of the FP32 precision (a pulse covariance makes the covariance "
+                "amplitude-dependent): the outer loop's first iteration through the passive-set tables (FP32 "
+                "search, double-float judge), then the FP64 fit from it, KKT-converged",
 }
 # the pulse covariance of the fp32-cov workload: 1e-4 exp(-|i-j| / 3) over the
 # template's samples 7..18 of the 19-sample fullpulse (a pulse-shape jitter)
@@ -193,6 +193,14 @@ def pulse_covariance():
 
 def default_workload(form: str) -> str:
     return {"fp64": "ecal-1m-pu2", "fp32-cov": "ecal-1m-pu2"}.get(form, "warm-eval-10m")
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per channel of a
+# launch, measured by ncu on the kernel of the form named (a capture of one
+# 2,097,152-channel chunk; the bytes grow with the channels, so a launch's
+# traffic is this times its channels); the summary with the command is the
+# profiles/ file given
+NCU_DRAM_BYTES_PER_CHANNEL = {
+    ("judge_kernel", "warm"): (194.1, "profiles/judge_kernel_fp32_warm-2m.md"),
+}
 # useful FLOPs of one warm-start prediction: 12 inputs -> 128 -> 128 -> 20
 # outputs, 2 per multiply-add (the network pads to 16 inputs and 32 outputs)
 MLP_FLOPS_PER_CHANNEL = 2 * (12 * 128 + 128 * 128 + 128 * 20)
@@ -575,7 +583,7 @@ def run_ours(args, world, rank, local):
             "vs_baseline": None,
             "dtype": {"fp64": "f64", "mixed": "f32+f64", "fp32": "f32 (double-float judge; f64 repair)",
                       "warm": "f32 (double-float judge; f64 repair; bf16 MLP)",
-                      "fp32-cov": "f32 outer loop; f64 final iteration"}[args.form],
+                      "fp32-cov": "f32 first iteration (double-float judge); f64 from the second"}[args.form],
             "data": "synthetic (seeded Philox generator; the workload's shapes and value distributions)",
             "config": workload_config(args, wl, n, world),
             "engine": {
@@ -642,21 +650,29 @@ def kernel_rooflines(mf, eng, kernels, args, n, ctype, plain_flops, form_fp64_fl
         N, K = c.nsamples, c.npulses
         judge += m * (N * (N + 1) + 4 * N * K)
         judge_df += m * judge_df_flops(mf.conditions_arrays(c)[0])
-    df_form = args.form in ("fp32", "warm")
+    df_form = args.form in ("fp32", "warm", "fp32-cov")
     warm = args.form == "warm"
     out = {}
     for name, (launches, total) in kernels.items():
         per_step = launches / args.steps
         ms = total / args.steps
         mean_s = total / launches * 1e-3
-        if name == "fit_fp64_kernel":
-            work, bound, peak, unit = plain_flops / per_step, "fp64", fp64_peak, "TFLOP/s"
-        elif name == "fit_cov_kernel":  # its FP64 phase's counted flops (the FP32 phase is not FP64 work)
+        if name == "fit_fp64_kernel" and args.form == "fp32-cov":
+            # the per-channel form's FP64 continuation: its own counted FP64 flops
             work, bound, peak, unit = form_fp64_flops / per_step, "fp64", fp64_peak, "TFLOP/s"
+        elif name == "fit_fp64_kernel":
+            work, bound, peak, unit = plain_flops / per_step, "fp64", fp64_peak, "TFLOP/s"
         elif name == "judge_kernel" and df_form:
             work, bound, peak, unit = judge_df / per_step, "fp32", fp32_peak, "TFLOP/s"
         elif name == "judge_kernel":
             work, bound, peak, unit = judge / per_step, "fp64", fp64_peak, "TFLOP/s"
+        elif name == "repair_kernel" and args.form == "fp32-cov":
+            # the per-channel form's FP64 count is its continuation's: the repair's is not counted
+            # apart -- time and share without a roofline
+            out[name] = {"bound": None, "achieved": None, "peak": None, "unit": None, "frac": None,
+                         "traffic": None, "launches_per_step": per_step, "ms_per_step": ms,
+                         "share": ms / step_ms, "work_per_launch": None, "peak_source": None}
+            continue
         elif name == "repair_kernel":
             # the FP64 judge's share of the counted FP64 flops belongs to the judge (its repairs redo it)
             rest = form_fp64_flops - (0.0 if df_form else judge)
@@ -681,8 +697,13 @@ def kernel_rooflines(mf, eng, kernels, args, n, ctype, plain_flops, form_fp64_fl
             work = n * (10 * 8 + 8 + (2 + 40 if warm else 0) + 2 + 2 + 40) / per_step
             bound, peak, unit = "hbm", peaks["hbm_gbs"], "GB/s"
         achieved = work / mean_s / (1e12 if unit == "TFLOP/s" else 1e9)
+        measured = NCU_DRAM_BYTES_PER_CHANNEL.get((name, args.form))
         out[name] = {"bound": bound, "achieved": achieved, "peak": peak, "unit": unit, "frac": achieved / peak,
-                     "traffic": None, "launches_per_step": per_step, "ms_per_step": ms,
+                     "traffic": measured[0] * n / per_step if measured else None,
+                     "traffic_unit": "bytes per launch" if measured else None,
+                     "traffic_source": f"{measured[1]} ({measured[0]} B/channel x channels per launch)"
+                     if measured else None,
+                     "launches_per_step": per_step, "ms_per_step": ms,
                      "share": ms / step_ms, "work_per_launch": work,
                      "peak_source": ("cuBLAS DGEMM 4096^3 measured in this run (FP64 pipe)" if bound == "fp64"
                                      else "cuBLAS SGEMM 8192^3, TF32 off, measured in this run (FP32 pipe)"

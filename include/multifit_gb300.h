@@ -67,13 +67,13 @@ enum mf_channel_status {
 
 /* Arithmetic of the fit. MF_PREC_MIXED and MF_PREC_FP32 return each channel's
  * NNLS optimum (KKT point) within 1e-4 of the FP64 fit run to convergence.
- * They fit through the passive-set tables of a condition set when it has them
- * (no pulse covariance, N = K = 10 or 8) and errors are off; otherwise the
- * whole batch takes the per-channel form: each Minimize runs its outer chi2
- * loop in FP32 (covariance, Cholesky, whitening, FNNLS), then continues in
- * FP64 from that result (one FP64 covariance factor, refinement solve and
- * chi2 when the FP32 fit was right; more FP64 iterations when not), on the
- * grid schedule and from a cold start. */
+ * With no pulse covariance and errors off they fit through the passive-set
+ * tables of the condition set (N = K = 10 or 8). Otherwise the batch takes
+ * the per-channel form: the outer chi2 loop's first iteration (covariance
+ * pederr^2 samplecor, the tables' problem) through the tables, then the FP64
+ * fit from its amplitudes and chi2 -- the amplitude-dependent covariance, the
+ * FNNLS from their support, the stopping rule, the MINOS-like refits -- on the
+ * grid schedule. Shapes without tables are fitted in FP64 throughout. */
 enum mf_precision {
   MF_PREC_FP64 = 0,  /* plain FP64, bit-identical to the CPU oracle's canonical order */
   MF_PREC_MIXED = 1, /* FP32 search and screen; FP64 refinement solve, residual and chi2 (the judge) */
@@ -236,8 +236,7 @@ enum mf_kernel_kind {
   MF_K_REJUDGE = 6,   /* judge_fixed_kernel / judge_fixed_persist: the judge of the channels the fix changed */
   MF_K_FIX = 7,       /* fix_kernel / fix_persist: FP32 FNNLS step of the channels queued for it */
   MF_K_SCREEN = 8,    /* screen_kernel / screen_persist: FP32 double-float KKT screen (cold starts) */
-  MF_K_FIT_COV = 9,   /* fit_cov_kernel: per-channel form (pulse covariance, errors, shapes without tables) */
-  MF_K_COUNT = 10
+  MF_K_COUNT = 9
 };
 /* enable != 0 creates the context's event pool (and clears it); 0 frees it. */
 int mf_profile(mf_context* ctx, int enable);

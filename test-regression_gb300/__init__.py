@@ -118,7 +118,7 @@ class MfMlpTrainParams(C.Structure):
 NOALLOC_MAX_CHANNELS = 131072  # MF_NOALLOC_MAX_CHANNELS
 # mf_kernel_kind: the kernels mf_profile times
 KERNEL_KINDS = ("fit_fp64_kernel", "mlp_infer_tc_kernel", "search_kernel", "judge_kernel", "repair_kernel",
-                "partition_kernel", "judge_fixed_kernel", "fix_kernel", "screen_kernel", "fit_cov_kernel")
+                "partition_kernel", "judge_fixed_kernel", "fix_kernel", "screen_kernel")
 
 SIGNATURES = [
     ("mf_abi_version", C.c_int, []),

@@ -196,6 +196,7 @@ int fill_args(mf_context* ctx, const mf_batch* b, const mf_options* o, FitArgs* 
   a->status = b->status;
   a->iters = b->iters;
   a->flops = nullptr;
+  a->seeded = 0;
   return MF_OK;
 }
 
@@ -356,29 +357,52 @@ int dispatch_mixed(mf_context* c, const FitArgs& a, const mf_options* o, cudaStr
 }
 
 // The mixed and FP32 precisions fit a batch through the passive-set tables
-// when every condition set it uses has them and no errors are asked for;
-// otherwise (a pulse covariance makes the covariance depend on the channel's
-// amplitudes, the MINOS-like errors refit with a constrained column, or a
-// shape has no tables) through the per-channel form, on the grid schedule
-// and from a cold start (the learned warm start seeds the table search only).
+// alone when every condition set it uses has them, none has a pulse
+// covariance and no errors are asked for. Otherwise they take the per-channel
+// form: with the amplitudes at zero, the reference's first outer iteration
+// (PulseChiSqSNNLS.cpp:149-166) fits with the covariance pederr^2 samplecor --
+// exactly the tables' problem -- so that iteration (the costly one: its FNNLS
+// starts from an empty passive set) runs through the tables, and the FP64 fit
+// continues the outer loop from it: the covariance built from those
+// amplitudes (with the pulse covariance), FNNLS from their support, the
+// stopping rule against their chi2, then the MINOS-like refits. The result
+// follows the FP64 trajectory from the second iteration on. Sets without
+// tables (shapes other than N = K = 10 or 8) run the whole loop in FP64.
+int dispatch_per_channel(mf_context* c, const FitArgs& a, const mf_options* o, cudaStream_t s, bool instrumented,
+                         bool allow_graph, int lane) {
+  bool tables = true;
+  for (int t = 0; t < a.n_ctypes; ++t)
+    if (!c->tab_ok[t]) tables = false;
+  FitArgs a64 = a;
+  a64.opt.nnls_start = MF_START_SUPPORT;
+  a64.opt.max_iter_nnls = o->max_iter_nnls > 0 ? o->max_iter_nnls : 1;
+  if (tables) {
+    mf_options first = *o;
+    first.compute_errors = 0;
+    const int rc = dispatch_mixed(c, a, &first, s, allow_graph, lane);
+    if (rc) return rc;
+    a64.seeded = 1;
+  }
+  const int block = o->block_size && o->block_size <= 128 ? o->block_size : 128;
+  const cudaError_t e = launch_fit_fp64(a64, block, s, instrumented, &c->timer);
+  if (e != cudaSuccess) {
+    set_last_error("per-channel fit launch", e);
+    return MF_ECUDA;
+  }
+  return MF_OK;
+}
+
 bool per_channel_form(const mf_context* c, const FitArgs& a, const mf_options* o) {
   if (o->compute_errors) return true;
   for (int t = 0; t < a.n_ctypes; ++t)
-    if (!c->tab_ok[t]) return true;
+    if (!c->tab_ok[t] || c->cond[t].has_fpc) return true;
   return false;
 }
 
 int dispatch_form(mf_context* c, const FitArgs& a, const mf_options* o, cudaStream_t s, bool instrumented,
                   bool allow_graph, int lane) {
-  if ((o->precision == MF_PREC_MIXED || o->precision == MF_PREC_FP32) && per_channel_form(c, a, o)) {
-    const int block = o->block_size && o->block_size <= 128 ? o->block_size : 128;
-    const cudaError_t e = launch_fit_cov(a, block, s, instrumented, &c->timer);
-    if (e != cudaSuccess) {
-      set_last_error("per-channel fit launch", e);
-      return MF_ECUDA;
-    }
-    return MF_OK;
-  }
+  if ((o->precision == MF_PREC_MIXED || o->precision == MF_PREC_FP32) && per_channel_form(c, a, o))
+    return dispatch_per_channel(c, a, o, s, instrumented, allow_graph, lane);
   if (o->precision == MF_PREC_MIXED || o->precision == MF_PREC_FP32)
     return dispatch_mixed(c, a, o, s, allow_graph, lane);
   if (o->precision != MF_PREC_FP64 || o->schedule != MF_SCHED_GRID || o->warm_start != MF_WARM_NONE)
@@ -472,15 +496,16 @@ void free_tables(mf_context* c, int t) {
   c->tab_ok[t] = 0;
 }
 
-// Builds the mixed-form tables of set t and uploads them. A set the mixed form
-// cannot serve (pulse covariance, K > N, a shape without a build, or a
-// non-positive-definite samplecor) keeps tab_ok = 0; mf_fit then reports
-// MF_EUNSUPPORTED for the mixed precision on it.
+// Builds the mixed-form tables of set t and uploads them. The tables depend on
+// the pulse matrix and samplecor only, so a set with a pulse covariance has
+// them too (they serve its first outer iteration). A set they cannot serve
+// (K > N, a shape without a build, or a non-positive-definite samplecor)
+// keeps tab_ok = 0; the mixed precision then fits it in FP64 throughout.
 int upload_tables(mf_context* c, int t) {
   free_tables(c, t);
   const DevConditions& d = c->cond[t];
   const bool shape_ok = (d.N == 10 && d.K == 10) || (d.N == 8 && d.K == 8);
-  if (d.has_fpc || !shape_ok) return MF_OK;
+  if (!shape_ok) return MF_OK;
   HostTables& h = c->tab[t];
   if (build_mixed_tables(d, &h) != MF_OK) return MF_OK;
   cudaError_t e = cudaSetDevice(c->device);
@@ -1151,7 +1176,7 @@ extern "C" int mf_fit_noalloc(mf_context* c, const mf_batch* b, const mf_options
     return MF_EINVAL;
   }
   for (int t = 0; t < a.n_ctypes; ++t)
-    if (!c->tab_ok[t]) {
+    if (!c->tab_ok[t] || c->cond[t].has_fpc) {
       std::snprintf(g_last_error, sizeof(g_last_error),
                     "mf_fit_noalloc: condition set %d has no passive-set tables (shape or pulse covariance)", t);
       return MF_EUNSUPPORTED;

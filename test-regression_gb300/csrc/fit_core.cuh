@@ -6,11 +6,10 @@
 // (nnls/src/inplace_fnnls.cu:72-233, nnls/src/inplace_fnnls_test_cholesky.cu:
 // 35-227), updateCov, ComputeChiSq, Minimize and ComputeApproxUncertainty.
 //
-// T = double is the plain FP64 drop-in (fit_fp64.cu, compiled --fmad=false:
-// every accumulation is an explicit fused multiply-add with the index
-// ascending, each triangular solve divides once by the diagonal, so the
-// kernel reproduces the CPU oracle bit for bit). T = float is the FP32 outer
-// loop of the per-channel form (fit_cov.cu).
+// With T = double this is the plain FP64 drop-in (fit_fp64.cu, compiled
+// --fmad=false: every accumulation is an explicit fused multiply-add with the
+// index ascending, each triangular solve divides once by the diagonal, so the
+// kernel reproduces the CPU oracle bit for bit).
 #pragma once
 #include <cfloat>
 
@@ -25,17 +24,10 @@ template <>
 struct Big<double> {
   static constexpr double value = DBL_MAX;
 };
-template <>
-struct Big<float> {
-  static constexpr float value = FLT_MAX;
-};
 
 __device__ __forceinline__ double fmaT(double a, double b, double c) { return fma(a, b, c); }
-__device__ __forceinline__ float fmaT(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ double sqrtT(double a) { return sqrt(a); }
-__device__ __forceinline__ float sqrtT(float a) { return sqrtf(a); }
 __device__ __forceinline__ double fabsT(double a) { return fabs(a); }
-__device__ __forceinline__ float fabsT(float a) { return fabsf(a); }
 
 struct Flop {
   double v;
@@ -278,16 +270,7 @@ __device__ void fnnls(const T* A, const T* b, T* x, int N, int K, T eps, int max
     for (int i = nP; i < K; ++i) {
       T acc = 0;
       for (int j = 0; j < K; ++j) acc = fmaT(AtA[i * ld + j], x[j], acc);
-      T w = Atb[i] - acc;
-      if constexpr (sizeof(T) == sizeof(float)) {
-        // FP32: w carries a round-off of up to ~K 2^-24 of |Atb_i| + sum_j
-        // |AtA_ij x_j|; what stays within 2^-17 of that scale counts as
-        // zero, so the loop does not chase round-off (the FP64 phase that
-        // follows settles those columns)
-        T mag = fabsT(Atb[i]);
-        for (int j = 0; j < K; ++j) mag = fmaT(fabsT(AtA[i * ld + j]), fabsT(x[j]), mag);
-        w -= T(0x1p-17) * mag;
-      }
+      const T w = Atb[i] - acc;
       f.fma(K);
       f.op(1);
       if (i == nP || w > wmax) {
@@ -326,6 +309,8 @@ struct FitState {
   FnnlsOut st;
   int outer_iters;
   int outer_maxed;
+  int first_iter;  // Minimize's first outer iteration (1 when the first was done elsewhere)
+  int first_done;  // ... and whether the stopping rule already held after it
 };
 
 // updateCov, multifit_cpu/src/PulseChiSqSNNLS.cpp:169-194
@@ -386,8 +371,8 @@ __device__ T compute_chisq(int N, int K, const FitState<T>& S, Counter<C>& f) {
 template <int NT, int KT, bool C, typename T>
 __device__ void minimize(const DevConditions& c, const DevOptions& o, int N, int K, T pederr, FitState<T>& S,
                          Counter<C>& f, unsigned lanes) {
-  bool done = false;
-  for (int it = 0;; ++it) {
+  bool done = S.first_done != 0;
+  for (int it = S.first_iter;; ++it) {
     const bool run = !done && it < o.max_iter_outer;
     const unsigned act = __ballot_sync(lanes, run);
     if (act == 0u) break;
@@ -423,8 +408,14 @@ __device__ T approx_uncertainty(int N, const FitState<T>& S, int k, Counter<C>& 
 // DoFit, multifit_cpu/src/PulseChiSqSNNLS.cpp:21-147, for channel ch of the
 // batch: the main Minimize, then (with errors on) the two constrained refits
 // of the in-time amplitude, and the outputs. mini(S, pederr, lanes) is the
-// Minimize the caller uses (the FP64 one of the drop-in, or the FP32-then-FP64
-// one of the per-channel form); it runs on the lanes given.
+// Minimize the caller uses; it runs on the lanes given.
+//
+// With a.seeded the main Minimize's first outer iteration has been done
+// already (the per-channel form of the mixed and FP32 precisions: with the
+// amplitudes at zero the covariance is pederr^2 samplecor, the problem of the
+// passive-set tables): its amplitudes and chi2 are read from the outputs and
+// the loop goes on from the second iteration, with the reference's stopping
+// rule against that chi2 (against 0 after the first iteration).
 template <int NT, int KT, bool C, typename Mini>
 __device__ void dofit_with(const FitArgs& a, const DevConditions& c, int64_t ch, unsigned lanes, Counter<C>& f,
                            Mini&& mini) {
@@ -445,8 +436,27 @@ __device__ void dofit_with(const FitArgs& a, const DevConditions& c, int64_t ch,
   S.st = FnnlsOut{0, 0, 0, 0};
   S.outer_iters = 0;
   S.outer_maxed = 0;
+  S.first_iter = 0;
+  S.first_done = 0;
+  if (a.seeded) {
+    const double* seed = a.amplitudes + ch * a.amp_stride;
+    const bool maxed = a.status && (a.status[ch] & CH_NNLS_MAXITER);
+    if (a.opt.compute_errors && fabs(a.chi2[ch]) < a.opt.dchi2_tol) {
+      // the loop stops at once: the error refits need the first iteration's
+      // covariance factor, that of pederr^2 samplecor
+      update_cov<NT, KT>(c, N, K, pederr, S, f);
+    }
+    for (int k = 0; k < K; ++k) S.amp[k] = seed[k];
+    S.chisq = a.chi2[ch];
+    S.st.converged = maxed ? 0 : 1;
+    S.outer_iters = 1;
+    S.first_iter = 1;
+    S.first_done = fabs(S.chisq) < a.opt.dchi2_tol ? 1 : 0;
+  }
 
   mini(S, pederr, lanes);
+  S.first_iter = 0;  // the error refits run their whole loop
+  S.first_done = 0;
   const FnnlsOut main_st = S.st;
   const int main_outer = S.outer_iters;
   const int main_maxed = S.outer_maxed;

@@ -52,6 +52,7 @@ struct FitArgs {
   uint8_t* status;
   int32_t* iters;
   double* flops;  // optional per-channel executed-flop count (instrumented build only)
+  int seeded;     // 1: outputs hold the first outer iteration's amplitudes and chi2 (fit_core.cuh dofit_with)
 };
 
 // Status bits (mirror of enum mf_channel_status).
@@ -82,9 +83,6 @@ struct LaunchTimer {
   }
 };
 
-// Per-channel form of the mixed and FP32 precisions (fit_cov.cu): FP32 outer
-// loop, then FP64 from its result.
-cudaError_t launch_fit_cov(const FitArgs& a, int block, cudaStream_t s, bool instrumented, LaunchTimer* tm);
 cudaError_t launch_fit_fp64(const FitArgs& a, int block, cudaStream_t s, bool instrumented,
                             LaunchTimer* tm = nullptr);
 
