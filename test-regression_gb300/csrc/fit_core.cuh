@@ -47,31 +47,36 @@ struct Counter {
 };
 
 // linalgebra/interface/cholesky.hpp:8-38 (rows [r0, r1) of a row-major factor)
-template <bool C, typename T>
-__device__ __forceinline__ void chol_rows(const T* M, T* L, int ld, int r0, int r1, Counter<C>& f) {
+// R: also keep the reciprocals of the diagonal in rinv and multiply by them
+// instead of dividing (one division per row: the per-channel form's FP64
+// continuation, which needs no bit parity with the oracle)
+template <bool C, typename T, bool R = false>
+__device__ __forceinline__ void chol_rows(const T* M, T* L, int ld, int r0, int r1, Counter<C>& f, T* rinv = nullptr) {
   for (int i = r0; i < r1; ++i) {
     T sumsq = 0;
     for (int j = 0; j < i; ++j) {
       T s2 = 0;
       for (int k = 0; k < j; ++k) s2 = fmaT(L[i * ld + k], L[j * ld + k], s2);
-      const T v = (M[i * ld + j] - s2) / L[j * ld + j];
+      const T v = R ? (M[i * ld + j] - s2) * rinv[j] : (M[i * ld + j] - s2) / L[j * ld + j];
       L[i * ld + j] = v;
       sumsq = fmaT(v, v, sumsq);
       f.fma(j + 1);
       f.op(2);
     }
     L[i * ld + i] = sqrtT(M[i * ld + i] - sumsq);
+    if (R) rinv[i] = T(1) / L[i * ld + i];
     f.op(2);
   }
 }
 
 // linalgebra/interface/substitution.hpp:10-26
-template <bool C, typename T>
-__device__ __forceinline__ void fwd(const T* L, int ld, const T* b, T* y, int n, Counter<C>& f) {
+template <bool C, typename T, bool R = false>
+__device__ __forceinline__ void fwd(const T* L, int ld, const T* b, T* y, int n, Counter<C>& f,
+                                    const T* rinv = nullptr) {
   for (int i = 0; i < n; ++i) {
     T t = b[i];
     for (int j = 0; j < i; ++j) t = fmaT(-L[i * ld + j], y[j], t);
-    y[i] = t / L[i * ld + i];
+    y[i] = R ? t * rinv[i] : t / L[i * ld + i];
     f.fma(i);
     f.op(1);
   }
@@ -305,6 +310,7 @@ struct FitState {
   T amp[KMAX];
   T P[KMAX * KMAX];  // column-major N x K
   T LC[KMAX * KMAX]; // row-major lower factor of the covariance, ld = KMAX
+  T LCr[KMAX];       // reciprocals of LC's diagonal (kept by the reciprocal variant only)
   T chisq;
   FnnlsOut st;
   int outer_iters;
@@ -314,7 +320,7 @@ struct FitState {
 };
 
 // updateCov, multifit_cpu/src/PulseChiSqSNNLS.cpp:169-194
-template <int NT, int KT, bool C, typename T>
+template <int NT, int KT, bool C, typename T, bool R = false>
 __device__ void update_cov(const DevConditions& c, int N, int K, T pederr, FitState<T>& S, Counter<C>& f) {
   T M[KMAX * KMAX];
   const T ped2 = pederr * pederr;
@@ -340,11 +346,11 @@ __device__ void update_cov(const DevConditions& c, int N, int K, T pederr, FitSt
       f.fma(ns * (ns + 1) / 2);
     }
   }
-  chol_rows(M, S.LC, KMAX, 0, N, f);
+  chol_rows<C, T, R>(M, S.LC, KMAX, 0, N, f, S.LCr);
 }
 
 // ComputeChiSq, multifit_cpu/src/PulseChiSqSNNLS.cpp:196-200
-template <bool C, typename T>
+template <bool C, typename T, bool R = false>
 __device__ T compute_chisq(int N, int K, const FitState<T>& S, Counter<C>& f) {
   T r[KMAX], z[KMAX];
   for (int i = 0; i < N; ++i) {
@@ -354,7 +360,7 @@ __device__ T compute_chisq(int N, int K, const FitState<T>& S, Counter<C>& f) {
   }
   f.fma(N * K);
   f.op(N);
-  fwd(S.LC, KMAX, r, z, N, f);
+  fwd<C, T, R>(S.LC, KMAX, r, z, N, f, S.LCr);
   T c = 0;
   for (int i = 0; i < N; ++i) c = fmaT(z[i], z[i], c);
   f.fma(N);
@@ -368,7 +374,7 @@ __device__ T compute_chisq(int N, int K, const FitState<T>& S, Counter<C>& f) {
 // costs the full pipe time whatever the number of active lanes, so the
 // covariance factor, the whitening and chi2 must be issued once for all lanes
 // rather than once per group of lanes that left FNNLS together.
-template <int NT, int KT, bool C, typename T>
+template <int NT, int KT, bool C, typename T, bool R = false>
 __device__ void minimize(const DevConditions& c, const DevOptions& o, int N, int K, T pederr, FitState<T>& S,
                          Counter<C>& f, unsigned lanes) {
   bool done = S.first_done != 0;
@@ -377,13 +383,13 @@ __device__ void minimize(const DevConditions& c, const DevOptions& o, int N, int
     const unsigned act = __ballot_sync(lanes, run);
     if (act == 0u) break;
     if (!run) continue;
-    update_cov<NT, KT>(c, N, K, pederr, S, f);
+    update_cov<NT, KT, C, T, R>(c, N, K, pederr, S, f);
     T A[KMAX * KMAX], b[KMAX];
-    for (int k = 0; k < K; ++k) fwd(S.LC, KMAX, S.P + k * N, A + k * N, N, f);
-    fwd(S.LC, KMAX, S.samp, b, N, f);
+    for (int k = 0; k < K; ++k) fwd<C, T, R>(S.LC, KMAX, S.P + k * N, A + k * N, N, f, S.LCr);
+    fwd<C, T, R>(S.LC, KMAX, S.samp, b, N, f, S.LCr);
     fnnls<NT, KT>(A, b, S.amp, N, K, T(o.nnls_eps), o.max_iter_nnls, o.nnls_start, S.st, f);
     __syncwarp(act);
-    const T now = compute_chisq(N, K, S, f);
+    const T now = compute_chisq<C, T, R>(N, K, S, f);
     const T delta = now - S.chisq;
     f.op(1);
     S.chisq = now;
@@ -394,10 +400,10 @@ __device__ void minimize(const DevConditions& c, const DevOptions& o, int N, int
 }
 
 // ComputeApproxUncertainty, multifit_cpu/src/PulseChiSqSNNLS.cpp:202-207
-template <bool C, typename T>
+template <bool C, typename T, bool R = false>
 __device__ T approx_uncertainty(int N, const FitState<T>& S, int k, Counter<C>& f) {
   T z[KMAX];
-  fwd(S.LC, KMAX, S.P + k * N, z, N, f);
+  fwd<C, T, R>(S.LC, KMAX, S.P + k * N, z, N, f, S.LCr);
   T n2 = 0;
   for (int i = 0; i < N; ++i) n2 = fmaT(z[i], z[i], n2);
   f.fma(N);
@@ -416,7 +422,7 @@ __device__ T approx_uncertainty(int N, const FitState<T>& S, int k, Counter<C>& 
 // passive-set tables): its amplitudes and chi2 are read from the outputs and
 // the loop goes on from the second iteration, with the reference's stopping
 // rule against that chi2 (against 0 after the first iteration).
-template <int NT, int KT, bool C, typename Mini>
+template <int NT, int KT, bool C, bool R = false, typename Mini>
 __device__ void dofit_with(const FitArgs& a, const DevConditions& c, int64_t ch, unsigned lanes, Counter<C>& f,
                            Mini&& mini) {
   const int N = NT > 0 ? NT : c.N;
@@ -444,7 +450,7 @@ __device__ void dofit_with(const FitArgs& a, const DevConditions& c, int64_t ch,
     if (a.opt.compute_errors && fabs(a.chi2[ch]) < a.opt.dchi2_tol) {
       // the loop stops at once: the error refits need the first iteration's
       // covariance factor, that of pederr^2 samplecor
-      update_cov<NT, KT>(c, N, K, pederr, S, f);
+      update_cov<NT, KT, C, double, R>(c, N, K, pederr, S, f);
     }
     for (int k = 0; k < K; ++k) S.amp[k] = seed[k];
     S.chisq = a.chi2[ch];
@@ -466,7 +472,7 @@ __device__ void dofit_with(const FitArgs& a, const DevConditions& c, int64_t ch,
 
   if (a.opt.compute_errors && c.intime_col >= 0) {
     const int kin = c.intime_col;
-    const double approxerr = approx_uncertainty(N, S, kin, f);
+    const double approxerr = approx_uncertainty<C, double, R>(N, S, kin, f);
     const double chisq0 = S.chisq;
     const double x0 = ampmin[kin];
     double pulse_in[KMAX];
@@ -478,7 +484,7 @@ __device__ void dofit_with(const FitArgs& a, const DevConditions& c, int64_t ch,
     S.amp[kin] = xplus;
     for (int i = 0; i < N; ++i) S.samp[i] = fma(-xplus, pulse_in[i], in[i]);
     mini(S, pederr, lanes);
-    const double chip = compute_chisq(N, K, S, f);
+    const double chip = compute_chisq<C, double, R>(N, K, S, f);
     const double sigmaplus = fabs(xplus - x0) / sqrt(chip - chisq0);
     const bool lower = x0 / sigmaplus > 0.5;
     const unsigned lanes2 = __ballot_sync(lanes, lower);
@@ -487,7 +493,7 @@ __device__ void dofit_with(const FitArgs& a, const DevConditions& c, int64_t ch,
       S.amp[kin] = xminus;
       for (int i = 0; i < N; ++i) S.samp[i] = fma(-xminus, pulse_in[i], in[i]);
       mini(S, pederr, lanes2);
-      const double chim = compute_chisq(N, K, S, f);
+      const double chim = compute_chisq<C, double, R>(N, K, S, f);
       const double sigmaminus = fabs(xminus - x0) / sqrt(chim - chisq0);
       err = 0.5 * (sigmaplus + sigmaminus);
     } else {

@@ -22,20 +22,24 @@
 namespace mfgb {
 namespace {
 
-// DoFit with the FP64 Minimize: the plain drop-in.
-template <int NT, int KT, bool C>
+// DoFit with the FP64 Minimize: the plain drop-in (R = false), or the
+// per-channel form's FP64 continuation (R = true: the covariance factor's
+// diagonal inverted once per row, multiplications for the ~(K + 3) N
+// divisions of the factor, whitening and chi2 -- on this GPU an FP64 division
+// is a sequence of about ten FP64 instructions).
+template <int NT, int KT, bool C, bool R>
 __device__ void dofit(const FitArgs& a, const DevConditions& c, int64_t ch, unsigned lanes) {
   const int N = NT > 0 ? NT : c.N;
   const int K = KT > 0 ? KT : c.K;
   Counter<C> f;
-  dofit_with<NT, KT, C>(a, c, ch, lanes, f, [&](FitState<double>& S, double pederr, unsigned ln) {
-    minimize<NT, KT>(c, a.opt, N, K, pederr, S, f, ln);
+  dofit_with<NT, KT, C, R>(a, c, ch, lanes, f, [&](FitState<double>& S, double pederr, unsigned ln) {
+    minimize<NT, KT, C, double, R>(c, a.opt, N, K, pederr, S, f, ln);
   });
 }
 
 // One launch per condition set (lanes of other sets idle); out-of-range set
 // indices are flagged by the first launch.
-template <int NT, int KT, bool C>
+template <int NT, int KT, bool C, bool R = false>
 __global__ void __launch_bounds__(128) fit_fp64_kernel(const FitArgs a, int set, int flag_bad) {
   const int64_t ch = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   bool mine = false;
@@ -51,7 +55,7 @@ __global__ void __launch_bounds__(128) fit_fp64_kernel(const FitArgs a, int set,
     }
   }
   const unsigned lanes = __ballot_sync(0xffffffffu, mine);  // taken while the warp is converged
-  if (mine) dofit<NT, KT, C>(a, a.cond[set], ch, lanes);
+  if (mine) dofit<NT, KT, C, R>(a, a.cond[set], ch, lanes);
 }
 
 }  // namespace
@@ -63,7 +67,11 @@ cudaError_t launch_sets(const FitArgs& a, int block, cudaStream_t s, LaunchTimer
     const DevConditions& c = a.cond[t];
     const int flag = t == 0;
     if (tm) tm->mark(MF_K_FIT_FP64, s);
-    if (c.N == 10 && c.K == 10) fit_fp64_kernel<10, 10, C><<<grid, block, 0, s>>>(a, t, flag);
+    // the seeded continuation of the per-channel form with reciprocals (its
+    // instrumented count runs the division form)
+    if (a.seeded && !C && c.N == 10 && c.K == 10) fit_fp64_kernel<10, 10, false, true><<<grid, block, 0, s>>>(a, t, flag);
+    else if (a.seeded && !C) fit_fp64_kernel<0, 0, false, true><<<grid, block, 0, s>>>(a, t, flag);
+    else if (c.N == 10 && c.K == 10) fit_fp64_kernel<10, 10, C><<<grid, block, 0, s>>>(a, t, flag);
     else if (c.N == 8 && c.K == 8) fit_fp64_kernel<8, 8, C><<<grid, block, 0, s>>>(a, t, flag);
     else fit_fp64_kernel<0, 0, C><<<grid, block, 0, s>>>(a, t, flag);
     cudaError_t e = cudaGetLastError();
