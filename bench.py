@@ -199,7 +199,7 @@ def default_workload(form: str) -> str:
 # traffic is this times its channels); the summary with the command is the
 # profiles/ file given
 NCU_DRAM_BYTES_PER_CHANNEL = {
-    ("judge_kernel", "warm"): (194.1, "profiles/judge_kernel_fp32_warm-2m.md"),
+    ("judge_kernel", "warm"): (194.4, "profiles/judge_kernel_fp32_warm-2m.md"),
 }
 # useful FLOPs of one warm-start prediction: 12 inputs -> 128 -> 128 -> 20
 # outputs, 2 per multiply-add (the network pads to 16 inputs and 32 outputs)
