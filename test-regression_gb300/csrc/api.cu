@@ -568,6 +568,7 @@ void fill_dev_mixed(const mf_context* c, int t, DevMixed* m) {
   m->pinv32 = c->d_pinv32[t];
   m->pinv32lo = c->d_pinv32lo[t];
   m->pinv2 = c->d_pinv2[t];
+  m->g2 = c->d_pinv2[t] + h.g2_off;
 }
 
 int grow_staging(mf_context* c, int64_t n, int ss, int as) {

@@ -105,7 +105,9 @@ struct HostTables {
   std::vector<double> pinv64;
   std::vector<float> pinv32;
   std::vector<float> pinv32lo;        // pinv64 = pinv32 + pinv32lo to ~2^-48
-  std::vector<float> pinv2;           // element e as the pair (pinv32[e], pinv32lo[e]) at [2e], [2e + 1]
+  std::vector<float> pinv2;           // element e as the pair (pinv32[e], pinv32lo[e]) at [2e], [2e + 1],
+                                      // then G column by column as pairs (G32, G32lo) from [g2_off]
+  int g2_off = 0;
 };
 int build_mixed_tables(const DevConditions& c, HostTables* t);
 
@@ -130,6 +132,7 @@ struct DevMixed {
   const float* pinv32;
   const float* pinv32lo;
   const float* pinv2;  // (hi, lo) pairs; a row of an even N starts on 16 bytes
+  const float* g2;     // G as (hi, lo) pairs, column k at [2 k N] (inside the pinv2 buffer)
 };
 
 struct MixedArgs {

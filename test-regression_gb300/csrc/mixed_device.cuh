@@ -705,14 +705,39 @@ __device__ __forceinline__ void judge_df_body(const MixedArgs& a, const DevMixed
       yl[i] = lo;
     }
   }
-  // x = G_S^+ y through the table's float pairs (rows outside the set read the
-  // zero row), with dx[k] = sum_i |G^+_ki y_i|, the scale of x_k's round-off.
-  // A row's (hi, lo) pairs come two elements per 16-byte load when N is even.
-  float xh[K], xl[K], dx[K];
+  // Column by column: x_k = G_S^+_k y through the table's float pairs (a
+  // column outside the set reads the zero row), dx_k = sum_i |G^+_ki y_i| (the
+  // scale of x_k's round-off), then x_k enters the residual r = y - G x at
+  // once. The loop over the columns stays rolled: unrolled, the judge's body
+  // ran to ~6,000 instructions and instruction fetch was its first stall; the
+  // column's G entries come from the pair table in global memory, the same
+  // address in every lane. The amplitudes are written as they come; a
+  // channel the judge queues gets them rewritten by the fix or the repair.
+  //
+  // Round-off bounds, per channel. The table and y are exact to ~2^-48 and each
+  // double-float multiply-add errs by ~2^-48 of its terms, so with N <= 10
+  // terms per sum |x_k - x_S,k| <= N 2^-48 dx_k < 2^-44 dx_k (xb), and the
+  // computed residual errs by at most e_i = sum_k |G_ik| (xb_k + 2^-44 |x_k|)
+  // + 2^-44 |y_i| (the solve's error carried through G, plus the residual's
+  // own rounding), so a gradient errs by at most sum_i |G_ik| e_i. Where the
+  // true residual is tiny (near-exact fits, e.g. ten active pulses on ten
+  // samples) these errors can flip the sign of a gradient or an amplitude, so
+  // decisions inside the bounds go to the FP64 repair.
+  float rh[N], rl[N], e[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    rh[i] = yh[i];
+    rl[i] = yl[i];
+    e[i] = 0x1p-44f * fabsf(yh[i]);
+  }
+  bool ok = true, finite = true;
+  uint16_t support = 0;
+  double xin = 0.;
+  double* out = a.amplitudes + ch * a.amp_stride;
   {
     const int off = __ldg(T.offset + m);
     int r = 0;
-#pragma unroll
+#pragma unroll 1
     for (int k = 0; k < K; ++k) {
       const bool inset = (m >> k) & 1u;
       const int row = inset ? off + r * N : T.zero_row;
@@ -737,67 +762,58 @@ __device__ __forceinline__ void judge_df_body(const MixedArgs& a, const DevMixed
           mag = fmaf(fabsf(q.x), fabsf(yh[i]), mag);
         }
       }
-      xh[k] = hi;
-      xl[k] = lo;
-      dx[k] = mag;
-    }
-  }
-  // Round-off bounds, per channel. The table and y are exact to ~2^-48 and each
-  // double-float multiply-add errs by ~2^-48 of its terms, so with N <= 10
-  // terms per sum |x_k - x_S,k| <= N 2^-48 dx_k < 2^-44 dx_k (xb), and the
-  // computed residual errs by at most e_i = sum_k |G_ik| (xb_k + 2^-44 |x_k|)
-  // + 2^-44 |y_i| (the solve's error carried through G, plus the residual's
-  // own rounding), so a gradient errs by at most sum_i |G_ik| e_i. Where the
-  // true residual is tiny (near-exact fits, e.g. ten active pulses on ten
-  // samples) these errors can flip the sign of a gradient or an amplitude, so
-  // decisions inside the bounds go to the FP64 repair.
-  bool ok = true;
-  float xb[K];
+      const float xb = 0x1p-44f * mag;
+      if (inset && !(hi > xb)) ok = false;
+      const float ek = fmaf(0x1p-44f, fabsf(hi), xb);
+      // r -= G_k x_k (G's structural zeros add exact zeros)
+      const float nh = -hi, nl = -lo;
+      if constexpr (N % 2 == 0) {
+        const float4* gp = reinterpret_cast<const float4*>(T.g2 + 2 * k * N);
 #pragma unroll
-  for (int k = 0; k < K; ++k) {
-    xb[k] = 0x1p-44f * dx[k];
-    if ((m & (1u << k)) && !(xh[k] > xb[k])) ok = false;
+        for (int i = 0; i < N; i += 2) {
+          const float4 g = __ldg(gp + i / 2);
+          df_fma(rh[i], rl[i], g.x, g.y, nh, nl);
+          e[i] = fmaf(fabsf(g.x), ek, e[i]);
+          df_fma(rh[i + 1], rl[i + 1], g.z, g.w, nh, nl);
+          e[i + 1] = fmaf(fabsf(g.z), ek, e[i + 1]);
+        }
+      } else {
+        const float2* gp = reinterpret_cast<const float2*>(T.g2 + 2 * k * N);
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          const float2 g = __ldg(gp + i);
+          df_fma(rh[i], rl[i], g.x, g.y, nh, nl);
+          e[i] = fmaf(fabsf(g.x), ek, e[i]);
+        }
+      }
+      const double xk = double(hi) + double(lo);
+      out[k] = xk;
+      finite = finite && finite64(xk);
+      if (pos64(xk)) support |= uint16_t(1u << k);
+      if (k == T.intime_col) xin = xk;
+    }
   }
   const bool pos_ok = ok;
   unsigned add = 0;
-  // r = y - G x
-  float rh[N], rl[N], rf[N];
-#pragma unroll
-  for (int i = 0; i < N; ++i) {
-    rh[i] = yh[i];
-    rl[i] = yl[i];
-  }
-#pragma unroll
-  for (int k = 0; k < K; ++k)
-#pragma unroll
-    for (int i = 0; i < N; ++i)
-      if (i >= T.gfz[k]) df_fma(rh[i], rl[i], -T.G32[k * N + i], -T.G32lo[k * N + i], xh[k], xl[k]);
+  float rf[N];
 #pragma unroll
   for (int i = 0; i < N; ++i) rf[i] = __fadd_rn(rh[i], rl[i]);
   if (ok) {
-    float e[N];
-#pragma unroll
-    for (int i = 0; i < N; ++i) e[i] = 0x1p-44f * fabsf(yh[i]);
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      const float ek = fmaf(0x1p-44f, fabsf(xh[k]), xb[k]);
-#pragma unroll
-      for (int i = 0; i < N; ++i)
-        if (i >= T.gfz[k]) e[i] = fmaf(fabsf(T.G32[k * N + i]), ek, e[i]);
-    }
     const float tol = a.eps32 * s2h;
-#pragma unroll
+#pragma unroll 1
     for (int k = 0; k < K; ++k) {
+      if (m & (1u << k)) continue;
       float w = 0.f, mag = 0.f, werr = 0.f;
+      const float2* gp = reinterpret_cast<const float2*>(T.g2 + 2 * k * N);
 #pragma unroll
-      for (int i = 0; i < N; ++i)
-        if (i >= T.gfz[k]) {
-          w = fmaf(T.G32[k * N + i], rf[i], w);
-          mag = fmaf(fabsf(T.G32[k * N + i]), fabsf(rf[i]), mag);
-          werr = fmaf(fabsf(T.G32[k * N + i]), e[i], werr);
-        }
-      if (!(m & (1u << k)) && !(fmaf(0x1p-19f, mag, w + werr) < tol)) ok = false;
-      if (!(m & (1u << k)) && fmaf(-0x1p-19f, mag, w - werr) > tol) add |= 1u << k;  // provably violating
+      for (int i = 0; i < N; ++i) {
+        const float g = __ldg(gp + i).x;
+        w = fmaf(g, rf[i], w);
+        mag = fmaf(fabsf(g), fabsf(rf[i]), mag);
+        werr = fmaf(fabsf(g), e[i], werr);
+      }
+      if (!(fmaf(0x1p-19f, mag, w + werr) < tol)) ok = false;
+      if (fmaf(-0x1p-19f, mag, w - werr) > tol) add |= 1u << k;  // provably violating
     }
   }
   if (!ok) {  // compaction into the fix or the repair queue
@@ -809,27 +825,38 @@ __device__ __forceinline__ void judge_df_body(const MixedArgs& a, const DevMixed
   float ch2 = 0.f, cl2 = 0.f;
 #pragma unroll
   for (int i = 0; i < N; ++i) {
-    float p, e;
-    two_prod(rh[i], rh[i], p, e);
-    e = fmaf(2.f * rh[i], rl[i], e);
-    df_acc(ch2, cl2, p, e);
+    float p, q;
+    two_prod(rh[i], rh[i], p, q);
+    q = fmaf(2.f * rh[i], rl[i], q);
+    df_acc(ch2, cl2, p, q);
   }
-  double x[K];
-#pragma unroll
-  for (int k = 0; k < K; ++k) x[k] = double(xh[k]) + double(xl[k]);
   // chi2 / pederr^2 in double-float: q1 = c / s2 rounded, then the remainder
   // c - q1 s2 (exact leading difference) divided once more (~2^-46 relative)
   double chi2;
   if (!bad) {
     const float q1 = __fdiv_rn(ch2, s2h);
-    float p, e;
-    two_prod(q1, s2h, p, e);
-    const float rem = __fadd_rn(__fsub_rn(ch2, p), __fsub_rn(cl2, fmaf(q1, s2l, e)));
+    float p, q;
+    two_prod(q1, s2h, p, q);
+    const float rem = __fadd_rn(__fsub_rn(ch2, p), __fsub_rn(cl2, fmaf(q1, s2l, q)));
     chi2 = double(q1) + double(__fdiv_rn(rem, s2h));
   } else {
     chi2 = (double(ch2) + double(cl2)) / (sig * sig);
   }
-  store_outputs<N, K>(a, T, ch, x, chi2, bad, true, int(cnt & 255u), int(cnt >> 8) + 1, K + 4);
+  for (int k = K; k < a.amp_stride && k < KMAX; ++k) out[k] = 0.;
+  a.chi2[ch] = chi2;
+  if (a.intime) a.intime[ch] = T.intime_col >= 0 ? xin : 0.;
+  if (a.active_mask) a.active_mask[ch] = support;
+  if (a.status) {
+    uint8_t st = 0;
+    if (!(finite && finite64(chi2))) st |= CH_NONFINITE;
+    if (bad) st |= CH_BADINPUT;
+    a.status[ch] = st;
+  }
+  if (a.iters) {
+    const int adds = int(cnt & 255u), solves = int(cnt >> 8) + 1;
+    a.iters[ch] = 1 | ((adds < 4095 ? adds : 4095) << 8) | ((solves < 4095 ? solves : 4095) << 20);
+  }
+  if (a.flops) a.flops[ch] = double(K + 4);
 }
 
 }  // namespace

@@ -170,10 +170,17 @@ int build_mixed_tables(const DevConditions& c, HostTables* t) {
   // the same operators as (hi, lo) pairs, for the double-float solve: with N
   // even every row (offset[m] + r N elements, 8 bytes each) starts on a
   // 16-byte boundary, so a row is N / 2 16-byte loads
-  t->pinv2.assign(2 * size_t(total + N), 0.0f);
+  // followed by G as pairs, column by column (the double-float judge reads a
+  // column per loop step, the same address in every lane)
+  t->g2_off = 2 * (total + N);
+  t->pinv2.assign(size_t(t->g2_off) + 2 * size_t(K) * N, 0.0f);
   for (int e = 0; e < total + N; ++e) {
     t->pinv2[2 * size_t(e)] = t->pinv32[e];
     t->pinv2[2 * size_t(e) + 1] = t->pinv32lo[e];
+  }
+  for (int e = 0; e < K * N; ++e) {
+    t->pinv2[size_t(t->g2_off) + 2 * size_t(e)] = t->G32[e];
+    t->pinv2[size_t(t->g2_off) + 2 * size_t(e) + 1] = t->G32lo[e];
   }
   return MF_OK;
 }
