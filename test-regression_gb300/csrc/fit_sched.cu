@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(128) screen_persist(const MixedArgs a, int set
 }
 
 template <int N, int K>
-__global__ void __launch_bounds__(128) fix_persist(const MixedArgs a, int set) {
+__global__ void __launch_bounds__(128) fix_persist(const MixedArgs a, int set, int rounds) {
   const DevMixed& T = a.tab[set];
   const unsigned total = a.ws_sched[SCHED_FIXQ + set];
   const int lane = threadIdx.x & 31;
@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(128) fix_persist(const MixedArgs a, int set) {
     const unsigned base = steal(a.ws_sched + SCHED_STEAL + set * 6 + 2, 32u);
     if (base >= total) break;
     const unsigned i = base + unsigned(lane);
-    if (i < total) fix_body<N, K>(a, T, unsigned(a.ws_fixq[i]));
+    if (i < total) fix_body<N, K>(a, T, unsigned(a.ws_fixq[i]), rounds);
   }
 }
 
@@ -330,14 +330,14 @@ cudaError_t launch_set(const MixedArgs& a, int set, int block, int lanes, cudaSt
     if (tm) tm->mark(MF_K_SCREEN, s);
     screen_persist<N, K><<<wave(screen_persist<N, K>, 128, a), 128, 0, s>>>(a, set);
     if (tm) tm->mark(MF_K_FIX, s);
-    fix_persist<N, K><<<wave(fix_persist<N, K>, 128, a), 128, 0, s>>>(a, set);
+    fix_persist<N, K><<<wave(fix_persist<N, K>, 128, a), 128, 0, s>>>(a, set, 2);
   }
   if (tm) tm->mark(MF_K_JUDGE, s);
   if (a.judge_df) judge_persist<N, K, true><<<wave(judge_persist<N, K, true>, 128, a), 128, 0, s>>>(a, a.tab[set], set, WARM);
   else judge_persist<N, K, false><<<wave(judge_persist<N, K, false>, 128, a), 128, 0, s>>>(a, a.tab[set], set, WARM);
   if (WARM) {
     if (tm) tm->mark(MF_K_FIX, s);
-    fix_persist<N, K><<<wave(fix_persist<N, K>, 128, a), 128, 0, s>>>(a, set);
+    fix_persist<N, K><<<wave(fix_persist<N, K>, 128, a), 128, 0, s>>>(a, set, 1);
     if (tm) tm->mark(MF_K_REJUDGE, s);
     if (a.judge_df)
       judge_fixed_persist<N, K, true><<<wave(judge_fixed_persist<N, K, true>, 128, a), 128, 0, s>>>(a, a.tab[set], set);

@@ -575,10 +575,14 @@ __device__ __forceinline__ void screen_body(const MixedArgs& a, const DevMixed& 
 // 21, add = the columns that provably violate the KKT condition; ch <
 // MIXED_CHUNK = 2^21):
 // the FNNLS step with the added columns in FP32 (the inner loop drops those
-// that come out non-positive), then the double-float screen of the new set
-// and, if it finds more, one more step. Writes the hand-off for the judge.
+// that come out non-positive), then, with rounds = 2, the double-float screen
+// of the new set and, if it finds more, one more step. Writes the hand-off for
+// the judge. Cold starts (queued by the screen, judged once after) take two
+// rounds; warm starts (queued by the judge, judged again after) one: there the
+// screen round cost more than the repairs it saved (warm step 6.31 -> 6.14 ms
+// per 10M with one round; cold with one round 9.5 -> 13.0 ms, repairs x9).
 template <int N, int K>
-__device__ __forceinline__ void fix_body(const MixedArgs& a, const DevMixed& T, unsigned entry) {
+__device__ __forceinline__ void fix_body(const MixedArgs& a, const DevMixed& T, unsigned entry, int rounds) {
   const int64_t ch = int64_t(entry & 0x1fffffu);
   unsigned add = entry >> 21;
   unsigned m = a.ws_mask[ch];
@@ -610,7 +614,7 @@ __device__ __forceinline__ void fix_body(const MixedArgs& a, const DevMixed& T, 
     m |= add;
     adds += __popc(add);
     solves += inner_loop<K>(m, x32, s32);
-    add = round == 0 ? refine_screen<N, K>(T, sh, sl, m, x32, solves, srhs) : 0u;
+    add = round + 1 < rounds ? refine_screen<N, K>(T, sh, sl, m, x32, solves, srhs) : 0u;
   }
   a.ws_mask[ch] = uint16_t(m);
   a.ws_count[ch] = uint16_t((adds < 255 ? adds : 255) | ((solves < 255 ? solves : 255) << 8));
