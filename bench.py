@@ -195,11 +195,11 @@ def default_workload(form: str) -> str:
     return {"fp64": "ecal-1m-pu2", "fp32-cov": "ecal-1m-pu2"}.get(form, "warm-eval-10m")
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per channel of a
 # launch, measured by ncu on the kernel of the form named (a capture of one
-# 2,097,152-channel chunk; the bytes grow with the channels, so a launch's
+# 2,000,000-channel launch; the bytes grow with the channels, so a launch's
 # traffic is this times its channels); the summary with the command is the
 # profiles/ file given
 NCU_DRAM_BYTES_PER_CHANNEL = {
-    ("judge_kernel", "warm"): (194.4, "profiles/judge_kernel_fp32_warm-2m.md"),
+    ("judge_kernel", "warm"): (179.2, "profiles/judge_kernel_fp32_warm-2m.md"),
 }
 # useful FLOPs of one warm-start prediction: 12 inputs -> 128 -> 128 -> 20
 # outputs, 2 per multiply-add (the network pads to 16 inputs and 32 outputs)
