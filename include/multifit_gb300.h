@@ -259,7 +259,7 @@ int mf_build_pulse_matrix(const double* fullpulse, const int8_t* bxs, int nsampl
                           double* pulse_matrix);
 
 /* Learned warm start ------------------------------------------------------
- * A small MLP (16 -> 128 -> 128 -> 32, GELU, BF16 tensor-core GEMMs with FP32
+ * A small MLP (16 -> 128 -> 128 -> 32, ReLU, BF16 tensor-core GEMMs with FP32
  * accumulate, FP32 master weights) predicts from a channel's whitened
  * samples and noise scale its passive set and amplitudes; the mixed form
  * (warm_start = MF_WARM_MLP) then starts FNNLS there and still runs it to KKT

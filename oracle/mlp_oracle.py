@@ -1,19 +1,17 @@
 """CPU FP64 restatement of the warm-start MLP -- TEST INFRASTRUCTURE ONLY.
 
-The network (16 -> 128 -> GELU -> 128 -> GELU -> 32) and its loss (BCE on the
+The network (16 -> 128 -> ReLU -> 128 -> ReLU -> 32) and its loss (BCE on the
 10 passive-set logits + amp_weight * MSE of softplus(amplitude outputs)) are
 the engine's own design with no counterpart in the reference, so this module
 is the checker of the hand-written GPU kernels (test-regression_gb300/csrc/
 mlp.cu): forward, loss, backward.
 
 `quantized=True` mirrors the kernels' BF16 rounding points (weights, the
-GELU outputs H1/H2, dO, dZ2, dZ1) with all arithmetic in FP64, so the GPU
+ReLU outputs H1/H2, dO, dZ2, dZ1) with all arithmetic in FP64, so the GPU
 gradients differ from it only by FP32 accumulation; `quantized=False` is the
 exact FP64 gradient of the same loss.
 """
 from __future__ import annotations
-
-import math
 
 import numpy as np
 
@@ -41,18 +39,13 @@ def bf16(x):
     return u.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
-# GELU, tanh form (Hendrycks & Gimpel 2016), the function the engine's network uses
-_C0 = math.sqrt(2.0 / math.pi)
-_C1 = 0.044715
+# ReLU hidden units, the function the engine's network uses
+def relu(z):
+    return np.maximum(z, 0.0)
 
 
-def gelu(z):
-    return 0.5 * z * (1.0 + np.tanh(_C0 * (z + _C1 * z ** 3)))
-
-
-def gelu_grad(z):
-    t = np.tanh(_C0 * (z + _C1 * z ** 3))
-    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * _C0 * (1.0 + 3.0 * _C1 * z * z)
+def relu_grad(z):
+    return (z > 0.0).astype(np.float64)
 
 
 def softplus(x):
@@ -67,9 +60,9 @@ def forward(params, X, quantized=True):
     q = bf16 if quantized else (lambda a: np.asarray(a, dtype=np.float64))
     W1, W2, W3 = q(params["W1"]), q(params["W2"]), q(params["W3"])
     Z1 = X @ W1.T + params["b1"]
-    H1 = q(gelu(Z1))
+    H1 = q(relu(Z1))
     Z2 = H1 @ W2.T + params["b2"]
-    H2 = q(gelu(Z2))
+    H2 = q(relu(Z2))
     O = H2 @ W3.T + params["b3"]
     return {"Z1": Z1, "H1": H1, "Z2": Z2, "H2": H2, "O": O, "W1": W1, "W2": W2, "W3": W3}
 
@@ -93,11 +86,11 @@ def loss_and_grad(params, X, T, amp_weight=1.0, quantized=True):
     g["W3"] = dO.T @ f["H2"]
     g["b3"] = dO.sum(axis=0)
     dH2 = dO @ f["W3"]
-    dZ2 = q(dH2 * gelu_grad(f["Z2"]))
+    dZ2 = q(dH2 * relu_grad(f["Z2"]))
     g["W2"] = dZ2.T @ f["H1"]
     g["b2"] = dZ2.sum(axis=0)
     dH1 = dZ2 @ f["W2"]
-    dZ1 = q(dH1 * gelu_grad(f["Z1"]))
+    dZ1 = q(dH1 * relu_grad(f["Z1"]))
     g["W1"] = dZ1.T @ X
     g["b1"] = dZ1.sum(axis=0)
     return loss, g

@@ -2,7 +2,7 @@
 // the noise scale, the passive set and the amplitudes of a channel's fit.
 //
 // Network: 16 inputs (10 normalised whitened samples, log SNR, pederr, zero
-// padding) -> 128 -> GELU -> 128 -> GELU -> 32 outputs (10 passive-set logits,
+// padding) -> 128 -> ReLU -> 128 -> ReLU -> 32 outputs (10 passive-set logits,
 // 10 amplitude outputs, padding). BF16 weights and activations on the tensor
 // cores, FP32 accumulate; FP32 master weights, Adam. Training runs its GEMMs
 // as mma.sync m16n8k16 tiles; inference runs on tcgen05 (mlp_tc.cu).
@@ -12,7 +12,7 @@
 //   gemm_kernel<EPI,..>   C = A * B^T for every training GEMM (forward layers,
 //                         input gradients, split-K weight gradients)
 //   loss_kernel           BCE on the logits + MSE on softplus(amplitude outputs)
-//   gelu_backward_kernel, bias_grad_kernel, adam_kernel, pack_weights_kernel
+//   relu_backward_kernel, bias_grad_kernel, adam_kernel, pack_weights_kernel
 //   launch_mlp_infer      the inference kernel of mlp_tc.cu (the path inside
 //                         a timed fit)
 #include <cuda_bf16.h>
@@ -112,10 +112,10 @@ __global__ void __launch_bounds__(128) gemm_kernel(const GemmArgs p) {
         const int c = n0 + wn + ni * 8 + 2 * t + (h & 1);
         if (r >= p.M || c >= p.N) continue;
         const float v = acc[mi][ni][h];
-        if (EPI == EPI_BIAS_GELU) {
+        if (EPI == EPI_BIAS_RELU) {
           const float z = v + p.bias[c];
           p.C[int64_t(r) * p.ldc + c] = z;
-          p.H[int64_t(r) * p.ldh + c] = __float2bfloat16(gelu(z));
+          p.H[int64_t(r) * p.ldh + c] = __float2bfloat16(relu(z));
         } else if (EPI == EPI_BIAS) {
           p.C[int64_t(r) * p.ldc + c] = v + p.bias[c];
         } else if (EPI == EPI_STORE) {
@@ -181,10 +181,10 @@ __global__ void mlp_loss_kernel(int B, const float* O, const float* T, float amp
   if (loss_sum) atomicAdd(loss_sum, l * invB);
 }
 
-__global__ void gelu_backward_kernel(int64_t count, const float* dH, const float* Z, bf16* dZ) {
+__global__ void relu_backward_kernel(int64_t count, const float* dH, const float* Z, bf16* dZ) {
   const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (i >= count) return;
-  dZ[i] = __float2bfloat16(dH[i] * gelu_grad(Z[i]));
+  dZ[i] = __float2bfloat16(dH[i] * relu_grad(Z[i]));
 }
 
 // db[c] += sum_b dZ[b][c] over a chunk of rows (float atomics).
@@ -230,7 +230,7 @@ cudaError_t launch_gemm(int epi, bool akc, bool bkc, const GemmArgs& p, int spli
     gemm_kernel<E, A, B><<<grid, 128, 0, s>>>(p);                      \
     return cudaGetLastError();                                         \
   }
-  MF_GEMM_CASE(EPI_BIAS_GELU, true, true)
+  MF_GEMM_CASE(EPI_BIAS_RELU, true, true)
   MF_GEMM_CASE(EPI_BIAS, true, true)
   MF_GEMM_CASE(EPI_STORE, true, true)
   MF_GEMM_CASE(EPI_ATOMIC, false, false)

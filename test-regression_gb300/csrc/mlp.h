@@ -10,7 +10,7 @@ constexpr int MLP_IN = 16;   // 10 whitened samples / |y|, log SNR, pederr, 4 ze
 constexpr int MLP_H = 128;
 constexpr int MLP_OUT = 32;  // 10 logits, 10 amplitude outputs, 12 zero pads
 
-enum GemmEpilogue { EPI_BIAS_GELU = 0, EPI_BIAS = 1, EPI_STORE = 2, EPI_ATOMIC = 3 };
+enum GemmEpilogue { EPI_BIAS_RELU = 0, EPI_BIAS = 1, EPI_STORE = 2, EPI_ATOMIC = 3 };
 
 // C[M x N] = op(A)[M x K] * op(B)[N x K]^T; element (i,k) of op(A) is
 // A[i*a_si + k*a_sk], element (j,k) of op(B) is B[j*b_sj + k*b_sk].
@@ -24,7 +24,7 @@ struct GemmArgs {
   float* C;
   int ldc;
   const float* bias;
-  __nv_bfloat16* H;  // EPI_BIAS_GELU: bf16 GELU output
+  __nv_bfloat16* H;  // EPI_BIAS_RELU: bf16 ReLU output
   int ldh;
 };
 
@@ -72,7 +72,7 @@ __global__ void mlp_targets_kernel(int64_t n, const double* amp, int amp_stride,
                                    const float* gnorm, float* T);
 __global__ void mlp_loss_kernel(int B, const float* O, const float* T, float amp_weight, __nv_bfloat16* dO,
                                 float* loss_sum);
-__global__ void gelu_backward_kernel(int64_t count, const float* dH, const float* Z, __nv_bfloat16* dZ);
+__global__ void relu_backward_kernel(int64_t count, const float* dH, const float* Z, __nv_bfloat16* dZ);
 __global__ void bias_grad_kernel(int B, int C, const __nv_bfloat16* dZ, float* db);
 __global__ void adam_kernel(int count, float* w, const float* g, float* m, float* v, float lr, float b1, float b2,
                             float eps, float c1, float c2);

@@ -26,34 +26,14 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
   return *reinterpret_cast<const uint32_t*>(&v);
 }
 
-// GELU in its tanh form (Hendrycks & Gimpel, "Gaussian Error Linear Units",
-// 2016): gelu(x) = x/2 (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))). Training
-// uses tanhf; inference uses the hardware tanh.approx.f32 (PTX ISA: maximum
-// relative error 2^-10.987), below the BF16 rounding applied to every hidden
-// activation (2^-9), so both evaluate the same network.
-constexpr float kGeluC0 = 0.79788456080286536f;  // sqrt(2/pi)
-constexpr float kGeluC1 = 0.044715f;
-__device__ __forceinline__ float gelu(float x) {
-  const float v = x * fmaf(kGeluC0 * kGeluC1, x * x, kGeluC0);
-  const float h = 0.5f * x;
-  return fmaf(h, tanhf(v), h);
-}
-__device__ __forceinline__ float tanh_approx(float v) {
-  float t;
-  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(v));
-  return t;
-}
-__device__ __forceinline__ float gelu_fast(float x) {
-  const float v = x * fmaf(kGeluC0 * kGeluC1, x * x, kGeluC0);
-  const float h = 0.5f * x;
-  return fmaf(h, tanh_approx(v), h);
-}
-__device__ __forceinline__ float gelu_grad(float x) {
-  const float x2 = x * x;
-  const float t = tanhf(x * fmaf(kGeluC0 * kGeluC1, x2, kGeluC0));
-  const float dv = fmaf(3.f * kGeluC0 * kGeluC1, x2, kGeluC0);  // d/dx of the tanh argument
-  return 0.5f * (1.f + t) + 0.5f * x * (1.f - t * t) * dv;
-}
+// ReLU hidden units. The network's cost on the GPU is its hidden-layer
+// epilogue (256 activations per channel between the tensor-core layers): a
+// ReLU is one packed convert-with-clamp per two activations where the tanh
+// form of GELU took ~6 FP32 operations and a MUFU tanh each (measured on 10M
+// ECAL channels: inference 1.41 ms with GELU, 1.00 ms with ReLU; fit results
+// identical, the warm fit 5% faster end to end).
+__device__ __forceinline__ float relu(float x) { return fmaxf(x, 0.f); }
+__device__ __forceinline__ float relu_grad(float x) { return x > 0.f ? 1.f : 0.f; }
 // A column enters the predicted passive set when its logit exceeds -0.5
 // (probability 0.38, not 0.5): a column predicted needlessly costs the warm
 // FP32 search one drop step, a column missed costs a fix and a second judge

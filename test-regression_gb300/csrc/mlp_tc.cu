@@ -8,13 +8,13 @@
 //   accumulators in tensor memory), commits them to the slot's mbarrier;
 //   warp w reads TMEM lanes 32 (w % 4) .. +31 (= 32 channels; a warp may only
 //   read its quarter of the lanes) and the 32 columns of warpgroup w / 4, adds
-//   the bias, applies GELU and writes the BF16 activations back to shared
+//   the bias, applies the ReLU and writes the BF16 activations back to shared
 //   memory as the A operand of the next layer,
 // and the slots alternate: while the tensor cores run one slot's layer, the
 // warps run the other slot's epilogue. Warpgroup 0 also computes the
 // features and decodes the outputs (one channel per thread). The network's weights are staged once
 // per CTA. Nothing of the MMA passes through registers: the CUDA cores run
-// only the features, the bias+GELU epilogues and the decode of the outputs.
+// only the features, the bias+ReLU epilogues and the decode of the outputs.
 //
 // Shared-memory operand layout (no swizzle, K-major): 8-row x 16-byte core
 // matrices; element (r, k) of a matrix with K columns sits at byte
@@ -137,23 +137,35 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
       : "memory");
 }
 
+// Starts moving the line holding p into L2 (no register is written).
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+// max(lo, 0) and max(hi, 0) rounded to BF16 and packed, lo in the low half:
+// one instruction (the PTX convert packs its first operand in the high half).
+__device__ __forceinline__ uint32_t pack_relu_bf16(float lo, float hi) {
+  uint32_t d;
+  asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+  return d;
+}
+
 __device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
   asm volatile("st.shared.v4.b32 [%0], {%1,%2,%3,%4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d) : "memory");
 }
 
 // 32 columns (this warpgroup's) of a layer's output for this thread's channel
-// (TMEM lane = row) -> bias + GELU -> BF16 into the next layer's A operand
+// (TMEM lane = row) -> bias + ReLU -> BF16 into the next layer's A operand
 // (K = 128): k groups 4 cg .. 4 cg + 3 of the row, 16 columns at a time.
-__device__ __forceinline__ void gelu_epilogue(uint32_t tm, const float* bias, uint32_t hrow) {
+__device__ __forceinline__ void relu_epilogue(uint32_t tm, const float* bias, uint32_t hrow) {
 #pragma unroll
   for (int half = 0; half < 2; ++half) {
     uint32_t r[16];
     tmem_ld16(tm + 16u * half, r);
     uint32_t p[8];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const float2 bb = *reinterpret_cast<const float2*>(bias + 16 * half + 2 * j);
-      p[j] = pack_bf16(gelu_fast(__uint_as_float(r[2 * j]) + bb.x), gelu_fast(__uint_as_float(r[2 * j + 1]) + bb.y));
+    for (int q = 0; q < 4; ++q) {
+      const float4 bb = *reinterpret_cast<const float4*>(bias + 16 * half + 4 * q);
+      p[2 * q] = pack_relu_bf16(__uint_as_float(r[4 * q]) + bb.x, __uint_as_float(r[4 * q + 1]) + bb.y);
+      p[2 * q + 1] = pack_relu_bf16(__uint_as_float(r[4 * q + 2]) + bb.z, __uint_as_float(r[4 * q + 3]) + bb.w);
     }
     st_shared_v4(hrow + (2 * half) * 128, p[0], p[1], p[2], p[3]);
     st_shared_v4(hrow + (2 * half + 1) * 128, p[4], p[5], p[6], p[7]);
@@ -269,7 +281,7 @@ __global__ void __launch_bounds__(kThreads, 2) mlp_infer_tc_kernel(const MlpInfe
                  pack_bf16(f[14], f[15]));
   };
   auto epilogue = [&](int s, const float* bias) {
-    gelu_epilogue(slot_tm(s) + lane_off + 32u * cg, bias + 32 * cg, slot_h(s) + kmaj(row, 32 * cg, MLP_H));
+    relu_epilogue(slot_tm(s) + lane_off + 32u * cg, bias + 32 * cg, slot_h(s) + kmaj(row, 32 * cg, MLP_H));
   };
   // the outputs of channel i from columns 0..31 of slot s's layer 3
   auto decode = [&](int s, int64_t i, bool mine, float scale) {
@@ -322,6 +334,17 @@ __global__ void __launch_bounds__(kThreads, 2) mlp_infer_tc_kernel(const MlpInfe
     issue(0, 1);
     issue(1, 1);
     if (!wait(0)) { dead = true; break; }
+    // the samples of the channels whose features this thread computes at the
+    // end of this pair start towards L2 now, four stages ahead of their use
+    if (cg >= 2 && t0 + stride < tiles) {
+      const int64_t i = chan(t0 + stride, cg - 2);
+      if (i < a.n) {
+        const double* sp = a.samples + i * a.sample_stride;
+        prefetch_l2(sp);
+        prefetch_l2(sp + 9);  // the row of 10 samples may cross a line
+        prefetch_l2(a.pederr + i);
+      }
+    }
     epilogue(0, S.b1);
     stage_sync();
     issue(0, 2);

@@ -183,10 +183,10 @@ int mlp_train(MlpState& s, const HostTables& tab, int64_t n, int sample_stride, 
       g.B = s.W1h; g.b_sj = MLP_IN; g.b_sk = 1;
       g.M = B; g.N = MLP_H; g.K = MLP_IN; g.k_split = MLP_IN;
       g.C = Z1; g.ldc = MLP_H; g.bias = s.params + P_B1; g.H = H1; g.ldh = MLP_H;
-      e = launch_gemm(EPI_BIAS_GELU, true, true, g, 1, st);
+      e = launch_gemm(EPI_BIAS_RELU, true, true, g, 1, st);
       g.A = H1; g.a_si = MLP_H; g.B = s.W2h; g.b_sj = MLP_H; g.K = MLP_H; g.k_split = MLP_H;
       g.C = Z2; g.bias = s.params + P_B2; g.H = H2;
-      if (e == cudaSuccess) e = launch_gemm(EPI_BIAS_GELU, true, true, g, 1, st);
+      if (e == cudaSuccess) e = launch_gemm(EPI_BIAS_RELU, true, true, g, 1, st);
       g.A = H2; g.B = s.W3h; g.N = MLP_OUT; g.C = O; g.ldc = MLP_OUT; g.bias = s.params + P_B3; g.H = nullptr;
       if (e == cudaSuccess) e = launch_gemm(EPI_BIAS, true, true, g, 1, st);
       if (e != cudaSuccess) break;
@@ -205,7 +205,7 @@ int mlp_train(MlpState& s, const HostTables& tab, int64_t n, int sample_stride, 
       g.B = s.W3t; g.b_sj = MLP_OUT; g.b_sk = 1;
       g.M = B; g.N = MLP_H; g.K = MLP_OUT; g.k_split = MLP_OUT; g.C = dH2; g.ldc = MLP_H;
       if (e == cudaSuccess) e = launch_gemm(EPI_STORE, true, true, g, 1, st);
-      gelu_backward_kernel<<<blocks(int64_t(B) * MLP_H, 256), 256, 0, st>>>(int64_t(B) * MLP_H, dH2, Z2, dZ2);
+      relu_backward_kernel<<<blocks(int64_t(B) * MLP_H, 256), 256, 0, st>>>(int64_t(B) * MLP_H, dH2, Z2, dZ2);
       // layer 2 gradients
       std::memset(&g, 0, sizeof(g));
       g.A = dZ2; g.a_si = 1; g.a_sk = MLP_H;
@@ -218,7 +218,7 @@ int mlp_train(MlpState& s, const HostTables& tab, int64_t n, int sample_stride, 
       g.B = s.W2t; g.b_sj = MLP_H; g.b_sk = 1;
       g.M = B; g.N = MLP_H; g.K = MLP_H; g.k_split = MLP_H; g.C = dH1; g.ldc = MLP_H;
       if (e == cudaSuccess) e = launch_gemm(EPI_STORE, true, true, g, 1, st);
-      gelu_backward_kernel<<<blocks(int64_t(B) * MLP_H, 256), 256, 0, st>>>(int64_t(B) * MLP_H, dH1, Z1, dZ1);
+      relu_backward_kernel<<<blocks(int64_t(B) * MLP_H, 256), 256, 0, st>>>(int64_t(B) * MLP_H, dH1, Z1, dZ1);
       // layer 1 gradients
       std::memset(&g, 0, sizeof(g));
       g.A = dZ1; g.a_si = 1; g.a_sk = MLP_H;
