@@ -828,26 +828,31 @@ int mf_fit_count_flops(mf_context* c, const mf_batch* b, const mf_options* o, do
 
 // Chunk boundaries of a host-pointer fit: offs[0] = 0 < ... < offs[k] = n,
 // returns k. Full chunks of B = MIXED_CHUNK channels with a ramp of B/4 and
-// B/2 at both ends: only the first chunk's copy-in and the last chunk's
-// copy-out are not hidden under a fit (88 B in and 99 B out per channel at
-// ~200 GB/s each way against ~0.76 ns of fit per channel). Measured on 10M
-// warm channels (e2e ms per step): 8.74 with this rule, 8.80 with B halved,
-// 9.53 with B quartered, 9.02 without the ramp; the device fit alone 7.55.
-// Batches too small for the ramp are cut into up to eight equal chunks of at
-// least B/8.
-int host_chunks(int64_t n, int64_t* offs) {
+// B/2 at both ends (with `taper`, B/2, B/4 and B/8 at the end): only the first
+// chunk's copy-in and the last chunk's copy-out are not hidden under a fit
+// (88 B in and 99 B out per channel; the link carries 211 GB/s host to
+// device, 193 GB/s back, 327 GB/s both ways at once). Measured on 10M warm
+// channels (e2e ms per step, device fit 7.55 ms at the time): 8.74 with this
+// rule, 8.80 with B halved, 9.53 with B quartered, 9.02 without the ramp; the
+// B/8 taper takes 0.03 ms more off the warm pipeline, where the last copy-out
+// is on the critical path. Batches too small for the ramp are cut into up to
+// eight equal chunks of at least B/8.
+int host_chunks(int64_t n, int64_t* offs, bool taper) {
   constexpr int64_t B = MIXED_CHUNK, R = B / 8;
-  constexpr int64_t ramp[2] = {B / 4, B / 2};
-  constexpr int64_t ramp_sum = B / 4 + B / 2;
+  constexpr int64_t up[2] = {B / 4, B / 2};
+  constexpr int64_t down[2][3] = {{B / 2, B / 4, 0}, {B / 2, B / 4, B / 8}};
+  const int64_t* dn = down[taper ? 1 : 0];
+  const int ndown = taper ? 3 : 2;
+  const int64_t ramp_sum = up[0] + up[1] + dn[0] + dn[1] + dn[2];
   int k = 0;
   offs[0] = 0;
-  if (n >= 2 * ramp_sum + B) {
-    for (int64_t r : ramp) offs[k + 1] = offs[k] + r, ++k;
-    const int64_t middle = n - 2 * ramp_sum;
+  if (n >= ramp_sum + B) {
+    for (int64_t r : up) offs[k + 1] = offs[k] + r, ++k;
+    const int64_t middle = n - ramp_sum;
     int64_t parts = (middle + B - 1) / B;  // beyond the event slots the middle chunks grow past B
-    if (parts > mf_context::kHostChunks - 4) parts = mf_context::kHostChunks - 4;
+    if (parts > mf_context::kHostChunks - 5) parts = mf_context::kHostChunks - 5;
     for (int64_t p = 0; p < parts; ++p) offs[k + 1] = offs[2] + middle * (p + 1) / parts, ++k;
-    for (int j = 1; j >= 0; --j) offs[k + 1] = offs[k] + ramp[j], ++k;
+    for (int j = 0; j < ndown; ++j) offs[k + 1] = offs[k] + dn[j], ++k;
   } else {
     int64_t parts = (n + R - 1) / R;
     if (parts > 8) parts = 8;
@@ -859,13 +864,23 @@ int host_chunks(int64_t n, int64_t* offs) {
 
 // Host-pointer fit, pipelined: the batch is cut into chunks (host_chunks); the
 // copy-in of chunk i+1 (h2d stream) and the copy-out of chunk i-1 (d2h stream)
-// run under the fit of chunk i, ordered by events. The mixed forms fit even
-// chunks on the context stream and odd chunks on a second stream with its own
-// workspace (lane 1), so neighbouring fits overlap (one chunk's queue kernels,
-// whose time is set by their slowest channels, run beside the next chunk's
-// search); chunk i + 2 reuses chunk i's lane on the same stream. The FP64 form and per-kernel profiling keep
-// one stream. With pinned host buffers the step costs about max(copies, fit)
-// instead of their sum.
+// run under the fit of chunk i, ordered by events. With pinned host buffers
+// the step costs about max(copies, fit) instead of their sum. Two shapes:
+// - cold starts of the mixed and FP32 forms (fit 9-12 ms per 10M channels
+//   against 5.7 ms of copies): even chunks fit on the context stream and odd
+//   chunks on a second stream with its own workspace (lane 1), so
+//   neighbouring fits overlap (one chunk's queue kernels, whose time is set by
+//   their slowest channels, run beside the next chunk's search); chunk i + 2
+//   reuses chunk i's lane on the same stream;
+// - the warm start (fit 5.8 ms, as long as the copies): chunks fit in order
+//   on one stream, so each chunk's copy-out starts as early as it can; the
+//   copy-in of chunk i waits for the fit of chunk i - 2, leaving the link to
+//   the copy-outs once the next two inputs are in; the last chunks taper to
+//   B/8. Measured on 10M channels (e2e ms per step): warm 7.53 two lanes,
+//   7.31 one lane with the throttle and the taper; cold FP32 9.74 two lanes vs
+//   9.89 one, cold mixed 12.52 vs 13.29, ECAL/HCAL persistent FP32 10.21 vs
+//   11.04.
+// The FP64 form and per-kernel profiling keep one stream.
 int mf_fit_host(mf_context* c, const mf_batch* hb, const mf_options* o) {
   if (!c || !hb) return MF_EINVAL;
   std::lock_guard<std::mutex> g(c->mu);
@@ -896,9 +911,10 @@ int mf_fit_host(mf_context* c, const mf_batch* hb, const mf_options* o) {
     set_last_error("mf_fit_host: stream/event setup", e);
     return MF_ECUDA;
   }
+  const bool warm = o->warm_start == MF_WARM_MLP;
   int64_t offs[mf_context::kHostChunks + 1];
-  const int nchunks = host_chunks(n, offs);
-  const bool two = nchunks > 1 && !c->timer.ev &&
+  const int nchunks = host_chunks(n, offs, warm);
+  const bool two = nchunks > 1 && !c->timer.ev && !warm &&
                    (o->precision == MF_PREC_MIXED || o->precision == MF_PREC_FP32);
   if (two) {
     rc = grow_lane1(c);
@@ -913,7 +929,8 @@ int mf_fit_host(mf_context* c, const mf_batch* hb, const mf_options* o) {
   };
   for (int i = 0; i < nchunks && e == cudaSuccess && rc == MF_OK; ++i) {
     const int64_t off = offs[i], m = offs[i + 1] - offs[i];
-    // copy in
+    // copy in (the warm start: at most two chunks ahead of the fits)
+    if (warm && i >= 2 && e == cudaSuccess) e = cudaStreamWaitEvent(c->h2d_stream, c->fit_done[i - 2], 0);
     cp(c->d_samples + off * ss, hb->samples + off * ss, sizeof(double) * m * ss, cudaMemcpyHostToDevice, c->h2d_stream);
     cp(c->d_pederr + off, hb->pederr + off, sizeof(double) * m, cudaMemcpyHostToDevice, c->h2d_stream);
     if (hb->ctype) cp(c->d_ctype + off, hb->ctype + off, m, cudaMemcpyHostToDevice, c->h2d_stream);

@@ -54,13 +54,21 @@ def fit_fixture(mf, cuda, d, options):
     return o
 
 
+def _has_fpc(name):
+    with np.load(os.path.join(GOLDEN, f"fits_{name}.npz")) as z:
+        return "fullpulsecov" in z.files
+
+
+# (fixture, errors): every fixture with MINOS errors; without errors only the
+# fixtures with a pulse covariance (the others are served by the tables)
+CASES = [(name, errors) for name in ["ecal_fpc", "ecal_c0", "ecal_logamp", "hcal", "edge"] for errors in (0, 1)
+         if errors or _has_fpc(name)]
+
+
 @pytest.mark.parametrize("prec", PRECS)
-@pytest.mark.parametrize("errors", [0, 1])
-@pytest.mark.parametrize("name", ["ecal_fpc", "ecal_c0", "ecal_logamp", "hcal", "edge"])
+@pytest.mark.parametrize("name,errors", CASES)
 def test_per_channel_form_on_fixtures(mf, cuda, name, errors, prec):
     d = dict(np.load(os.path.join(GOLDEN, f"fits_{name}.npz")))
-    if not errors and "fullpulsecov" not in d:
-        pytest.skip("without a pulse covariance or errors the tables serve this fixture")
     mode = "err" if errors else "kkt"
     o = fit_fixture(mf, cuda, d, mf.default_options(precision=prec_of(mf, prec), max_iter_nnls=1000,
                                                      compute_errors=errors))
