@@ -278,7 +278,9 @@ int mf_mlp_param_count(void);
 int mf_mlp_init(mf_context* ctx, int ctype, uint64_t seed);
 /* Trains on device data: batch.samples/pederr/ctype are the inputs and
  * batch.amplitudes holds their converged fits (the targets). Writes the mean
- * loss of each epoch to epoch_loss (host, may be NULL). Synchronous. */
+ * loss of each epoch to epoch_loss (host, may be NULL). Synchronous. Its
+ * GEMMs run on the tensor cores (tcgen05) with bounded waits: MF_ETIMEOUT if
+ * one gave up (the network is then left untrained). */
 int mf_mlp_train(mf_context* ctx, const mf_batch* data, const mf_mlp_train_params* p, float* epoch_loss, void* stream);
 /* Gradient check: one forward/backward on the first p->batch channels of
  * `data` without an update. Host outputs: grads[mf_mlp_param_count()], the

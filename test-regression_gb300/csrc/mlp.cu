@@ -4,12 +4,12 @@
 // Network: 16 inputs (10 normalised whitened samples, log SNR, pederr, zero
 // padding) -> 128 -> ReLU -> 128 -> ReLU -> 32 outputs (10 passive-set logits,
 // 10 amplitude outputs, padding). BF16 weights and activations on the tensor
-// cores, FP32 accumulate; FP32 master weights, Adam. Training runs its GEMMs
-// as mma.sync m16n8k16 tiles; inference runs on tcgen05 (mlp_tc.cu).
+// cores, FP32 accumulate; FP32 master weights, Adam. Training and inference
+// (mlp_tc.cu) both run their GEMMs on tcgen05 with FP32 accumulators in TMEM.
 //
 // Kernels:
 //   mlp_features_kernel   channel -> feature row (bf16) + per-channel scale
-//   gemm_kernel<EPI,..>   C = A * B^T for every training GEMM (forward layers,
+//   gemm_tc_kernel<EPI,..> C = A * B^T for every training GEMM (forward layers,
 //                         input gradients, split-K weight gradients)
 //   loss_kernel           BCE on the logits + MSE on softplus(amplitude outputs)
 //   relu_backward_kernel, bias_grad_kernel, adam_kernel, pack_weights_kernel
@@ -23,107 +23,176 @@
 #include "mf_internal.h"
 #include "mlp.h"
 #include "mlp_common.cuh"
+#include "tc_common.cuh"
 
 namespace mfgb {
 namespace {
 
 typedef __nv_bfloat16 bf16;
 
-constexpr int BM = 64, BN = 64, BK = 32, PAD = 8;
+using namespace tc;
 
-// Warp-level 32x32 tile product over one BK slice held in shared memory
-// (row-major [rows][BK+PAD], k contiguous), accumulating into acc[2][4][4].
-__device__ __forceinline__ void warp_tile_mma(const bf16 (*As)[BK + PAD], const bf16 (*Bs)[BK + PAD], int wm, int wn,
-                                              float (&acc)[2][4][4]) {
-  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+// Training GEMM on the 5th-generation tensor cores: one CTA of 128 threads
+// computes a 128 x 32 tile of C (rows m0.., columns j0..; one TMEM
+// accumulator of 128 lanes x 32 columns). Per round the threads stage up to
+// 64 of its K into shared memory in the no-swizzle K-major layout (element
+// (i, k) of op(X) is X[i*si + k*sk]; KC picks the coalescing direction: k
+// contiguous -- then 16-byte loads, one core-matrix row each -- or i
+// contiguous for the transposed operands of the weight gradients;
+// out-of-range elements are zero), one thread issues the round's
+// tcgen05.mma (M = 128, N = 16 or 32, K = 16 per instruction) and commits it
+// to the CTA's mbarrier, and all wait for it before the next staging. The
+// epilogue reads the accumulator back with tcgen05.ld: warp w holds rows
+// 32 w .. 32 w + 31. A wait that gives up (0.2 s) sets MLP_ERR_TRAIN_TIMEOUT
+// in the error word, waits once more (bounded) for the MMAs in flight, skips
+// the epilogue and frees the TMEM.
+constexpr int TM = 128;  // rows per CTA = MMA M = TMEM lanes
+constexpr int TN = 32;   // columns per CTA
+constexpr int TKC = 64;  // K staged per round
+constexpr uint32_t kGemmTmemCols = 32;
+constexpr uint64_t kGemmWaitNs = 200000000ull;
+
+struct GemmSmem {
+  bf16 A[TM * TKC];  // 16 KB
+  bf16 B[TN * TKC];  // 4 KB
+  unsigned long long bar;
+  uint32_t tmem;
+};
+// at most 10 CTAs of this size fit an SM's shared memory: 10 x 32 TMEM
+// columns, within the SM's 512, so tcgen05.alloc never waits
+constexpr size_t kGemmSmem = sizeof(GemmSmem);
+static_assert(233472 / (kGemmSmem + 1024) * kGemmTmemCols <= 512, "TMEM per SM");
+
+extern __shared__ __align__(128) unsigned char gemm_smem_raw[];
+
+template <bool KC>
+__device__ __forceinline__ void stage_tile(bf16* S, const bf16* X, int64_t si, int64_t sk, int i0, int k0, int I,
+                                           int kend, int rows, int kc) {
+  unsigned char* base = reinterpret_cast<unsigned char*>(S);
+  if (KC && sk == 1 && si % 8 == 0 && (reinterpret_cast<uintptr_t>(X) & 15) == 0) {
+    // 8 consecutive k of a row = one 16-byte core-matrix row
+    const int groups = kc / 8;
+    for (int e = threadIdx.x; e < rows * groups; e += blockDim.x) {
+      const int i = e / groups, g = e % groups;
+      const int gi = i0 + i, gk = k0 + 8 * g;
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (gi < I) {
+        const bf16* src = X + int64_t(gi) * si + gk;
+        if (gk + 8 <= kend) {
+          v = *reinterpret_cast<const uint4*>(src);
+        } else {
+          bf16 t[8];
 #pragma unroll
-  for (int kk = 0; kk < BK; kk += 16) {
-    uint32_t a[2][4], b[4][2];
-#pragma unroll
-    for (int mi = 0; mi < 2; ++mi) {
-      const int r = wm + mi * 16 + g;
-      a[mi][0] = ld32(&As[r][kk + 2 * t]);
-      a[mi][1] = ld32(&As[r + 8][kk + 2 * t]);
-      a[mi][2] = ld32(&As[r][kk + 8 + 2 * t]);
-      a[mi][3] = ld32(&As[r + 8][kk + 8 + 2 * t]);
+          for (int q = 0; q < 8; ++q) t[q] = gk + q < kend ? src[q] : __float2bfloat16(0.f);
+          v = *reinterpret_cast<const uint4*>(t);
+        }
+      }
+      *reinterpret_cast<uint4*>(base + kmaj(i, 8 * g, kc)) = v;
     }
-#pragma unroll
-    for (int ni = 0; ni < 4; ++ni) {
-      const int c = wn + ni * 8 + g;
-      b[ni][0] = ld32(&Bs[c][kk + 2 * t]);
-      b[ni][1] = ld32(&Bs[c][kk + 8 + 2 * t]);
-    }
-#pragma unroll
-    for (int mi = 0; mi < 2; ++mi)
-#pragma unroll
-      for (int ni = 0; ni < 4; ++ni) mma_bf16(acc[mi][ni], a[mi], b[ni]);
+    return;
   }
-}
-
-// Loads a BM x BK (or BN x BK) tile of op(X) into shared memory. Element
-// (i, k) of op(X) is X[i*si + k*sk]; KC selects the coalescing direction
-// (k contiguous or i contiguous). Out-of-range elements are zero.
-template <bool KC, int ROWS>
-__device__ __forceinline__ void load_tile(bf16 (*S)[BK + PAD], const bf16* X, int64_t si, int64_t sk, int i0, int k0,
-                                          int I, int Kend) {
-  const int tid = threadIdx.x;
-#pragma unroll
-  for (int e = tid; e < ROWS * BK; e += 128) {
+  for (int e = threadIdx.x; e < rows * kc; e += blockDim.x) {
     int i, k;
     if (KC) {
-      i = e / BK;
-      k = e % BK;
+      i = e / kc;
+      k = e % kc;
     } else {
-      k = e / ROWS;
-      i = e % ROWS;
+      k = e / rows;
+      i = e % rows;
     }
     const int gi = i0 + i, gk = k0 + k;
     bf16 v = __float2bfloat16(0.f);
-    if (gi < I && gk < Kend) v = X[gi * si + gk * sk];
-    S[i][k] = v;
+    if (gi < I && gk < kend) v = X[int64_t(gi) * si + int64_t(gk) * sk];
+    *reinterpret_cast<bf16*>(base + kmaj(i, k, kc)) = v;
   }
 }
 
 template <int EPI, bool AKC, bool BKC>
-__global__ void __launch_bounds__(128) gemm_kernel(const GemmArgs p) {
-  __shared__ __align__(16) bf16 As[BM][BK + PAD];
-  __shared__ __align__(16) bf16 Bs[BN][BK + PAD];
-  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+__global__ void __launch_bounds__(128) gemm_tc_kernel(const GemmArgs p) {
+  GemmSmem& S = *reinterpret_cast<GemmSmem*>(gemm_smem_raw);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.x * TM, j0 = blockIdx.y * TN;
+  const int ncols = min(TN, p.N - j0);
+  const int ntile = (ncols + 15) & ~15;  // MMA N: 16 or 32
   const int kbeg = blockIdx.z * p.k_split;
   const int kend = min(p.K, kbeg + p.k_split);
-  const int warp = threadIdx.x >> 5;
-  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
-  float acc[2][4][4] = {};
-  for (int k0 = kbeg; k0 < kend; k0 += BK) {
-    load_tile<AKC, BM>(As, p.A, p.a_si, p.a_sk, m0, k0, p.M, kend);
-    load_tile<BKC, BN>(Bs, p.B, p.b_sj, p.b_sk, n0, k0, p.N, kend);
-    __syncthreads();
-    warp_tile_mma(As, Bs, wm, wn, acc);
-    __syncthreads();
+  const uint32_t bar = smem_u32(&S.bar);
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&S.tmem)),
+                 "r"(kGemmTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = S.tmem;
+  const uint32_t id = idesc_bf16(TM, ntile);
+  constexpr uint64_t kStep = 256 >> 4;  // descriptor advance of one K = 16 step
+  const bf16* Bj = p.B + int64_t(j0) * p.b_sj;
+  uint32_t phase = 0;
+  bool ok = true, any = false;
+  for (int k0 = kbeg; k0 < kend; k0 += TKC) {
+    const int kc = min(TKC, (kend - k0 + 15) & ~15);  // this round's K: 16, 32, 48 or 64
+    stage_tile<AKC>(S.A, p.A, p.a_si, p.a_sk, m0, k0, p.M, kend, TM, kc);
+    stage_tile<BKC>(S.B, Bj, p.b_sj, p.b_sk, 0, k0, ncols, kend, ntile, kc);
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (tid == 0) {
+      const uint64_t dA = sdesc(smem_u32(S.A), 128, uint32_t(kc) * 16);
+      const uint64_t dB = sdesc(smem_u32(S.B), 128, uint32_t(kc) * 16);
+      for (int kk = 0; kk < kc / 16; ++kk)
+        mma_bf16_tc(tmem, dA + kk * kStep, dB + kk * kStep, id, (any || kk > 0) ? 1u : 0u);
+      mma_commit(bar);
+    }
+    any = true;
+    ok = __syncthreads_and(mbar_wait(bar, phase, kGemmWaitNs));
+    if (!ok) break;
+    phase ^= 1u;
+    tc_fence_after();
+  }
+  if (!ok) {
+    if (tid == 0 && p.err) atomicOr(p.err, MLP_ERR_TRAIN_TIMEOUT);
+    mbar_wait(bar, phase, kGemmWaitNs);
+  } else if (any) {
+    const int row = m0 + warp * 32 + lane;
+    const bool live = row < p.M;
+    for (int c0 = 0; c0 < ntile; c0 += 16) {
+      uint32_t r[16];
+      __syncwarp();  // the TMEM load is warp-wide
+      tmem_ld16(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0), r);
+      if (live) {
 #pragma unroll
-  for (int mi = 0; mi < 2; ++mi)
-#pragma unroll
-    for (int ni = 0; ni < 4; ++ni)
-#pragma unroll
-      for (int h = 0; h < 4; ++h) {
-        const int r = m0 + wm + mi * 16 + g + (h >= 2 ? 8 : 0);
-        const int c = n0 + wn + ni * 8 + 2 * t + (h & 1);
-        if (r >= p.M || c >= p.N) continue;
-        const float v = acc[mi][ni][h];
-        if (EPI == EPI_BIAS_RELU) {
-          const float z = v + p.bias[c];
-          p.C[int64_t(r) * p.ldc + c] = z;
-          p.H[int64_t(r) * p.ldh + c] = __float2bfloat16(relu(z));
-        } else if (EPI == EPI_BIAS) {
-          p.C[int64_t(r) * p.ldc + c] = v + p.bias[c];
-        } else if (EPI == EPI_STORE) {
-          p.C[int64_t(r) * p.ldc + c] = v;
-        } else {  // EPI_ATOMIC: split-K accumulation of a weight gradient
-          atomicAdd(&p.C[int64_t(r) * p.ldc + c], v);
+        for (int j = 0; j < 16; ++j) {
+          if (c0 + j >= ncols) break;
+          const int c = j0 + c0 + j;
+          const float v = __uint_as_float(r[j]);
+          if (EPI == EPI_BIAS_RELU) {
+            const float z = v + p.bias[c];
+            p.C[int64_t(row) * p.ldc + c] = z;
+            p.H[int64_t(row) * p.ldh + c] = __float2bfloat16(relu(z));
+          } else if (EPI == EPI_BIAS) {
+            p.C[int64_t(row) * p.ldc + c] = v + p.bias[c];
+          } else if (EPI == EPI_STORE) {
+            p.C[int64_t(row) * p.ldc + c] = v;
+          } else {  // EPI_ATOMIC: split-K accumulation of a weight gradient
+            atomicAdd(&p.C[int64_t(row) * p.ldc + c], v);
+          }
         }
       }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kGemmTmemCols) : "memory");
 }
 
 }  // namespace
@@ -224,11 +293,12 @@ __global__ void pack_weights_kernel(const float* w, bf16* wh, bf16* wt, int out,
 // launchers
 // --------------------------------------------------------------------------
 cudaError_t launch_gemm(int epi, bool akc, bool bkc, const GemmArgs& p, int splits, cudaStream_t s) {
-  dim3 grid((p.N + BN - 1) / BN, (p.M + BM - 1) / BM, splits);
-#define MF_GEMM_CASE(E, A, B)                                          \
-  if (epi == E && akc == A && bkc == B) {                              \
-    gemm_kernel<E, A, B><<<grid, 128, 0, s>>>(p);                      \
-    return cudaGetLastError();                                         \
+  if (p.N < 1 || p.M < 1 || p.K < 1 || p.k_split < 1 || splits < 1) return cudaErrorInvalidValue;
+  const dim3 grid(unsigned((p.M + TM - 1) / TM), unsigned((p.N + TN - 1) / TN), unsigned(splits));
+#define MF_GEMM_CASE(E, A, B)                                                \
+  if (epi == E && akc == A && bkc == B) {                                    \
+    gemm_tc_kernel<E, A, B><<<grid, 128, kGemmSmem, s>>>(p);                 \
+    return cudaGetLastError();                                               \
   }
   MF_GEMM_CASE(EPI_BIAS_RELU, true, true)
   MF_GEMM_CASE(EPI_BIAS, true, true)

@@ -26,6 +26,7 @@ struct GemmArgs {
   const float* bias;
   __nv_bfloat16* H;  // EPI_BIAS_RELU: bf16 ReLU output
   int ldh;
+  unsigned* err;     // error word: MLP_ERR_TRAIN_TIMEOUT when a tensor-core wait gives up
 };
 
 struct MlpFeatArgs {
@@ -65,7 +66,8 @@ struct MlpInferArgs {
 };
 
 // Bits of the inference error word.
-constexpr unsigned MLP_ERR_TIMEOUT = 1u;  // a bounded wait on the tensor cores gave up
+constexpr unsigned MLP_ERR_TIMEOUT = 1u;        // a bounded wait of the inference on the tensor cores gave up
+constexpr unsigned MLP_ERR_TRAIN_TIMEOUT = 2u;  // ... of a training GEMM
 
 __global__ void mlp_features_kernel(const MlpFeatArgs a);
 __global__ void mlp_targets_kernel(int64_t n, const double* amp, int amp_stride, const float* scale,

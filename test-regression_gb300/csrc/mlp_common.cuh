@@ -1,24 +1,9 @@
-// Device helpers shared by the MLP kernels (training, inference, fused warm fit).
+// Device helpers shared by the MLP kernels (training and inference).
 #pragma once
 #include <cuda_bf16.h>
 #include <stdint.h>
 
 namespace mfgb {
-
-// D += A * B on the tensor cores: m16n8k16, BF16 operands, FP32 accumulate.
-// A fragment (row-major 16x16): a[0] = rows g, k 2t..2t+1; a[1] = rows g+8;
-// a[2] = rows g, k 8+2t..; a[3] = rows g+8, k 8+2t... B fragment (16x8,
-// "col"): b[0] = k 2t..2t+1 of column g, b[1] = k 8+2t... D: d[0..1] = row g,
-// columns 2t, 2t+1; d[2..3] = row g+8. (g = lane / 4, t = lane % 4.)
-__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-__device__ __forceinline__ uint32_t ld32(const __nv_bfloat16* p) { return *reinterpret_cast<const uint32_t*>(p); }
 
 // Two floats -> one register holding two BF16 (first in the low half).
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {

@@ -179,6 +179,7 @@ int mlp_train(MlpState& s, const HostTables& tab, int64_t n, int sample_stride, 
       GemmArgs g;
       // forward
       std::memset(&g, 0, sizeof(g));
+      g.err = s.infer_err;
       g.A = Xb; g.a_si = MLP_IN; g.a_sk = 1;
       g.B = s.W1h; g.b_sj = MLP_IN; g.b_sk = 1;
       g.M = B; g.N = MLP_H; g.K = MLP_IN; g.k_split = MLP_IN;
@@ -193,14 +194,16 @@ int mlp_train(MlpState& s, const HostTables& tab, int64_t n, int sample_stride, 
       mlp_loss_kernel<<<blocks(B, 256), 256, 0, st>>>(B, O, Tb, tp.amp_weight, dO, loss + ep);
       e = cudaMemsetAsync(s.grads, 0, sizeof(float) * P_COUNT, st);
       // layer 3 gradients
-      const int ks = 512, splits = (B + ks - 1) / ks;
+      const int ks = 256, splits = (B + ks - 1) / ks;
       std::memset(&g, 0, sizeof(g));
+      g.err = s.infer_err;
       g.A = dO; g.a_si = 1; g.a_sk = MLP_OUT;
       g.B = H2; g.b_sj = 1; g.b_sk = MLP_H;
       g.M = MLP_OUT; g.N = MLP_H; g.K = B; g.k_split = ks; g.C = s.grads + P_W3; g.ldc = MLP_H;
       if (e == cudaSuccess) e = launch_gemm(EPI_ATOMIC, false, false, g, splits, st);
       bias_grad_kernel<<<64, MLP_OUT, 0, st>>>(B, MLP_OUT, dO, s.grads + P_B3);
       std::memset(&g, 0, sizeof(g));
+      g.err = s.infer_err;
       g.A = dO; g.a_si = MLP_OUT; g.a_sk = 1;
       g.B = s.W3t; g.b_sj = MLP_OUT; g.b_sk = 1;
       g.M = B; g.N = MLP_H; g.K = MLP_OUT; g.k_split = MLP_OUT; g.C = dH2; g.ldc = MLP_H;
@@ -208,12 +211,14 @@ int mlp_train(MlpState& s, const HostTables& tab, int64_t n, int sample_stride, 
       relu_backward_kernel<<<blocks(int64_t(B) * MLP_H, 256), 256, 0, st>>>(int64_t(B) * MLP_H, dH2, Z2, dZ2);
       // layer 2 gradients
       std::memset(&g, 0, sizeof(g));
+      g.err = s.infer_err;
       g.A = dZ2; g.a_si = 1; g.a_sk = MLP_H;
       g.B = H1; g.b_sj = 1; g.b_sk = MLP_H;
       g.M = MLP_H; g.N = MLP_H; g.K = B; g.k_split = ks; g.C = s.grads + P_W2; g.ldc = MLP_H;
       if (e == cudaSuccess) e = launch_gemm(EPI_ATOMIC, false, false, g, splits, st);
       bias_grad_kernel<<<64, MLP_H, 0, st>>>(B, MLP_H, dZ2, s.grads + P_B2);
       std::memset(&g, 0, sizeof(g));
+      g.err = s.infer_err;
       g.A = dZ2; g.a_si = MLP_H; g.a_sk = 1;
       g.B = s.W2t; g.b_sj = MLP_H; g.b_sk = 1;
       g.M = B; g.N = MLP_H; g.K = MLP_H; g.k_split = MLP_H; g.C = dH1; g.ldc = MLP_H;
@@ -221,6 +226,7 @@ int mlp_train(MlpState& s, const HostTables& tab, int64_t n, int sample_stride, 
       relu_backward_kernel<<<blocks(int64_t(B) * MLP_H, 256), 256, 0, st>>>(int64_t(B) * MLP_H, dH1, Z1, dZ1);
       // layer 1 gradients
       std::memset(&g, 0, sizeof(g));
+      g.err = s.infer_err;
       g.A = dZ1; g.a_si = 1; g.a_sk = MLP_H;
       g.B = Xb; g.b_sj = 1; g.b_sk = MLP_IN;
       g.M = MLP_H; g.N = MLP_IN; g.K = B; g.k_split = ks; g.C = s.grads + P_W1; g.ldc = MLP_IN;
@@ -250,10 +256,25 @@ int mlp_train(MlpState& s, const HostTables& tab, int64_t n, int sample_stride, 
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     for (int ep = 0; ep < tp.epochs; ++ep) epoch_loss[ep] /= float(nb);
   }
+  if (e == cudaSuccess) {
+    // a bounded tensor-core wait of a training GEMM gave up: its products are
+    // missing from the weights, so the network is not trained
+    unsigned flags = 0;
+    e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaMemcpy(&flags, s.infer_err, sizeof(flags), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && (flags & MLP_ERR_TRAIN_TIMEOUT)) {
+      flags &= ~MLP_ERR_TRAIN_TIMEOUT;
+      e = cudaMemcpy(s.infer_err, &flags, sizeof(flags), cudaMemcpyHostToDevice);
+      if (e == cudaSuccess) {
+        set_last_error("mlp_train: a tensor-core wait of a training GEMM timed out", cudaSuccess);
+        rc = MF_ETIMEOUT;
+      }
+    }
+  }
   if (e != cudaSuccess) {
     set_last_error("mlp_train", e);
     rc = MF_ECUDA;
-  } else if (!probe) {
+  } else if (!probe && rc == MF_OK) {
     s.trained = true;
   }
   cudaStreamSynchronize(st);
