@@ -45,17 +45,21 @@ using namespace tc;
 // epilogue reads the accumulator back with tcgen05.ld: warp w holds rows
 // 32 w .. 32 w + 31. A wait that gives up (0.2 s) sets MLP_ERR_TRAIN_TIMEOUT
 // in the error word, waits once more (bounded) for the MMAs in flight, skips
-// the epilogue and frees the TMEM.
+// the epilogue and frees the TMEM (test_stall makes the first wait give up
+// after 1 ms on an mbarrier nothing arrives on).
 constexpr int TM = 128;  // rows per CTA = MMA M = TMEM lanes
 constexpr int TN = 32;   // columns per CTA
 constexpr int TKC = 64;  // K staged per round
 constexpr uint32_t kGemmTmemCols = 32;
 constexpr uint64_t kGemmWaitNs = 200000000ull;
 
+constexpr uint64_t kGemmTestWaitNs = 1000000ull;  // the timeout test's wait: 1 ms
+
 struct GemmSmem {
   bf16 A[TM * TKC];  // 16 KB
   bf16 B[TN * TKC];  // 4 KB
   unsigned long long bar;
+  unsigned long long never;  // nothing arrives on it (the timeout test's wait)
   uint32_t tmem;
 };
 // at most 10 CTAs of this size fit an SM's shared memory: 10 x 32 TMEM
@@ -116,9 +120,10 @@ __global__ void __launch_bounds__(128) gemm_tc_kernel(const GemmArgs p) {
   const int ntile = (ncols + 15) & ~15;  // MMA N: 16 or 32
   const int kbeg = blockIdx.z * p.k_split;
   const int kend = min(p.K, kbeg + p.k_split);
-  const uint32_t bar = smem_u32(&S.bar);
+  const uint32_t bar = smem_u32(&S.bar), never = smem_u32(&S.never);
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(never) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -152,7 +157,7 @@ __global__ void __launch_bounds__(128) gemm_tc_kernel(const GemmArgs p) {
       mma_commit(bar);
     }
     any = true;
-    ok = __syncthreads_and(mbar_wait(bar, phase, kGemmWaitNs));
+    ok = __syncthreads_and(p.test_stall ? mbar_wait(never, 0u, kGemmTestWaitNs) : mbar_wait(bar, phase, kGemmWaitNs));
     if (!ok) break;
     phase ^= 1u;
     tc_fence_after();

@@ -27,6 +27,7 @@ struct GemmArgs {
   __nv_bfloat16* H;  // EPI_BIAS_RELU: bf16 ReLU output
   int ldh;
   unsigned* err;     // error word: MLP_ERR_TRAIN_TIMEOUT when a tensor-core wait gives up
+  int test_stall;    // wait first on an mbarrier nothing arrives on (timeout test)
 };
 
 struct MlpFeatArgs {

@@ -180,6 +180,7 @@ int mlp_train(MlpState& s, const HostTables& tab, int64_t n, int sample_stride, 
       // forward
       std::memset(&g, 0, sizeof(g));
       g.err = s.infer_err;
+      g.test_stall = s.test_stall;
       g.A = Xb; g.a_si = MLP_IN; g.a_sk = 1;
       g.B = s.W1h; g.b_sj = MLP_IN; g.b_sk = 1;
       g.M = B; g.N = MLP_H; g.K = MLP_IN; g.k_split = MLP_IN;
@@ -197,6 +198,7 @@ int mlp_train(MlpState& s, const HostTables& tab, int64_t n, int sample_stride, 
       const int ks = 256, splits = (B + ks - 1) / ks;
       std::memset(&g, 0, sizeof(g));
       g.err = s.infer_err;
+      g.test_stall = s.test_stall;
       g.A = dO; g.a_si = 1; g.a_sk = MLP_OUT;
       g.B = H2; g.b_sj = 1; g.b_sk = MLP_H;
       g.M = MLP_OUT; g.N = MLP_H; g.K = B; g.k_split = ks; g.C = s.grads + P_W3; g.ldc = MLP_H;
@@ -204,6 +206,7 @@ int mlp_train(MlpState& s, const HostTables& tab, int64_t n, int sample_stride, 
       bias_grad_kernel<<<64, MLP_OUT, 0, st>>>(B, MLP_OUT, dO, s.grads + P_B3);
       std::memset(&g, 0, sizeof(g));
       g.err = s.infer_err;
+      g.test_stall = s.test_stall;
       g.A = dO; g.a_si = MLP_OUT; g.a_sk = 1;
       g.B = s.W3t; g.b_sj = MLP_OUT; g.b_sk = 1;
       g.M = B; g.N = MLP_H; g.K = MLP_OUT; g.k_split = MLP_OUT; g.C = dH2; g.ldc = MLP_H;
@@ -212,6 +215,7 @@ int mlp_train(MlpState& s, const HostTables& tab, int64_t n, int sample_stride, 
       // layer 2 gradients
       std::memset(&g, 0, sizeof(g));
       g.err = s.infer_err;
+      g.test_stall = s.test_stall;
       g.A = dZ2; g.a_si = 1; g.a_sk = MLP_H;
       g.B = H1; g.b_sj = 1; g.b_sk = MLP_H;
       g.M = MLP_H; g.N = MLP_H; g.K = B; g.k_split = ks; g.C = s.grads + P_W2; g.ldc = MLP_H;
@@ -219,6 +223,7 @@ int mlp_train(MlpState& s, const HostTables& tab, int64_t n, int sample_stride, 
       bias_grad_kernel<<<64, MLP_H, 0, st>>>(B, MLP_H, dZ2, s.grads + P_B2);
       std::memset(&g, 0, sizeof(g));
       g.err = s.infer_err;
+      g.test_stall = s.test_stall;
       g.A = dZ2; g.a_si = MLP_H; g.a_sk = 1;
       g.B = s.W2t; g.b_sj = MLP_H; g.b_sk = 1;
       g.M = B; g.N = MLP_H; g.K = MLP_H; g.k_split = MLP_H; g.C = dH1; g.ldc = MLP_H;
@@ -227,6 +232,7 @@ int mlp_train(MlpState& s, const HostTables& tab, int64_t n, int sample_stride, 
       // layer 1 gradients
       std::memset(&g, 0, sizeof(g));
       g.err = s.infer_err;
+      g.test_stall = s.test_stall;
       g.A = dZ1; g.a_si = 1; g.a_sk = MLP_H;
       g.B = Xb; g.b_sj = 1; g.b_sk = MLP_IN;
       g.M = MLP_H; g.N = MLP_IN; g.K = B; g.k_split = ks; g.C = s.grads + P_W1; g.ldc = MLP_IN;
@@ -274,9 +280,8 @@ int mlp_train(MlpState& s, const HostTables& tab, int64_t n, int sample_stride, 
   if (e != cudaSuccess) {
     set_last_error("mlp_train", e);
     rc = MF_ECUDA;
-  } else if (!probe && rc == MF_OK) {
-    s.trained = true;
   }
+  if (!probe) s.trained = rc == MF_OK;  // a failed training has modified the weights
   cudaStreamSynchronize(st);
   void* ps[] = {X, H1, H2, dO, dZ2, dZ1, scale, T, Z1, Z2, O, dH2, dH1, loss, gnorm};
   for (void* p : ps) cudaFree(p);

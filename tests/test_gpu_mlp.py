@@ -227,5 +227,36 @@ def test_inference_timeout_reports_and_keeps_results(mf, cuda, mlp_engine):
         assert np.array_equal(again[k], warm[k]), k
 
 
+def test_training_timeout_reports_and_recovers(mf, cuda):
+    """The training GEMMs' bounded waits: with the test hook every tcgen05
+    wait of a training GEMM gives up after 1 ms (an mbarrier nothing arrives
+    on). mf_mlp_train returns MF_ETIMEOUT and leaves the network untrained (a
+    warm fit is refused with MF_ENOTRAINED); with the hook off the same
+    training succeeds and the warm fit runs."""
+    import ctypes as C
+
+    eng = mf.Engine(0)
+    eng.set_conditions(0, mf.synth_conditions(mf.SYNTH_ECAL)[0])
+    eng.mlp_init(0, seed=9)
+    tr = train_set(mf, cuda, eng, 8192, seed=45)
+    p = mf.mlp_params(epochs=1, batch=4096)
+    losses = np.zeros(1, dtype=np.float32)
+    eng.mlp_test_stall(True)
+    try:
+        rc = eng.lib.mf_mlp_train(eng.h, C.byref(tr.batch), C.byref(p), losses.ctypes.data, None)
+    finally:
+        eng.mlp_test_stall(False)
+    assert rc == mf.ETIMEOUT, rc
+    assert "timed out" in mf.load_library().mf_last_error().decode()
+    opt = mf.default_options(precision=mf.PREC_FP32, warm_start=mf.WARM_MLP, max_iter_nnls=1000)
+    inp = tr.inputs_host()
+    with pytest.raises(mf.MultifitError, match=rf"\({mf.ENOTRAINED}\)"):
+        eng.fit_host(inp["samples"][:1000], inp["pederr"][:1000], options=opt)
+    eng.mlp_train(tr.batch, p)  # hook off: trains, and the warm fit runs
+    out = eng.fit_host(inp["samples"][:1000], inp["pederr"][:1000], options=opt)
+    assert np.isfinite(out["amplitudes"]).all()
+    eng.close()
+
+
 def relerr_rows(a, r):
     return np.abs(a - r).max(axis=1) / np.maximum(np.abs(r).max(axis=1), 1e-300)
