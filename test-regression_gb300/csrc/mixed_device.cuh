@@ -709,14 +709,15 @@ __device__ __forceinline__ void judge_df_body(const MixedArgs& a, const DevMixed
       yl[i] = lo;
     }
   }
-  // Column by column: x_k = G_S^+_k y through the table's float pairs (a
-  // column outside the set reads the zero row), dx_k = sum_i |G^+_ki y_i| (the
-  // scale of x_k's round-off), then x_k enters the residual r = y - G x at
-  // once. The loop over the columns stays rolled: unrolled, the judge's body
-  // ran to ~6,000 instructions and instruction fetch was its first stall; the
-  // column's G entries come from the pair table in global memory, the same
-  // address in every lane. The amplitudes are written as they come; a
-  // channel the judge queues gets them rewritten by the fix or the repair.
+  // Column by column over the channel's passive set (its own trip count: a
+  // warp runs as many iterations as its largest set, where a loop over all K
+  // columns ran the inactive ones through a zero row as exact no-ops):
+  // x_k = G_S^+_k y through the table's float pairs, dx_k = sum_i |G^+_ki y_i|
+  // (the scale of x_k's round-off), then x_k enters the residual r = y - G x
+  // at once. The loop stays rolled: unrolled, the judge's body ran to ~6,000
+  // instructions and instruction fetch was its first stall. The amplitudes are
+  // written as they come; a channel the judge queues gets them rewritten by
+  // the fix or the repair.
   //
   // Round-off bounds, per channel. The table and y are exact to ~2^-48 and each
   // double-float multiply-add errs by ~2^-48 of its terms, so with N <= 10
@@ -738,14 +739,18 @@ __device__ __forceinline__ void judge_df_body(const MixedArgs& a, const DevMixed
   uint16_t support = 0;
   double xin = 0.;
   double* out = a.amplitudes + ch * a.amp_stride;
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+    if (!((m >> k) & 1u)) out[k] = 0.;
   {
     const int off = __ldg(T.offset + m);
-    int r = 0;
+    const int p = __popc(m);
+    unsigned rest = m;
 #pragma unroll 1
-    for (int k = 0; k < K; ++k) {
-      const bool inset = (m >> k) & 1u;
-      const int row = inset ? off + r * N : T.zero_row;
-      r += inset ? 1 : 0;
+    for (int r = 0; r < p; ++r) {
+      const int k = __ffs(rest) - 1;
+      rest &= rest - 1u;
+      const int row = off + r * N;
       float hi = 0.f, lo = 0.f, mag = 0.f;
       if constexpr (N % 2 == 0) {
         const float4* rp = reinterpret_cast<const float4*>(T.pinv2 + 2 * row);
@@ -767,7 +772,7 @@ __device__ __forceinline__ void judge_df_body(const MixedArgs& a, const DevMixed
         }
       }
       const float xb = 0x1p-44f * mag;
-      if (inset && !(hi > xb)) ok = false;
+      if (!(hi > xb)) ok = false;
       const float ek = fmaf(0x1p-44f, fabsf(hi), xb);
       // r -= G_k x_k (G's structural zeros add exact zeros)
       const float nh = -hi, nl = -lo;
