@@ -143,7 +143,8 @@ __device__ __forceinline__ void search_body_coop(const MixedArgs& a, const DevMi
       if (m & (1u << k)) x32[k] = fmaxf(wa[k], 1e-30f);
     if (m) solves += inner_loop<K>(m, x32, s32);
   }
-  for (int it = 0; it < a.max_iter32; ++it) {
+  const int iters = WARM ? kWarmSearchIters : a.max_iter32;
+  for (int it = 0; it < iters; ++it) {
     float wmax = 0.f;
     int imax = -1;
 #pragma unroll

@@ -293,6 +293,14 @@ __device__ __forceinline__ unsigned refine_screen(const DevMixed& T, const float
 // ---------------------------------------------------------------------------
 // FP32 active-set search
 // ---------------------------------------------------------------------------
+// Outer iterations of the search from a learned warm start. Nearly every
+// channel settles within two; the rare channel that keeps adding columns held
+// its whole warp, and after two iterations it is left to the judge, which
+// queues it for the fix (and, failing that, the repair) in full warps.
+// Measured on 10M warm channels: search 1.42 -> 1.00 ms (cap 4: 1.03, cap 1:
+// 0.93 with the queues 0.04 ms longer), same KKT points. Cold starts keep
+// max_iter32.
+constexpr int kWarmSearchIters = 2;
 // The FP32 search of channel ch (one lane): writes the hand-off (passive mask,
 // add and solve counts, FP32 amplitudes) for the FP64 judge.
 template <int N, int K, bool WARM>
@@ -331,7 +339,8 @@ __device__ __forceinline__ void search_body(const MixedArgs& a, const DevMixed& 
       if (m & (1u << k)) x32[k] = fmaxf(wa[k], 1e-30f);
     if (m) solves += inner_loop<K>(m, x32, s32);
   }
-  for (int it = 0; it < a.max_iter32; ++it) {
+  const int iters = WARM ? kWarmSearchIters : a.max_iter32;
+  for (int it = 0; it < iters; ++it) {
     float wmax = 0.f;
     int imax = -1;
 #pragma unroll
