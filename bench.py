@@ -199,7 +199,7 @@ def default_workload(form: str) -> str:
 # traffic is this times its channels); the summary with the command is the
 # profiles/ file given
 NCU_DRAM_BYTES_PER_CHANNEL = {
-    ("judge_kernel", "warm"): (179.2, "profiles/judge_kernel_fp32_warm-2m.md"),
+    ("judge_kernel", "warm"): (180.8, "profiles/judge_kernel_fp32_warm-2m.md"),
 }
 # useful FLOPs of one warm-start prediction: 12 inputs -> 128 -> 128 -> 20
 # outputs, 2 per multiply-add (the network pads to 16 inputs and 32 outputs)
@@ -273,17 +273,26 @@ def fp32_peak_tflops(torch) -> float:
     return best
 
 
-def judge_df_flops(P) -> int:
-    """FP32 flops of the double-float judge per channel of a set with pulse
-    matrix P (N x K): 17 per emulated FMA (TwoProduct 3, two cross FMAs 4,
-    renormalised sum 10) over the whitening N(N+1)/2, the dense table solve
-    K N and the residual over G's structural non-zeros, plus the FP32 KKT
-    screen (4 K N) and the double-float chi2 (15 N)."""
+def judge_df_flops(P, active) -> float:
+    """FP32 flops of the double-float judge summed over channels of a set
+    with pulse matrix P (N x K), given their passive sets `active` (int
+    tensor of bit masks): 17 per emulated FMA (TwoProduct 3, two cross FMAs
+    4, renormalised sum 10) over the whitening N(N+1)/2 and, per passive
+    column k, the table solve row (N) and the residual over G_k's structural
+    non-zeros (nnz_k); plus the FP32 KKT screen of the other columns
+    (4 N each) and the double-float chi2 (15 N). The judge loops over the
+    passive set only, so this is the work it has to do, not a dense K-column
+    count."""
     import numpy as np
+    import torch
 
     N, K = P.shape
-    nnz = int(sum(N - int(np.argmax(P[:, k] != 0)) if (P[:, k] != 0).any() else 0 for k in range(K)))
-    return 17 * (N * (N + 1) // 2 + K * N + nnz) + 4 * K * N + 15 * N
+    nnz = [N - int(np.argmax(P[:, k] != 0)) if (P[:, k] != 0).any() else 0 for k in range(K)]
+    bits = (active.to(torch.int32).unsqueeze(1) >> torch.arange(K, device=active.device, dtype=torch.int32)) & 1
+    per_col = torch.tensor([N + z for z in nnz], device=active.device, dtype=torch.int64)
+    p = bits.sum(dim=1, dtype=torch.int64)
+    df = 17 * (N * (N + 1) // 2 + (bits.to(torch.int64) * per_col).sum(dim=1)) + 4 * (K - p) * N + 15 * N
+    return float(df.sum().item())
 
 
 def fp64_peak_tflops(torch) -> float:
@@ -560,7 +569,7 @@ def run_ours(args, world, rank, local):
     bytes_per_launch = n * (10 * 8 + 8) + n * (10 * 8 + 8 + 8 + 2 + 1)
     hbm_gbs = bytes_per_launch / (step_ms * 1e-3) / 1e9
     kernel_table = kernel_rooflines(mf, eng, kernels, args, n, ctype, flops_per_launch, form_fp64_flops,
-                                    fp64_peak, fp32_peak, peaks, peak_src, step_ms)
+                                    fp64_peak, fp32_peak, peaks, peak_src, step_ms, mask)
     dominant = max(kernel_table, key=lambda k: kernel_table[k]["ms_per_step"])
     roof = dict(kernel_table[dominant])
     roof["kernel"] = dominant
@@ -622,13 +631,15 @@ def run_ours(args, world, rank, local):
 
 
 def kernel_rooflines(mf, eng, kernels, args, n, ctype, plain_flops, form_fp64_flops, fp64_peak, fp32_peak, peaks,
-                     peak_src, step_ms):
+                     peak_src, step_ms, active):
     """Roofline of every kernel launched in the timed region: its algorithmic
     work per launch over its mean launch time (CUDA events from mf_profile).
 
     fit_fp64_kernel: the plain fit's executed FP64 flops (instrumented count).
     judge_kernel: N(N+1) + 4NK FP64 flops per channel of its set (whitening,
-      dense passive-set solve, residual; FMA = 2).
+      dense passive-set solve, residual; FMA = 2); the double-float judge's
+      FP32 flops from each channel's passive set (judge_df_flops, with the
+      form's active masks `active`).
     repair_kernel: the rest of the form's counted FP64 flops.
     mlp_infer_tc_kernel: MLP_FLOPS_PER_CHANNEL on the tensor cores (BF16, tcgen05).
     search_kernel: FP32 and latency-bound; its HBM bytes (samples, pederr,
@@ -649,7 +660,8 @@ def kernel_rooflines(mf, eng, kernels, args, n, ctype, plain_flops, form_fp64_fl
             continue
         N, K = c.nsamples, c.npulses
         judge += m * (N * (N + 1) + 4 * N * K)
-        judge_df += m * judge_df_flops(mf.conditions_arrays(c)[0])
+        sel = active if ctype is None else active[ctype == t]
+        judge_df += judge_df_flops(mf.conditions_arrays(c)[0], sel)
     df_form = args.form in ("fp32", "warm", "fp32-cov")
     warm = args.form == "warm"
     out = {}
