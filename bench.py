@@ -288,11 +288,15 @@ def judge_df_flops(P, active) -> float:
 
     N, K = P.shape
     nnz = [N - int(np.argmax(P[:, k] != 0)) if (P[:, k] != 0).any() else 0 for k in range(K)]
-    bits = (active.to(torch.int32).unsqueeze(1) >> torch.arange(K, device=active.device, dtype=torch.int32)) & 1
-    per_col = torch.tensor([N + z for z in nnz], device=active.device, dtype=torch.int64)
-    p = bits.sum(dim=1, dtype=torch.int64)
-    df = 17 * (N * (N + 1) // 2 + (bits.to(torch.int64) * per_col).sum(dim=1)) + 4 * (K - p) * N + 15 * N
-    return float(df.sum().item())
+    bits = active.to(torch.int32)
+    cols = 0  # passive columns, summed over the channels
+    rows = 0  # table rows and G non-zeros of the passive columns, summed
+    for k in range(K):
+        c = int(((bits >> k) & 1).sum().item())
+        cols += c
+        rows += c * (N + nnz[k])
+    n = int(active.numel())
+    return float(17 * (n * N * (N + 1) // 2 + rows) + 4 * N * (n * K - cols) + 15 * N * n)
 
 
 def fp64_peak_tflops(torch) -> float:
