@@ -273,6 +273,19 @@ def fp32_peak_tflops(torch) -> float:
     return best
 
 
+def judge_fp64_flops(N, active) -> float:
+    """FP64 flops of the FP64 judge summed over channels with passive sets
+    `active` (int tensor of bit masks): the whitening N(N+1), per passive
+    column the table row and the residual column (2N each, FMA = 2), and
+    chi2 (2N + 2); the judge loops over the passive set only."""
+    import torch
+
+    bits = active.to(torch.int32)
+    cols = sum(int(((bits >> k) & 1).sum().item()) for k in range(16))
+    n = int(active.numel())
+    return float(n * (N * (N + 1) + 2 * N + 2) + 4 * N * cols)
+
+
 def judge_df_flops(P, active) -> float:
     """FP32 flops of the double-float judge summed over channels of a set
     with pulse matrix P (N x K), given their passive sets `active` (int
@@ -640,10 +653,9 @@ def kernel_rooflines(mf, eng, kernels, args, n, ctype, plain_flops, form_fp64_fl
     work per launch over its mean launch time (CUDA events from mf_profile).
 
     fit_fp64_kernel: the plain fit's executed FP64 flops (instrumented count).
-    judge_kernel: N(N+1) + 4NK FP64 flops per channel of its set (whitening,
-      dense passive-set solve, residual; FMA = 2); the double-float judge's
-      FP32 flops from each channel's passive set (judge_df_flops, with the
-      form's active masks `active`).
+    judge_kernel: the FP64 judge's FP64 flops (judge_fp64_flops) and the
+      double-float judge's FP32 flops (judge_df_flops), both summed over each
+      channel's passive set (the form's active masks `active`).
     repair_kernel: the rest of the form's counted FP64 flops.
     mlp_infer_tc_kernel: MLP_FLOPS_PER_CHANNEL on the tensor cores (BF16, tcgen05).
     search_kernel: FP32 and latency-bound; its HBM bytes (samples, pederr,
@@ -663,8 +675,8 @@ def kernel_rooflines(mf, eng, kernels, args, n, ctype, plain_flops, form_fp64_fl
         if c is None:
             continue
         N, K = c.nsamples, c.npulses
-        judge += m * (N * (N + 1) + 4 * N * K)
         sel = active if ctype is None else active[ctype == t]
+        judge += judge_fp64_flops(N, sel)
         judge_df += judge_df_flops(mf.conditions_arrays(c)[0], sel)
     df_form = args.form in ("fp32", "warm", "fp32-cov")
     warm = args.form == "warm"

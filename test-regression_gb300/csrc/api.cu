@@ -90,6 +90,7 @@ struct mf_context {
   float* d_pinv32[MF_MAX_CTYPES] = {nullptr, nullptr};
   float* d_pinv32lo[MF_MAX_CTYPES] = {nullptr, nullptr};
   float* d_pinv2[MF_MAX_CTYPES] = {nullptr, nullptr};
+  double* d_g64[MF_MAX_CTYPES] = {nullptr, nullptr};
   MlpState mlp;
   int sms = 152;
   // mixed-form hand-off workspace (MIXED_CHUNK channels), allocated with the tables
@@ -492,6 +493,8 @@ void free_tables(mf_context* c, int t) {
   cudaFree(c->d_pinv32[t]);
   cudaFree(c->d_pinv32lo[t]);
   cudaFree(c->d_pinv2[t]);
+  cudaFree(c->d_g64[t]);
+  c->d_g64[t] = nullptr;
   c->d_pinv32lo[t] = nullptr;
   c->d_pinv2[t] = nullptr;
   c->d_offset[t] = nullptr;
@@ -526,6 +529,9 @@ int upload_tables(mf_context* c, int t) {
     e = cudaMemcpy(c->d_pinv32lo[t], h.pinv32lo.data(), sizeof(float) * np, cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
     e = cudaMemcpy(c->d_pinv2[t], h.pinv2.data(), sizeof(float) * h.pinv2.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_g64[t], sizeof(double) * size_t(d.N) * d.K);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(c->d_g64[t], h.G64, sizeof(double) * size_t(d.N) * d.K, cudaMemcpyHostToDevice);
   if (e == cudaSuccess && !c->ws_mask) {
     e = cudaMalloc(&c->ws_mask, sizeof(uint16_t) * MIXED_CHUNK);
     if (e == cudaSuccess) e = cudaMalloc(&c->ws_count, sizeof(uint16_t) * MIXED_CHUNK);
@@ -573,6 +579,7 @@ void fill_dev_mixed(const mf_context* c, int t, DevMixed* m) {
   m->pinv32lo = c->d_pinv32lo[t];
   m->pinv2 = c->d_pinv2[t];
   m->g2 = c->d_pinv2[t] + h.g2_off;
+  m->g64 = c->d_g64[t];
 }
 
 int grow_staging(mf_context* c, int64_t n, int ss, int as) {

@@ -133,6 +133,8 @@ struct DevMixed {
   const float* pinv32lo;
   const float* pinv2;  // (hi, lo) pairs; a row of an even N starts on 16 bytes
   const float* g2;     // G as (hi, lo) pairs, column k at [2 k N] (inside the pinv2 buffer)
+  const double* g64;   // G in FP64, column k at [k N], in global memory: the FP64 judge reads a
+                       // different column in every lane, which the constant bank would serialise
 };
 
 struct MixedArgs {

@@ -402,43 +402,6 @@ __device__ __forceinline__ void residual_gradient(const DevMixed& T, const doubl
   }
 }
 
-// The judge's common path: the FP64 residual r = y - G x (kept for chi2) and
-// an FP32 screen of the KKT test on it. The FP32 gradient w_k = G_k^T r of a
-// column outside m is accurate to (N + 2) 2^-24 sum_i |G_ik r_i| < 2^-19 sum
-// (N <= 10 rounded FMAs, plus the rounding of G and r to FP32); a column passes
-// only if w_k plus that bound stays below tol, so every column the FP64 test
-// w_k >= tol could flag is sent to the FP64 repair, and only columns within
-// that bound of tol are sent there needlessly. Returns true when no column
-// needs the FP64 test; add collects the columns that provably violate it.
-template <int N, int K>
-__device__ __forceinline__ bool residual64_screen32(const DevMixed& T, const double* y, const double* x, unsigned m,
-                                                    double* r, float tol, unsigned& add) {
-#pragma unroll
-  for (int i = 0; i < N; ++i) r[i] = y[i];
-#pragma unroll
-  for (int k = 0; k < K; ++k)
-#pragma unroll
-    for (int i = 0; i < N; ++i)
-      if (i >= T.gfz[k]) r[i] = fma(-T.G64[k * N + i], x[k], r[i]);
-  float rf[N];
-#pragma unroll
-  for (int i = 0; i < N; ++i) rf[i] = float(r[i]);
-  bool ok = true;
-#pragma unroll
-  for (int k = 0; k < K; ++k) {
-    float w = 0.f, mag = 0.f;
-#pragma unroll
-    for (int i = 0; i < N; ++i)
-      if (i >= T.gfz[k]) {
-        w = fmaf(T.G32[k * N + i], rf[i], w);
-        mag = fmaf(fabsf(T.G32[k * N + i]), fabsf(rf[i]), mag);
-      }
-    if (!(m & (1u << k)) && !(fmaf(0x1p-19f, mag, w) < tol)) ok = false;
-    if (!(m & (1u << k)) && fmaf(-0x1p-19f, mag, w) > tol) add |= 1u << k;  // provably violating
-  }
-  return ok;
-}
-
 // y = L_R^-1 s in FP64 (packed rows, no division); returns true for a
 // non-finite or non-positive input.
 template <int N>
@@ -631,10 +594,47 @@ __device__ __forceinline__ void fix_body(const MixedArgs& a, const DevMixed& T, 
   for (int k = 0; k < K; ++k) wx[k] = x32[k];
 }
 
+// The FP32 screen of the KKT test on the FP64 residual r: the FP32 gradient
+// w_k = G_k^T r of a column outside m is accurate to (N + 2) 2^-24 sum_i
+// |G_ik r_i| < 2^-19 sum (N <= 10 rounded FMAs, plus the rounding of G and r
+// to FP32); a column passes only if w_k plus that bound stays below tol, so
+// every column the FP64 test w_k >= tol could flag is sent to the FP64
+// repair, and only columns within that bound of tol are sent there
+// needlessly. Returns true when no column needs the FP64 test; add collects
+// the columns that provably violate it.
+template <int N, int K>
+__device__ __forceinline__ bool kkt_screen32(const DevMixed& T, const double* r, unsigned m, float tol,
+                                             unsigned& add) {
+  float rf[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) rf[i] = float(r[i]);
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    float w = 0.f, mag = 0.f;
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      if (i >= T.gfz[k]) {
+        w = fmaf(T.G32[k * N + i], rf[i], w);
+        mag = fmaf(fabsf(T.G32[k * N + i]), fabsf(rf[i]), mag);
+      }
+    if (!(m & (1u << k)) && !(fmaf(0x1p-19f, mag, w) < tol)) ok = false;
+    if (!(m & (1u << k)) && fmaf(-0x1p-19f, mag, w) > tol) add |= 1u << k;  // provably violating
+  }
+  return ok;
+}
+
 // The FP64 judge of channel ch (one lane): writes the outputs; or, when
 // columns provably violate the KKT condition and the amplitudes are positive
 // and fix_count is given, queues the channel for the FP32 fix (ws_fixq,
 // entry ch | add << 21); otherwise queues it for the FP64 repair (ws_queue).
+// The FP64 solve on the search's passive set and the residual run column by
+// column over the set only (each lane its own trip count; a warp runs as many
+// iterations as its largest set): x_k = G_S^+_k y from the FP64 table, then
+// r -= G_k x_k at once, with G_k read from global memory (a different column
+// in every lane). The columns outside the set, once run through a zero row,
+// were exact no-ops. The amplitudes are written as they come; a channel the
+// judge queues gets them rewritten by the fix or the repair.
 template <int N, int K>
 __device__ __forceinline__ void judge_body(const MixedArgs& a, const DevMixed& T, int64_t ch, unsigned* qcount,
                                            unsigned* fix_count) {
@@ -642,26 +642,75 @@ __device__ __forceinline__ void judge_body(const MixedArgs& a, const DevMixed& T
   const unsigned cnt = a.ws_count[ch];
   double y[N], sig;
   const bool bad = whiten64<N>(a, T, ch, y, sig);
-  // common path, straight-line: the FP64 solve on the FP32 passive set, the
-  // residual and gradient, the KKT test max w < eps * pederr^2
-  double x[K], r[N];
-  solve64_dense<N, K>(T, m, y, x);
-  bool ok = true;
+  double r[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) r[i] = y[i];
+  bool ok = true, finite = true;
+  uint16_t support = 0;
+  double xin = 0.;
+  double* out = a.amplitudes + ch * a.amp_stride;
 #pragma unroll
   for (int k = 0; k < K; ++k)
-    if ((m & (1u << k)) && !pos64(x[k])) ok = false;
+    if (!((m >> k) & 1u)) out[k] = 0.;
+  const int p = __popc(m);
+  {
+    const double* P = T.pinv64 + __ldg(T.offset + m);
+    unsigned rest = m;
+#pragma unroll 1
+    for (int rr = 0; rr < p; ++rr) {
+      const int k = __ffs(rest) - 1;
+      rest &= rest - 1u;
+      const double2* row = reinterpret_cast<const double2*>(P + rr * N);
+      double xk = 0.;
+#pragma unroll
+      for (int q = 0; q < N / 2; ++q) {
+        const double2 v = __ldg(row + q);
+        xk = fma(v.x, y[2 * q], xk);
+        xk = fma(v.y, y[2 * q + 1], xk);
+      }
+      if (!pos64(xk)) ok = false;
+      const double2* g = reinterpret_cast<const double2*>(T.g64 + k * N);
+#pragma unroll
+      for (int q = 0; q < N / 2; ++q) {
+        const double2 v = __ldg(g + q);
+        r[2 * q] = fma(-v.x, xk, r[2 * q]);
+        r[2 * q + 1] = fma(-v.y, xk, r[2 * q + 1]);
+      }
+      out[k] = xk;
+      finite = finite && finite64(xk);
+      if (pos64(xk)) support |= uint16_t(1u << k);
+      if (k == T.intime_col) xin = xk;
+    }
+  }
   unsigned add = 0;
   const bool pos_ok = ok;
-  if (ok) ok = residual64_screen32<N, K>(T, y, x, m, r, float(a.eps * sig * sig), add);
+  if (ok) ok = kkt_screen32<N, K>(T, r, m, float(a.eps * sig * sig), add);
   if (!ok) {  // compaction into the fix or the repair queue
     if (fix_count && pos_ok && add) enqueue(fix_count, a.ws_fixq, int(unsigned(ch) | (add << 21)));
     else enqueue(qcount, a.ws_queue, int(ch));
     return;
   }
-  write_outputs<N, K>(a, T, ch, x, r, sig, bad, true, int(cnt & 255u), int(cnt >> 8) + 1,
-                      N * (N + 1) + 4 * N * K);
+  double chi2 = 0.;
+#pragma unroll
+  for (int i = 0; i < N; ++i) chi2 = fma(r[i], r[i], chi2);
+  chi2 = chi2 / (sig * sig);
+  for (int k = K; k < a.amp_stride && k < KMAX; ++k) out[k] = 0.;
+  a.chi2[ch] = chi2;
+  if (a.intime) a.intime[ch] = T.intime_col >= 0 ? xin : 0.;
+  if (a.active_mask) a.active_mask[ch] = support;
+  if (a.status) {
+    uint8_t st = 0;
+    if (!(finite && finite64(chi2))) st |= CH_NONFINITE;
+    if (bad) st |= CH_BADINPUT;
+    a.status[ch] = st;
+  }
+  if (a.iters) {
+    const int adds = int(cnt & 255u), solves = int(cnt >> 8) + 1;
+    a.iters[ch] = 1 | ((adds < 4095 ? adds : 4095) << 8) | ((solves < 4095 ? solves : 4095) << 20);
+  }
+  // executed FP64 flops: whitening, the passive solve and residual (2N each per column), chi2
+  if (a.flops) a.flops[ch] = double(N * (N + 1) + 4 * N * p + 2 * N + 2);
 }
-
 
 // ---------------------------------------------------------------------------
 // The judge in double-float FP32 arithmetic (MF_PREC_FP32)

@@ -152,8 +152,9 @@ def test_mixed_fp64_flop_counter(mf, cuda):
     b = db.outputs_host()
     assert np.array_equal(a["amplitudes"], b["amplitudes"])
     f = flops.cpu().numpy()
-    # whitening 110 + one FP64 solve + residual + chi2 at least
-    assert (f >= 110 + 20 + 22).all() and f.mean() < 2000
+    # whitening 110 + chi2 22 at least (the judge's solve and residual run over
+    # the passive set only: 40 per column)
+    assert (f >= 110 + 22).all() and f.mean() < 2000 and (f > 132).mean() > 0.9
     eng.close()
 
 
