@@ -10,6 +10,16 @@
 // --fmad=false: every accumulation is an explicit fused multiply-add with the
 // index ascending, each triangular solve divides once by the diagonal, so the
 // kernel reproduces the CPU oracle bit for bit).
+//
+// Per-thread storage. A thread's working set lives in local memory, cached
+// by L1 and L2; with ~400 resident threads per SM a 5 KB set overflowed both
+// and every access went to DRAM. So it is kept small: triangular factors and
+// the symmetric normal matrix are stored packed (row i of the lower triangle
+// at tri(i) = i(i+1)/2, 55 values for K = 10 instead of 100), the covariance
+// is factored in place, the pulse matrix is read from the condition set (the
+// kernel's parameters) instead of a per-thread copy, and the FNNLS factor
+// reuses the whitened matrix's buffer once the normal equations are formed.
+// Only where values are stored changes; every operation and its order stay.
 #pragma once
 #include <cfloat>
 
@@ -29,6 +39,17 @@ __device__ __forceinline__ double fmaT(double a, double b, double c) { return fm
 __device__ __forceinline__ double sqrtT(double a) { return sqrt(a); }
 __device__ __forceinline__ double fabsT(double a) { return fabs(a); }
 
+constexpr int KTRI = KMAX * (KMAX + 1) / 2;
+
+// start of row i of a packed lower triangle
+__device__ __forceinline__ int tri(int i) { return i * (i + 1) / 2; }
+
+// element (i, j) of a symmetric matrix stored as its packed lower triangle
+template <typename T>
+__device__ __forceinline__ T& sym(T* M, int i, int j) {
+  return i >= j ? M[tri(i) + j] : M[tri(j) + i];
+}
+
 struct Flop {
   double v;
   __device__ __forceinline__ void fma(double k) { v += 2 * k; }
@@ -46,93 +67,97 @@ struct Counter {
   }
 };
 
-// linalgebra/interface/cholesky.hpp:8-38 (rows [r0, r1) of a row-major factor)
+// linalgebra/interface/cholesky.hpp:8-38, in place: L holds the packed lower
+// triangle of the matrix on entry and its factor on return (element (i, j) is
+// read once, just before the factor's (i, j) is written over it).
 // R: also keep the reciprocals of the diagonal in rinv and multiply by them
 // instead of dividing (one division per row: the per-channel form's FP64
 // continuation, which needs no bit parity with the oracle)
 template <bool C, typename T, bool R = false>
-__device__ __forceinline__ void chol_rows(const T* M, T* L, int ld, int r0, int r1, Counter<C>& f, T* rinv = nullptr) {
-  for (int i = r0; i < r1; ++i) {
+__device__ __forceinline__ void chol_rows(T* L, int n, Counter<C>& f, T* rinv = nullptr) {
+  for (int i = 0; i < n; ++i) {
     T sumsq = 0;
     for (int j = 0; j < i; ++j) {
       T s2 = 0;
-      for (int k = 0; k < j; ++k) s2 = fmaT(L[i * ld + k], L[j * ld + k], s2);
-      const T v = R ? (M[i * ld + j] - s2) * rinv[j] : (M[i * ld + j] - s2) / L[j * ld + j];
-      L[i * ld + j] = v;
+      for (int k = 0; k < j; ++k) s2 = fmaT(L[tri(i) + k], L[tri(j) + k], s2);
+      const T v = R ? (L[tri(i) + j] - s2) * rinv[j] : (L[tri(i) + j] - s2) / L[tri(j) + j];
+      L[tri(i) + j] = v;
       sumsq = fmaT(v, v, sumsq);
       f.fma(j + 1);
       f.op(2);
     }
-    L[i * ld + i] = sqrtT(M[i * ld + i] - sumsq);
-    if (R) rinv[i] = T(1) / L[i * ld + i];
+    L[tri(i) + i] = sqrtT(L[tri(i) + i] - sumsq);
+    if (R) rinv[i] = T(1) / L[tri(i) + i];
     f.op(2);
   }
 }
 
-// linalgebra/interface/substitution.hpp:10-26
-template <bool C, typename T, bool R = false>
-__device__ __forceinline__ void fwd(const T* L, int ld, const T* b, T* y, int n, Counter<C>& f,
-                                    const T* rinv = nullptr) {
+// linalgebra/interface/substitution.hpp:10-26 (L packed; b(i) gives the
+// right-hand side's element i)
+template <bool C, typename T, bool R = false, typename Rhs>
+__device__ __forceinline__ void fwd(const T* L, Rhs&& b, T* y, int n, Counter<C>& f, const T* rinv = nullptr) {
   for (int i = 0; i < n; ++i) {
-    T t = b[i];
-    for (int j = 0; j < i; ++j) t = fmaT(-L[i * ld + j], y[j], t);
-    y[i] = R ? t * rinv[i] : t / L[i * ld + i];
+    T t = b(i);
+    for (int j = 0; j < i; ++j) t = fmaT(-L[tri(i) + j], y[j], t);
+    y[i] = R ? t * rinv[i] : t / L[tri(i) + i];
     f.fma(i);
     f.op(1);
   }
 }
 
-// linalgebra/interface/substitution.hpp:34-50 (L^T x = y)
+// linalgebra/interface/substitution.hpp:34-50 (L^T x = y, L packed)
 template <bool C, typename T>
-__device__ __forceinline__ void bwd(const T* L, int ld, const T* y, T* x, int n, Counter<C>& f) {
+__device__ __forceinline__ void bwd(const T* L, const T* y, T* x, int n, Counter<C>& f) {
   for (int i = n - 1; i >= 0; --i) {
     T t = y[i];
-    for (int j = i + 1; j < n; ++j) t = fmaT(-L[j * ld + i], x[j], t);
-    x[i] = t / L[i * ld + i];
+    for (int j = i + 1; j < n; ++j) t = fmaT(-L[tri(j) + i], x[j], t);
+    x[i] = t / L[tri(i) + i];
     f.fma(n - 1 - i);
     f.op(1);
   }
 }
 
-// linalgebra/interface/fused_cholesky_substitution.hpp:18-59
+// linalgebra/interface/fused_cholesky_substitution.hpp:18-59 (M symmetric,
+// M and L packed lower triangles)
 template <bool C, typename T>
-__device__ __forceinline__ void rc_add(const T* M, T* L, int ld, const T* b, T* y, int view, Counter<C>& f) {
+__device__ __forceinline__ void rc_add(const T* M, T* L, const T* b, T* y, int view, Counter<C>& f) {
   const int row = view - 1;
   T sum = 0, total = b[row];
   for (int col = 0; col < row; ++col) {
     T s2 = 0;
-    for (int j = 0; j < col; ++j) s2 = fmaT(L[row * ld + j], L[col * ld + j], s2);
-    const T v = (M[row * ld + col] - s2) / L[col * ld + col];
+    for (int j = 0; j < col; ++j) s2 = fmaT(L[tri(row) + j], L[tri(col) + j], s2);
+    const T v = (M[tri(row) + col] - s2) / L[tri(col) + col];
     total = fmaT(-v, y[col], total);
     sum = fmaT(v, v, sum);
-    L[row * ld + col] = v;
+    L[tri(row) + col] = v;
     f.fma(col + 3);
     f.op(2);
   }
-  const T d = sqrtT(M[row * ld + row] - sum);
-  L[row * ld + row] = d;
+  const T d = sqrtT(M[tri(row) + row] - sum);
+  L[tri(row) + row] = d;
   y[row] = total / d;
   f.op(3);
 }
 
-// linalgebra/interface/fused_cholesky_substitution.hpp:64-102
+// linalgebra/interface/fused_cholesky_substitution.hpp:64-102 (M symmetric,
+// M and L packed lower triangles)
 template <bool C, typename T>
-__device__ __forceinline__ void inbetween_removal(const T* M, T* L, int ld, const T* b, T* y, int pos, int view,
+__device__ __forceinline__ void inbetween_removal(const T* M, T* L, const T* b, T* y, int pos, int view,
                                                   Counter<C>& f) {
   for (int i = pos; i < view; ++i) {
     T sumsq = 0, total = b[i];
     for (int j = 0; j < i; ++j) {
       T s2 = 0;
-      for (int k = 0; k < j; ++k) s2 = fmaT(L[i * ld + k], L[j * ld + k], s2);
-      const T v = (M[i * ld + j] - s2) / L[j * ld + j];
-      L[i * ld + j] = v;
+      for (int k = 0; k < j; ++k) s2 = fmaT(L[tri(i) + k], L[tri(j) + k], s2);
+      const T v = (M[tri(i) + j] - s2) / L[tri(j) + j];
+      L[tri(i) + j] = v;
       total = fmaT(-v, y[j], total);
       sumsq = fmaT(v, v, sumsq);
       f.fma(j + 2);
       f.op(2);
     }
-    const T d = sqrtT(M[i * ld + i] - sumsq);
-    L[i * ld + i] = d;
+    const T d = sqrtT(M[tri(i) + i] - sumsq);
+    L[tri(i) + i] = d;
     y[i] = total / d;
     f.op(3);
   }
@@ -145,11 +170,15 @@ __device__ __forceinline__ void swap_d(T& a, T& b) {
   b = t;
 }
 
+// symmetric permutation of indices a and b of an n x n symmetric matrix
+// stored as its packed lower triangle: (a, a) <-> (b, b) and (a, k) <-> (b, k)
+// for every other k; (a, b) stays
 template <typename T>
-__device__ __forceinline__ void swap_sym(T* M, int ld, int n, int a, int b) {
+__device__ __forceinline__ void swap_sym(T* M, int n, int a, int b) {
   if (a == b) return;
-  for (int k = 0; k < n; ++k) swap_d(M[k * ld + a], M[k * ld + b]);
-  for (int k = 0; k < n; ++k) swap_d(M[a * ld + k], M[b * ld + k]);
+  swap_d(M[tri(a) + a], M[tri(b) + b]);
+  for (int k = 0; k < n; ++k)
+    if (k != a && k != b) swap_d(sym(M, a, k), sym(M, b, k));
 }
 
 struct FnnlsOut {
@@ -158,23 +187,23 @@ struct FnnlsOut {
 };
 
 // FNNLS, nnls/src/inplace_fnnls.cu:72-233 with the incremental factor.
-// A: N x K column-major, b: N, x: K warm start in / solution out.
+// A: N x K column-major (at least KTRI values: once the normal equations are
+// formed the buffer holds the packed factor of the passive block), b: N,
+// x: K warm start in / solution out.
 // start 0: the reference's start (empty passive set, warm x);
 // start 1: passive set seeded with the support of the warm x (ascending).
 template <int NT, int KT, bool C, typename T>
-__device__ void fnnls(const T* A, const T* b, T* x, int N, int K, T eps, int max_iter, int start, FnnlsOut& o,
+__device__ void fnnls(T* A, const T* b, T* x, int N, int K, T eps, int max_iter, int start, FnnlsOut& o,
                       Counter<C>& f) {
   if (NT > 0) N = NT;
   if (KT > 0) K = KT;
-  T AtA[KMAX * KMAX], Atb[KMAX], s[KMAX], L[KMAX * KMAX], y[KMAX];
+  T AtA[KTRI], Atb[KMAX], s[KMAX], y[KMAX];
   int8_t perm[KMAX];
-  const int ld = KMAX;
   for (int i = 0; i < K; ++i) {
     for (int j = i; j < K; ++j) {
       T acc = 0;
       for (int k = 0; k < N; ++k) acc = fmaT(A[i * N + k], A[j * N + k], acc);
-      AtA[j * ld + i] = acc;
-      AtA[i * ld + j] = acc;
+      AtA[tri(j) + i] = acc;
       f.fma(N);
     }
   }
@@ -184,12 +213,13 @@ __device__ void fnnls(const T* A, const T* b, T* x, int N, int K, T eps, int max
     Atb[i] = acc;
     f.fma(N);
   }
+  T* const L = A;  // A is not read again
   for (int i = 0; i < K; ++i) perm[i] = int8_t(i);
 
   int nP = 0, outer = 0, inner = 0, converged = 0;
 
   auto swap_in = [&](int p, int q) {
-    swap_sym(AtA, ld, K, p, q);
+    swap_sym(AtA, K, p, q);
     swap_d(Atb[p], Atb[q]);
     swap_d(x[p], x[q]);
     const int8_t t = perm[p];
@@ -216,13 +246,13 @@ __device__ void fnnls(const T* A, const T* b, T* x, int N, int K, T eps, int max
             y[0] = Atb[0] / l00;
             f.op(2);
           } else {
-            rc_add(AtA, L, ld, Atb, y, r, f);
+            rc_add(AtA, L, Atb, y, r, f);
           }
         }
       } else {
-        inbetween_removal(AtA, L, ld, Atb, y, position_removed, nP, f);
+        inbetween_removal(AtA, L, Atb, y, position_removed, nP, f);
       }
-      bwd(L, ld, y, s, nP, f);
+      bwd(L, y, s, nP, f);
 
       T smin = s[0];
       for (int i = 1; i < nP; ++i) smin = (s[i] < smin) ? s[i] : smin;
@@ -261,7 +291,7 @@ __device__ void fnnls(const T* A, const T* b, T* x, int N, int K, T eps, int max
     // columns with x_k > 0 and a non-zero whitened norm (the MINOS refits
     // zero the in-time column and hold its amplitude fixed)
     for (int k = 0; k < K; ++k)
-      if (x[k] > T(0) && AtA[k * ld + k] > T(0)) swap_in(nP++, k);
+      if (x[k] > T(0) && AtA[tri(k) + k] > T(0)) swap_in(nP++, k);
     if (nP > 0) inner_loop(nP);
   }
 
@@ -274,7 +304,7 @@ __device__ void fnnls(const T* A, const T* b, T* x, int N, int K, T eps, int max
     T wmax = 0;
     for (int i = nP; i < K; ++i) {
       T acc = 0;
-      for (int j = 0; j < K; ++j) acc = fmaT(AtA[i * ld + j], x[j], acc);
+      for (int j = 0; j < K; ++j) acc = fmaT(sym(AtA, i, j), x[j], acc);
       const T w = Atb[i] - acc;
       f.fma(K);
       f.op(1);
@@ -292,7 +322,7 @@ __device__ void fnnls(const T* A, const T* b, T* x, int N, int K, T eps, int max
     ++nP;
     inner_loop(1);
   }
-  T xo[KMAX];
+  T* const xo = s;  // s is not read again
   for (int i = 0; i < K; ++i) xo[perm[i]] = x[i];
   uint16_t mask = 0;
   for (int i = 0; i < nP; ++i) mask |= uint16_t(1u << perm[i]);
@@ -308,9 +338,9 @@ template <typename T>
 struct FitState {
   T samp[KMAX];
   T amp[KMAX];
-  T P[KMAX * KMAX];  // column-major N x K
-  T LC[KMAX * KMAX]; // row-major lower factor of the covariance, ld = KMAX
+  T LC[KTRI];        // lower factor of the covariance, packed rows
   T LCr[KMAX];       // reciprocals of LC's diagonal (kept by the reciprocal variant only)
+  int zcol;          // pulse-matrix column held at zero (the error refits' in-time column), or -1
   T chisq;
   FnnlsOut st;
   int outer_iters;
@@ -319,14 +349,22 @@ struct FitState {
   int first_done;  // ... and whether the stopping rule already held after it
 };
 
+// element (i, k) of the pulse matrix the fit uses: the condition set's, with
+// column S.zcol at zero
+template <typename T>
+__device__ __forceinline__ T pulse(const DevConditions& c, const FitState<T>& S, int N, int k, int i) {
+  return k == S.zcol ? T(0) : T(c.P[k * N + i]);
+}
+
 // updateCov, multifit_cpu/src/PulseChiSqSNNLS.cpp:169-194
+// (the covariance is formed in S.LC and factored there)
 template <int NT, int KT, bool C, typename T, bool R = false>
 __device__ void update_cov(const DevConditions& c, int N, int K, T pederr, FitState<T>& S, Counter<C>& f) {
-  T M[KMAX * KMAX];
+  T* const M = S.LC;
   const T ped2 = pederr * pederr;
   f.op(1);
   for (int i = 0; i < N; ++i)
-    for (int j = 0; j <= i; ++j) M[i * KMAX + j] = ped2 * T(c.R[j * N + i]);
+    for (int j = 0; j <= i; ++j) M[tri(i) + j] = ped2 * T(c.R[j * N + i]);
   f.op(N * (N + 1) / 2);
   if (c.has_fpc) {
     const int NF = N + 9;
@@ -340,31 +378,31 @@ __device__ void update_cov(const DevConditions& c, int N, int K, T pederr, FitSt
       for (int a = 0; a < ns; ++a)
         for (int cc = 0; cc <= a; ++cc) {
           const int i = first + a, j = first + cc;
-          M[i * KMAX + j] = fmaT(ampsq, T(c.fpc[(j + offset) * NF + (i + offset)]), M[i * KMAX + j]);
+          M[tri(i) + j] = fmaT(ampsq, T(c.fpc[(j + offset) * NF + (i + offset)]), M[tri(i) + j]);
         }
       f.op(1);
       f.fma(ns * (ns + 1) / 2);
     }
   }
-  chol_rows<C, T, R>(M, S.LC, KMAX, 0, N, f, S.LCr);
+  chol_rows<C, T, R>(S.LC, N, f, S.LCr);
 }
 
 // ComputeChiSq, multifit_cpu/src/PulseChiSqSNNLS.cpp:196-200
 template <bool C, typename T, bool R = false>
-__device__ T compute_chisq(int N, int K, const FitState<T>& S, Counter<C>& f) {
+__device__ T compute_chisq(const DevConditions& c, int N, int K, const FitState<T>& S, Counter<C>& f) {
   T r[KMAX], z[KMAX];
   for (int i = 0; i < N; ++i) {
     T acc = 0;
-    for (int k = 0; k < K; ++k) acc = fmaT(S.P[k * N + i], S.amp[k], acc);
+    for (int k = 0; k < K; ++k) acc = fmaT(pulse(c, S, N, k, i), S.amp[k], acc);
     r[i] = acc - S.samp[i];
   }
   f.fma(N * K);
   f.op(N);
-  fwd<C, T, R>(S.LC, KMAX, r, z, N, f, S.LCr);
-  T c = 0;
-  for (int i = 0; i < N; ++i) c = fmaT(z[i], z[i], c);
+  fwd<C, T, R>(S.LC, [&](int i) { return r[i]; }, z, N, f, S.LCr);
+  T chi2 = 0;
+  for (int i = 0; i < N; ++i) chi2 = fmaT(z[i], z[i], chi2);
   f.fma(N);
-  return c;
+  return chi2;
 }
 
 // NNLS + Minimize, multifit_cpu/src/PulseChiSqSNNLS.cpp:149-166, 219-273.
@@ -385,11 +423,11 @@ __device__ void minimize(const DevConditions& c, const DevOptions& o, int N, int
     if (!run) continue;
     update_cov<NT, KT, C, T, R>(c, N, K, pederr, S, f);
     T A[KMAX * KMAX], b[KMAX];
-    for (int k = 0; k < K; ++k) fwd<C, T, R>(S.LC, KMAX, S.P + k * N, A + k * N, N, f, S.LCr);
-    fwd<C, T, R>(S.LC, KMAX, S.samp, b, N, f, S.LCr);
+    for (int k = 0; k < K; ++k) fwd<C, T, R>(S.LC, [&](int i) { return pulse(c, S, N, k, i); }, A + k * N, N, f, S.LCr);
+    fwd<C, T, R>(S.LC, [&](int i) { return S.samp[i]; }, b, N, f, S.LCr);
     fnnls<NT, KT>(A, b, S.amp, N, K, T(o.nnls_eps), o.max_iter_nnls, o.nnls_start, S.st, f);
     __syncwarp(act);
-    const T now = compute_chisq<C, T, R>(N, K, S, f);
+    const T now = compute_chisq<C, T, R>(c, N, K, S, f);
     const T delta = now - S.chisq;
     f.op(1);
     S.chisq = now;
@@ -401,9 +439,9 @@ __device__ void minimize(const DevConditions& c, const DevOptions& o, int N, int
 
 // ComputeApproxUncertainty, multifit_cpu/src/PulseChiSqSNNLS.cpp:202-207
 template <bool C, typename T, bool R = false>
-__device__ T approx_uncertainty(int N, const FitState<T>& S, int k, Counter<C>& f) {
+__device__ T approx_uncertainty(const DevConditions& c, int N, const FitState<T>& S, int k, Counter<C>& f) {
   T z[KMAX];
-  fwd<C, T, R>(S.LC, KMAX, S.P + k * N, z, N, f, S.LCr);
+  fwd<C, T, R>(S.LC, [&](int i) { return pulse(c, S, N, k, i); }, z, N, f, S.LCr);
   T n2 = 0;
   for (int i = 0; i < N; ++i) n2 = fmaT(z[i], z[i], n2);
   f.fma(N);
@@ -411,10 +449,36 @@ __device__ T approx_uncertainty(int N, const FitState<T>& S, int k, Counter<C>& 
   return T(1) / sqrtT(n2);
 }
 
+// Coalesced staging of a warp's channel rows through shared memory: rows
+// [ch0, ch0 + nw) (nw <= 32) of a row-major array with `stride` elements per
+// row, `width` <= KMAX elements of each, to or from `rows` (KMAX per row).
+// Lane `lane` moves elements lane, lane + 32, ... of the warp's nw x width
+// block, so consecutive lanes touch consecutive addresses (a channel's own
+// row, read by its thread, is 80 bytes wide: 32 lanes reading their own rows
+// touch 32 rows per instruction). The store writes only the rows whose bit
+// is set in `sel` (the channels of the launch's condition set).
+__device__ __forceinline__ void stage_rows_in(const double* src, int64_t stride, int64_t ch0, int nw, int width,
+                                              double* rows, int lane) {
+  for (int e = lane; e < nw * width; e += 32) {
+    const int r = e / width, i = e - r * width;
+    rows[r * KMAX + i] = src[(ch0 + r) * stride + i];
+  }
+}
+
+__device__ __forceinline__ void stage_rows_out(const double* rows, double* dst, int64_t stride, int64_t ch0, int nw,
+                                               int width, unsigned sel, int lane) {
+  for (int e = lane; e < nw * width; e += 32) {
+    const int r = e / width, i = e - r * width;
+    if ((sel >> r) & 1u) dst[(ch0 + r) * stride + i] = rows[r * KMAX + i];
+  }
+}
+
 // DoFit, multifit_cpu/src/PulseChiSqSNNLS.cpp:21-147, for channel ch of the
 // batch: the main Minimize, then (with errors on) the two constrained refits
 // of the in-time amplitude, and the outputs. mini(S, pederr, lanes) is the
-// Minimize the caller uses; it runs on the lanes given.
+// Minimize the caller uses; it runs on the lanes given. `in` holds the
+// channel's N samples; the K amplitudes, then zeros up to `out_width`
+// values, are written to `out` (the caller stages both rows).
 //
 // With a.seeded the main Minimize's first outer iteration has been done
 // already (the per-channel form of the mixed and FP32 precisions: with the
@@ -424,19 +488,17 @@ __device__ T approx_uncertainty(int N, const FitState<T>& S, int k, Counter<C>& 
 // rule against that chi2 (against 0 after the first iteration).
 template <int NT, int KT, bool C, bool R = false, typename Mini>
 __device__ void dofit_with(const FitArgs& a, const DevConditions& c, int64_t ch, unsigned lanes, Counter<C>& f,
-                           Mini&& mini) {
+                           const double* in, double* out, int out_width, Mini&& mini) {
   const int N = NT > 0 ? NT : c.N;
   const int K = KT > 0 ? KT : c.K;
   FitState<double> S;
-  const double* in = a.samples + ch * a.sample_stride;
   const double pederr = a.pederr[ch];
   bool bad = !isfinite(pederr);
   for (int i = 0; i < N; ++i) {
     S.samp[i] = in[i];
     bad = bad || !isfinite(S.samp[i]);
   }
-  for (int k = 0; k < K; ++k)
-    for (int i = 0; i < N; ++i) S.P[k * N + i] = c.P[k * N + i];
+  S.zcol = -1;
   for (int k = 0; k < K; ++k) S.amp[k] = 0.;
   S.chisq = 0.;
   S.st = FnnlsOut{0, 0, 0, 0};
@@ -472,19 +534,17 @@ __device__ void dofit_with(const FitArgs& a, const DevConditions& c, int64_t ch,
 
   if (a.opt.compute_errors && c.intime_col >= 0) {
     const int kin = c.intime_col;
-    const double approxerr = approx_uncertainty<C, double, R>(N, S, kin, f);
+    const double approxerr = approx_uncertainty<C, double, R>(c, N, S, kin, f);
     const double chisq0 = S.chisq;
     const double x0 = ampmin[kin];
     double pulse_in[KMAX];
-    for (int i = 0; i < N; ++i) {
-      pulse_in[i] = S.P[kin * N + i];
-      S.P[kin * N + i] = 0.;
-    }
+    for (int i = 0; i < N; ++i) pulse_in[i] = c.P[kin * N + i];
+    S.zcol = kin;
     const double xplus = x0 + approxerr;
     S.amp[kin] = xplus;
     for (int i = 0; i < N; ++i) S.samp[i] = fma(-xplus, pulse_in[i], in[i]);
     mini(S, pederr, lanes);
-    const double chip = compute_chisq<C, double, R>(N, K, S, f);
+    const double chip = compute_chisq<C, double, R>(c, N, K, S, f);
     const double sigmaplus = fabs(xplus - x0) / sqrt(chip - chisq0);
     const bool lower = x0 / sigmaplus > 0.5;
     const unsigned lanes2 = __ballot_sync(lanes, lower);
@@ -493,7 +553,7 @@ __device__ void dofit_with(const FitArgs& a, const DevConditions& c, int64_t ch,
       S.amp[kin] = xminus;
       for (int i = 0; i < N; ++i) S.samp[i] = fma(-xminus, pulse_in[i], in[i]);
       mini(S, pederr, lanes2);
-      const double chim = compute_chisq<C, double, R>(N, K, S, f);
+      const double chim = compute_chisq<C, double, R>(c, N, K, S, f);
       const double sigmaminus = fabs(xminus - x0) / sqrt(chim - chisq0);
       err = 0.5 * (sigmaplus + sigmaminus);
     } else {
@@ -502,13 +562,12 @@ __device__ void dofit_with(const FitArgs& a, const DevConditions& c, int64_t ch,
     S.chisq = chisq0;
   }
 
-  double* out = a.amplitudes + ch * a.amp_stride;
   bool finite = isfinite(S.chisq);
   for (int k = 0; k < K; ++k) {
     out[k] = ampmin[k];
     finite = finite && isfinite(ampmin[k]);
   }
-  for (int k = K; k < a.amp_stride && k < KMAX; ++k) out[k] = 0.;
+  for (int k = K; k < out_width; ++k) out[k] = 0.;
   a.chi2[ch] = S.chisq;
   if (a.intime) a.intime[ch] = c.intime_col >= 0 ? ampmin[c.intime_col] : 0.;
   if (a.errors) a.errors[ch] = err;

@@ -28,19 +28,30 @@ namespace {
 // divisions of the factor, whitening and chi2 -- on this GPU an FP64 division
 // is a sequence of about ten FP64 instructions).
 template <int NT, int KT, bool C, bool R>
-__device__ void dofit(const FitArgs& a, const DevConditions& c, int64_t ch, unsigned lanes) {
+__device__ void dofit(const FitArgs& a, const DevConditions& c, int64_t ch, unsigned lanes, double* row) {
   const int N = NT > 0 ? NT : c.N;
   const int K = KT > 0 ? KT : c.K;
   Counter<C> f;
-  dofit_with<NT, KT, C, R>(a, c, ch, lanes, f, [&](FitState<double>& S, double pederr, unsigned ln) {
+  dofit_with<NT, KT, C, R>(a, c, ch, lanes, f, row, row, KMAX, [&](FitState<double>& S, double pederr, unsigned ln) {
     minimize<NT, KT, C, double, R>(c, a.opt, N, K, pederr, S, f, ln);
   });
 }
 
+constexpr int kFitBlock = 128;  // the largest block of the kernel (its launch bound)
+// Three blocks of 128 per SM: 168 registers a thread, with which the unrolled
+// 10 x 10 fit keeps its working set in registers and its packed arrays in a
+// 2.4 KB local frame (left free, the compiler chose 128 registers and spilled
+// 2.3 KB); 12 warps per SM keep the FP64 pipe ~90 % busy.
+constexpr int kFitBlocksPerSm = 3;
+
 // One launch per condition set (lanes of other sets idle); out-of-range set
-// indices are flagged by the first launch.
+// indices are flagged by the first launch. A warp stages its 32 channels'
+// samples, and afterwards their amplitudes, through one shared-memory row per
+// channel with coalesced loads and stores.
 template <int NT, int KT, bool C, bool R = false>
-__global__ void __launch_bounds__(128) fit_fp64_kernel(const FitArgs a, int set, int flag_bad) {
+__global__ void __launch_bounds__(kFitBlock, kFitBlocksPerSm) fit_fp64_kernel(const FitArgs a, int set, int flag_bad) {
+  __shared__ double stage[kFitBlock * KMAX];
+  const int lane = int(threadIdx.x & 31u);
   const int64_t ch = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   bool mine = false;
   if (ch < a.n) {
@@ -55,7 +66,18 @@ __global__ void __launch_bounds__(128) fit_fp64_kernel(const FitArgs a, int set,
     }
   }
   const unsigned lanes = __ballot_sync(0xffffffffu, mine);  // taken while the warp is converged
-  if (mine) dofit<NT, KT, C, R>(a, a.cond[set], ch, lanes);
+  if (lanes == 0u) return;
+  const DevConditions& c = a.cond[set];
+  const int N = NT > 0 ? NT : c.N;
+  const int64_t ch0 = ch - lane;
+  const int nw = a.n - ch0 < 32 ? int(a.n - ch0) : 32;  // the warp's channels inside the batch
+  double* const rows = stage + (threadIdx.x - lane) * KMAX;
+  stage_rows_in(a.samples, a.sample_stride, ch0, nw, N, rows, lane);
+  __syncwarp();
+  if (mine) dofit<NT, KT, C, R>(a, c, ch, lanes, rows + lane * KMAX);
+  __syncwarp();
+  // K amplitudes, then zeros up to the row's end or KMAX (amp_stride >= K)
+  stage_rows_out(rows, a.amplitudes, a.amp_stride, ch0, nw, a.amp_stride < KMAX ? a.amp_stride : KMAX, lanes, lane);
 }
 
 }  // namespace
@@ -82,7 +104,8 @@ cudaError_t launch_sets(const FitArgs& a, int block, cudaStream_t s, LaunchTimer
 
 cudaError_t launch_fit_fp64(const FitArgs& a, int block, cudaStream_t s, bool instrumented, LaunchTimer* tm) {
   if (a.n == 0) return cudaSuccess;
-  if (block <= 0) block = 128;
+  if (block <= 0) block = kFitBlock;
+  if (block > kFitBlock || block % 32) return cudaErrorInvalidConfiguration;
   return instrumented ? launch_sets<true>(a, block, s, tm) : launch_sets<false>(a, block, s, tm);
 }
 

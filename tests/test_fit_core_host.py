@@ -1,0 +1,166 @@
+"""The FP64 drop-in's device routines (csrc/fit_core.cuh) compiled for the host
+(tests/cpp/fit_core_host.cpp) and run on the CPU: bit for bit against the
+golden fixtures, the reference's own DoFit outputs and the oracle (executed
+flop counts included), for the specialised 10x10 / 8x8 and the generic-shape
+instantiations; the kernel's coalesced staging of samples and amplitudes with
+padded strides and with channels of another condition set in the warp; and
+the per-channel form's seeded continuation, which from the oracle's first
+outer iteration must finish the oracle's fit bit for bit.
+
+Tolerance: zero (same operations in the same order; IEEE fma, division and
+sqrt on both sides)."""
+import ctypes as C
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from _helpers import pack_iters
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+CUDA_INCLUDE = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+MODES = {"ref": (0, 10, 0), "kkt": (1, 1000, 0), "err": (1, 1000, 1)}
+F_COUNT, F_RECIP, F_GENERIC, F_SEEDED = 1, 2, 4, 8
+
+
+@pytest.fixture(scope="module")
+def lib(tmp_path_factory):
+    if not shutil.which("g++") or not os.path.exists(os.path.join(CUDA_INCLUDE, "cuda_runtime.h")):
+        pytest.skip("needs g++ and the CUDA headers")
+    out = str(tmp_path_factory.mktemp("fitcore") / "libfit_core_host.so")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-w", "-I", CUDA_INCLUDE,
+                    "-I", os.path.join(ROOT, "include"), "-I", os.path.join(ROOT, "test-regression_gb300", "csrc"),
+                    os.path.join(ROOT, "tests", "cpp", "fit_core_host.cpp"), "-o", out], check=True)
+    L = C.CDLL(out)
+    L.fit_core_host.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int64] + [C.c_int] * 5 + \
+        [C.c_void_p, C.c_int] + [C.c_void_p] * 7
+    return L
+
+
+def fit(lib, cond, samples, pederr, start, max_iter, errors, flags=0, skip_every=0, sample_stride=None,
+        amp_stride=None, seed=None, fill=0.0):
+    n = samples.shape[0]
+    N, K = cond.nsamples, cond.npulses
+    ss = sample_stride or N
+    ast = amp_stride or K
+    s = np.full((n, ss), 7.0)
+    s[:, :N] = samples[:, :N]
+    pe = np.ascontiguousarray(pederr, dtype=np.float64)
+    o = {"amplitudes": np.full((n, ast), fill), "chi2": np.zeros(n), "intime": np.zeros(n), "errors": np.zeros(n),
+         "active_mask": np.zeros(n, np.uint16), "status": np.zeros(n, np.uint8), "iters": np.zeros(n, np.int32),
+         "flops": np.zeros(n)}
+    if seed is not None:
+        o["amplitudes"][:, :K] = seed["amplitudes"]
+        o["chi2"][:] = seed["chi2"]
+        o["status"][:] = seed["status"]
+    rc = lib.fit_core_host(C.byref(cond), s.ctypes.data, ss, pe.ctypes.data, n, start, max_iter, errors, flags,
+                           skip_every, o["amplitudes"].ctypes.data, ast,
+                           *[o[k].ctypes.data for k in ("chi2", "intime", "errors", "active_mask", "status", "iters",
+                                                        "flops")])
+    assert rc == 0
+    return o
+
+
+@pytest.mark.parametrize("generic", [False, True])
+@pytest.mark.parametrize("mode", list(MODES))
+@pytest.mark.parametrize("name", ["ecal_c0", "ecal_logamp", "hcal", "ecal_fpc", "edge"])
+def test_fixture_bit_for_bit(mf, lib, name, mode, generic):
+    d = dict(np.load(os.path.join(GOLDEN, f"fits_{name}.npz")))
+    cond = mf.make_conditions(d["P"], d["R"], d["bxs"], fullpulsecov=d.get("fullpulsecov"))
+    start, max_iter, errors = MODES[mode]
+    o = fit(lib, cond, d["samples"], d["pederr"], start, max_iter, errors, F_GENERIC if generic else 0)
+    for k in ("amplitudes", "chi2", "active_mask", "status"):
+        assert np.array_equal(o[k], d[f"{mode}_{k}"]), k
+    assert np.array_equal(o["iters"], pack_iters(d[f"{mode}_iters"]))
+    if errors:
+        assert np.array_equal(o["errors"], d["err_errors"], equal_nan=True)
+
+
+@pytest.mark.parametrize("errors", [0, 1])
+@pytest.mark.parametrize("name", ["c0", "logamp", "warm", "fpc", "edge"])
+def test_reference_dofit_bit_for_bit(mf, lib, name, errors):
+    g = dict(np.load(os.path.join(GOLDEN, "dofit_ref.npz")))
+    F = g["fullpulsecov"] if bool(g[f"{name}_has_fpc"]) else None
+    cond = mf.make_conditions(g["P"], g["R"], g["bxs"], fullpulsecov=F)
+    o = fit(lib, cond, g[f"{name}_samples"], g[f"{name}_pederr"], 0, 10, errors)
+    assert np.array_equal(o["amplitudes"], g[f"{name}_e{errors}_amplitudes"])
+    assert np.array_equal(o["chi2"], g[f"{name}_e{errors}_chi2"])
+    if errors:
+        assert np.array_equal(o["errors"], g[f"{name}_e{errors}_errors"], equal_nan=True)
+
+
+def synthetic_sets(oracle, n):
+    """(label, conditions arrays, samples, pederr) of seeded ECAL / HCAL channels,
+    ECAL also with a pulse covariance."""
+    fpc = dict(np.load(os.path.join(GOLDEN, "fits_ecal_fpc.npz")))["fullpulsecov"] * 3.0
+    out = []
+    for wl in ("ecal-1m-pu2", "ecal-10m-logamp-pu4", "mixed-10m-ecal-hcal"):
+        inp = oracle.synth_generate(wl, 0, n)
+        for kind in (0, 1):
+            sel = np.nonzero(inp["ctype"] == kind)[0]
+            if sel.size == 0:
+                continue
+            P, R, bxs, _ = oracle.synth_conditions(kind)
+            for F in ([None, fpc] if kind == 0 and wl != "mixed-10m-ecal-hcal" else [None]):
+                out.append((f"{wl}/set{kind}/fpc={F is not None}", (P, R, bxs, F), inp["samples"][sel],
+                            inp["pederr"][sel]))
+    return out
+
+
+@pytest.mark.parametrize("setting", [(0, 10, 0), (1, 1000, 0), (1, 1000, 1), (0, 1000, 1)])
+def test_oracle_bit_for_bit_with_flop_counts(mf, oracle, lib, setting):
+    start, max_iter, errors = setting
+    for label, (P, R, bxs, F), s, pe in synthetic_sets(oracle, 3000):
+        cond = mf.make_conditions(P, R, bxs, fullpulsecov=F)
+        ref = oracle.fit_batch(s, pe, P, R, bxs, fullpulsecov=F, max_iter_nnls=max_iter, start=start,
+                               compute_errors=bool(errors), count_flops=True)
+        for flags in (0, F_COUNT):
+            o = fit(lib, cond, s, pe, start, max_iter, errors, flags)
+            keys = ["amplitudes", "chi2", "active_mask", "status"] + (["errors"] if errors else [])
+            keys += ["flops"] if flags == F_COUNT else []
+            for k in keys:
+                assert np.array_equal(o[k], ref[k], equal_nan=True), (label, flags, k)
+            assert np.array_equal(o["iters"], pack_iters(ref["iters"])), label
+
+
+@pytest.mark.parametrize("strides", [(13, 12), (10, 11), (16, 10), (10, 10)])
+def test_staging_padded_strides_and_other_sets(mf, lib, strides):
+    """Samples read from rows wider than N, amplitudes written to rows wider than
+    K (zeros up to KMAX, nothing beyond), and channels of another condition set
+    (every third one here) neither read as this set's nor written."""
+    d = dict(np.load(os.path.join(GOLDEN, "fits_ecal_logamp.npz")))
+    cond = mf.make_conditions(d["P"], d["R"], d["bxs"])
+    n = 77  # two full warps and a partial one
+    ss, ast = strides
+    o = fit(lib, cond, d["samples"][:n], d["pederr"][:n], 0, 10, 0, sample_stride=ss, amp_stride=ast,
+            skip_every=3, fill=-5.0)
+    mine = np.arange(n) % 3 != 2
+    assert np.array_equal(o["amplitudes"][mine, :10], d["ref_amplitudes"][:n][mine])
+    assert np.array_equal(o["chi2"][mine], d["ref_chi2"][:n][mine])
+    assert (o["amplitudes"][~mine] == -5.0).all()
+    assert (o["amplitudes"][:, 10:] == -5.0).all()
+
+
+@pytest.mark.parametrize("errors", [0, 1])
+def test_seeded_continuation_finishes_the_oracle_fit(mf, oracle, lib, errors):
+    """The per-channel form hands the FP64 kernel the first outer iteration's
+    amplitudes, chi2 and status; from the oracle's own first iteration the
+    kernel's continuation (division variant) must end at the oracle's full fit."""
+    fpc = dict(np.load(os.path.join(GOLDEN, "fits_ecal_fpc.npz")))["fullpulsecov"] * 3.0
+    P, R, bxs, _ = oracle.synth_conditions(0)
+    inp = oracle.synth_generate("ecal-1m-pu2", 0, 1500)
+    s, pe = inp["samples"], inp["pederr"]
+    cond = mf.make_conditions(P, R, bxs, fullpulsecov=fpc)
+    first = oracle.fit_batch(s, pe, P, R, bxs, fullpulsecov=fpc, max_iter_nnls=1000, start=1, max_iter_outer=1)
+    full = oracle.fit_batch(s, pe, P, R, bxs, fullpulsecov=fpc, max_iter_nnls=1000, start=1,
+                            compute_errors=bool(errors))
+    o = fit(lib, cond, s, pe, 1, 1000, errors, F_SEEDED, seed=first)
+    for k in ["amplitudes", "chi2", "active_mask"] + (["errors"] if errors else []):
+        assert np.array_equal(o[k], full[k], equal_nan=True), k
+    outer = pack_iters(full["iters"]) & 0xFF
+    assert np.array_equal(o["iters"] & 0xFF, outer)
+    # the pulse covariance makes the loop iterate: most channels go on past the first iteration
+    assert (outer > 2).mean() > 0.5
