@@ -198,6 +198,7 @@ int fill_args(mf_context* ctx, const mf_batch* b, const mf_options* o, FitArgs* 
   a->iters = b->iters;
   a->flops = nullptr;
   a->seeded = 0;
+  a->sms = ctx->sms;
   return MF_OK;
 }
 

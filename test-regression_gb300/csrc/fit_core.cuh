@@ -345,8 +345,6 @@ struct FitState {
   FnnlsOut st;
   int outer_iters;
   int outer_maxed;
-  int first_iter;  // Minimize's first outer iteration (1 when the first was done elsewhere)
-  int first_done;  // ... and whether the stopping rule already held after it
 };
 
 // element (i, k) of the pulse matrix the fit uses: the condition set's, with
@@ -405,36 +403,28 @@ __device__ T compute_chisq(const DevConditions& c, int N, int K, const FitState<
   return chi2;
 }
 
-// NNLS + Minimize, multifit_cpu/src/PulseChiSqSNNLS.cpp:149-166, 219-273.
-// `lanes` = the lanes of the warp that run this call together. The outer
-// iterations are warp-uniform (a ballot at the loop head), and the lanes
-// reconverge after the divergent FNNLS: on this GPU an FP64 warp instruction
-// costs the full pipe time whatever the number of active lanes, so the
-// covariance factor, the whitening and chi2 must be issued once for all lanes
-// rather than once per group of lanes that left FNNLS together.
+// One outer iteration of Minimize (multifit_cpu/src/PulseChiSqSNNLS.cpp:
+// 149-166, with NNLS :219-273): covariance and its factor, whitening, FNNLS
+// from the current amplitudes, chi2; returns |delta chi2| < tol. `act` = the
+// lanes of the warp running an iteration together: they reconverge after the
+// divergent FNNLS, because on this GPU an FP64 warp instruction costs the full
+// pipe time whatever the number of active lanes, so chi2 must be issued once
+// for all of them rather than once per group of lanes that left FNNLS together.
 template <int NT, int KT, bool C, typename T, bool R = false>
-__device__ void minimize(const DevConditions& c, const DevOptions& o, int N, int K, T pederr, FitState<T>& S,
-                         Counter<C>& f, unsigned lanes) {
-  bool done = S.first_done != 0;
-  for (int it = S.first_iter;; ++it) {
-    const bool run = !done && it < o.max_iter_outer;
-    const unsigned act = __ballot_sync(lanes, run);
-    if (act == 0u) break;
-    if (!run) continue;
-    update_cov<NT, KT, C, T, R>(c, N, K, pederr, S, f);
-    T A[KMAX * KMAX], b[KMAX];
-    for (int k = 0; k < K; ++k) fwd<C, T, R>(S.LC, [&](int i) { return pulse(c, S, N, k, i); }, A + k * N, N, f, S.LCr);
-    fwd<C, T, R>(S.LC, [&](int i) { return S.samp[i]; }, b, N, f, S.LCr);
-    fnnls<NT, KT>(A, b, S.amp, N, K, T(o.nnls_eps), o.max_iter_nnls, o.nnls_start, S.st, f);
-    __syncwarp(act);
-    const T now = compute_chisq<C, T, R>(c, N, K, S, f);
-    const T delta = now - S.chisq;
-    f.op(1);
-    S.chisq = now;
-    ++S.outer_iters;
-    if (fabsT(delta) < T(o.dchi2_tol)) done = true;
-  }
-  if (!done) S.outer_maxed = 1;
+__device__ bool outer_iteration(const DevConditions& c, const DevOptions& o, int N, int K, T pederr,
+                                FitState<T>& S, Counter<C>& f, unsigned act) {
+  update_cov<NT, KT, C, T, R>(c, N, K, pederr, S, f);
+  T A[KMAX * KMAX], b[KMAX];
+  for (int k = 0; k < K; ++k) fwd<C, T, R>(S.LC, [&](int i) { return pulse(c, S, N, k, i); }, A + k * N, N, f, S.LCr);
+  fwd<C, T, R>(S.LC, [&](int i) { return S.samp[i]; }, b, N, f, S.LCr);
+  fnnls<NT, KT>(A, b, S.amp, N, K, T(o.nnls_eps), o.max_iter_nnls, o.nnls_start, S.st, f);
+  __syncwarp(act);
+  const T now = compute_chisq<C, T, R>(c, N, K, S, f);
+  const T delta = now - S.chisq;
+  f.op(1);
+  S.chisq = now;
+  ++S.outer_iters;
+  return fabsT(delta) < T(o.dchi2_tol);
 }
 
 // ComputeApproxUncertainty, multifit_cpu/src/PulseChiSqSNNLS.cpp:202-207
@@ -448,15 +438,13 @@ __device__ T approx_uncertainty(const DevConditions& c, int N, const FitState<T>
   f.op(2);
   return T(1) / sqrtT(n2);
 }
-
 // Coalesced staging of a warp's channel rows through shared memory: rows
 // [ch0, ch0 + nw) (nw <= 32) of a row-major array with `stride` elements per
-// row, `width` <= KMAX elements of each, to or from `rows` (KMAX per row).
-// Lane `lane` moves elements lane, lane + 32, ... of the warp's nw x width
-// block, so consecutive lanes touch consecutive addresses (a channel's own
-// row, read by its thread, is 80 bytes wide: 32 lanes reading their own rows
-// touch 32 rows per instruction). The store writes only the rows whose bit
-// is set in `sel` (the channels of the launch's condition set).
+// row, `width` <= KMAX elements of each, into `rows` (KMAX per row). Lane
+// `lane` moves elements lane, lane + 32, ... of the warp's nw x width block,
+// so consecutive lanes read consecutive addresses (a channel's own row, read
+// by its thread, is 80 bytes wide: 32 lanes reading their own rows touch 32
+// rows per instruction).
 __device__ __forceinline__ void stage_rows_in(const double* src, int64_t stride, int64_t ch0, int nw, int width,
                                               double* rows, int lane) {
   for (int e = lane; e < nw * width; e += 32) {
@@ -465,136 +453,184 @@ __device__ __forceinline__ void stage_rows_in(const double* src, int64_t stride,
   }
 }
 
-__device__ __forceinline__ void stage_rows_out(const double* rows, double* dst, int64_t stride, int64_t ch0, int nw,
-                                               int width, unsigned sel, int lane) {
-  for (int e = lane; e < nw * width; e += 32) {
-    const int r = e / width, i = e - r * width;
-    if ((sel >> r) & 1u) dst[(ch0 + r) * stride + i] = rows[r * KMAX + i];
-  }
-}
-
-// DoFit, multifit_cpu/src/PulseChiSqSNNLS.cpp:21-147, for channel ch of the
-// batch: the main Minimize, then (with errors on) the two constrained refits
-// of the in-time amplitude, and the outputs. mini(S, pederr, lanes) is the
-// Minimize the caller uses; it runs on the lanes given. `in` holds the
-// channel's N samples; the K amplitudes, then zeros up to `out_width`
-// values, are written to `out` (the caller stages both rows).
+// DoFit (multifit_cpu/src/PulseChiSqSNNLS.cpp:21-147) of one channel as a
+// sequence of steps, so that a lane can take its next channel as soon as its
+// own is done instead of idling until the slowest lane of its warp finishes
+// (channels need 2 or 3 outer iterations, and the error estimate one or two
+// more Minimize calls). The per-channel arithmetic and its order are those
+// of DoFit; only the schedule across channels changes.
+//
+// start() loads the channel. prepare() moves on while the current Minimize
+// has stopped (main fit -> refit with the in-time amplitude held above its
+// value -> refit held below it -> done) and returns true when an outer
+// iteration is to run, false once the channel is finished and its outputs
+// are written. iterate() runs that outer iteration.
 //
 // With a.seeded the main Minimize's first outer iteration has been done
-// already (the per-channel form of the mixed and FP32 precisions: with the
-// amplitudes at zero the covariance is pederr^2 samplecor, the problem of the
-// passive-set tables): its amplitudes and chi2 are read from the outputs and
-// the loop goes on from the second iteration, with the reference's stopping
-// rule against that chi2 (against 0 after the first iteration).
-template <int NT, int KT, bool C, bool R = false, typename Mini>
-__device__ void dofit_with(const FitArgs& a, const DevConditions& c, int64_t ch, unsigned lanes, Counter<C>& f,
-                           const double* in, double* out, int out_width, Mini&& mini) {
-  const int N = NT > 0 ? NT : c.N;
-  const int K = KT > 0 ? KT : c.K;
+// already and its amplitudes, chi2 and status are read from the outputs; the
+// loop goes on from the second iteration, with the reference's stopping rule
+// against that chi2 (against 0 after the first iteration). seeded = 1: the
+// per-channel form of the mixed and FP32 precisions (with the amplitudes at
+// zero the covariance is pederr^2 samplecor, the problem of the passive-set
+// tables); seeded = 2: the FP64 kernel's own first pass, whose FNNLS
+// counters (iters) and executed flops are carried on too, so that the two
+// passes together give the single fit's outputs bit for bit.
+template <int NT, int KT, bool C, bool R = false>
+struct ChannelFit {
   FitState<double> S;
-  const double pederr = a.pederr[ch];
-  bool bad = !isfinite(pederr);
-  for (int i = 0; i < N; ++i) {
-    S.samp[i] = in[i];
-    bad = bad || !isfinite(S.samp[i]);
-  }
-  S.zcol = -1;
-  for (int k = 0; k < K; ++k) S.amp[k] = 0.;
-  S.chisq = 0.;
-  S.st = FnnlsOut{0, 0, 0, 0};
-  S.outer_iters = 0;
-  S.outer_maxed = 0;
-  S.first_iter = 0;
-  S.first_done = 0;
-  if (a.seeded) {
-    const double* seed = a.amplitudes + ch * a.amp_stride;
-    const bool maxed = a.status && (a.status[ch] & CH_NNLS_MAXITER);
-    if (a.opt.compute_errors && fabs(a.chi2[ch]) < a.opt.dchi2_tol) {
-      // the loop stops at once: the error refits need the first iteration's
-      // covariance factor, that of pederr^2 samplecor
-      update_cov<NT, KT, C, double, R>(c, N, K, pederr, S, f);
+  double samp0[KMAX];   // the channel's samples (the refits fit shifted copies)
+  double ampmin[KMAX];  // the main fit's amplitudes
+  double pederr, chisq0, x0, approxerr, sigmaplus, err;
+  int64_t ch;
+  FnnlsOut main_st;
+  int main_outer, main_maxed;
+  int it;     // outer iteration of the current Minimize
+  int phase;  // 0 main fit, 1 upper refit, 2 lower refit
+  bool done, bad;
+  Counter<C> f;
+
+  // samples: the channel's N samples (a warp's staging row)
+  __device__ void start(const FitArgs& a, const DevConditions& c, int64_t channel, const double* samples) {
+    const int N = NT > 0 ? NT : c.N;
+    const int K = KT > 0 ? KT : c.K;
+    ch = channel;
+    f = Counter<C>{};
+    pederr = a.pederr[ch];
+    bad = !isfinite(pederr);
+    for (int i = 0; i < N; ++i) {
+      samp0[i] = samples[i];
+      S.samp[i] = samples[i];
+      bad = bad || !isfinite(samples[i]);
     }
-    for (int k = 0; k < K; ++k) S.amp[k] = seed[k];
-    S.chisq = a.chi2[ch];
-    S.st.converged = maxed ? 0 : 1;
-    S.outer_iters = 1;
-    S.first_iter = 1;
-    S.first_done = fabs(S.chisq) < a.opt.dchi2_tol ? 1 : 0;
-  }
-
-  mini(S, pederr, lanes);
-  S.first_iter = 0;  // the error refits run their whole loop
-  S.first_done = 0;
-  const FnnlsOut main_st = S.st;
-  const int main_outer = S.outer_iters;
-  const int main_maxed = S.outer_maxed;
-  double ampmin[KMAX];
-  for (int k = 0; k < K; ++k) ampmin[k] = S.amp[k];
-  double err = 0.;
-
-  if (a.opt.compute_errors && c.intime_col >= 0) {
-    const int kin = c.intime_col;
-    const double approxerr = approx_uncertainty<C, double, R>(c, N, S, kin, f);
-    const double chisq0 = S.chisq;
-    const double x0 = ampmin[kin];
-    double pulse_in[KMAX];
-    for (int i = 0; i < N; ++i) pulse_in[i] = c.P[kin * N + i];
-    S.zcol = kin;
-    const double xplus = x0 + approxerr;
-    S.amp[kin] = xplus;
-    for (int i = 0; i < N; ++i) S.samp[i] = fma(-xplus, pulse_in[i], in[i]);
-    mini(S, pederr, lanes);
-    const double chip = compute_chisq<C, double, R>(c, N, K, S, f);
-    const double sigmaplus = fabs(xplus - x0) / sqrt(chip - chisq0);
-    const bool lower = x0 / sigmaplus > 0.5;
-    const unsigned lanes2 = __ballot_sync(lanes, lower);
-    if (lower) {
-      const double xminus = (x0 - approxerr) > 0. ? (x0 - approxerr) : 0.;
-      S.amp[kin] = xminus;
-      for (int i = 0; i < N; ++i) S.samp[i] = fma(-xminus, pulse_in[i], in[i]);
-      mini(S, pederr, lanes2);
-      const double chim = compute_chisq<C, double, R>(c, N, K, S, f);
-      const double sigmaminus = fabs(xminus - x0) / sqrt(chim - chisq0);
-      err = 0.5 * (sigmaplus + sigmaminus);
-    } else {
-      err = sigmaplus;
+    S.zcol = -1;
+    for (int k = 0; k < K; ++k) S.amp[k] = 0.;
+    S.chisq = 0.;
+    S.st = FnnlsOut{0, 0, 0, 0};
+    S.outer_iters = 0;
+    S.outer_maxed = 0;
+    it = 0;
+    done = false;
+    phase = 0;
+    err = 0.;
+    if (a.seeded) {
+      const double* seed = a.amplitudes + ch * a.amp_stride;
+      const bool maxed = a.status && (a.status[ch] & CH_NNLS_MAXITER);
+      if (a.opt.compute_errors && fabs(a.chi2[ch]) < a.opt.dchi2_tol) {
+        // the loop stops at once: the error refits need the first iteration's
+        // covariance factor, that of pederr^2 samplecor
+        update_cov<NT, KT, C, double, R>(c, N, K, pederr, S, f);
+      }
+      for (int k = 0; k < K; ++k) S.amp[k] = seed[k];
+      S.chisq = a.chi2[ch];
+      S.st.converged = maxed ? 0 : 1;
+      S.outer_iters = 1;
+      if (a.seeded == 2) {
+        if (a.iters) {
+          S.st.outer = (a.iters[ch] >> 8) & 0xfff;
+          S.st.inner = (a.iters[ch] >> 20) & 0xfff;
+        }
+        if (C && a.flops) f.f.v = a.flops[ch];
+      }
+      it = 1;
+      done = fabs(S.chisq) < a.opt.dchi2_tol;
     }
-    S.chisq = chisq0;
   }
 
-  bool finite = isfinite(S.chisq);
-  for (int k = 0; k < K; ++k) {
-    out[k] = ampmin[k];
-    finite = finite && isfinite(ampmin[k]);
+  __device__ bool prepare(const FitArgs& a, const DevConditions& c) {
+    const int N = NT > 0 ? NT : c.N;
+    const int K = KT > 0 ? KT : c.K;
+    for (;;) {
+      if (!done && it < a.opt.max_iter_outer) return true;
+      // the current Minimize has stopped
+      if (!done) S.outer_maxed = 1;
+      const int kin = c.intime_col;
+      if (phase == 0) {
+        main_st = S.st;
+        main_outer = S.outer_iters;
+        main_maxed = S.outer_maxed;
+        for (int k = 0; k < K; ++k) ampmin[k] = S.amp[k];
+        if (!(a.opt.compute_errors && kin >= 0)) break;
+        approxerr = approx_uncertainty<C, double, R>(c, N, S, kin, f);
+        chisq0 = S.chisq;
+        x0 = ampmin[kin];
+        S.zcol = kin;  // the in-time column held fixed
+        const double xplus = x0 + approxerr;
+        S.amp[kin] = xplus;
+        for (int i = 0; i < N; ++i) S.samp[i] = fma(-xplus, c.P[kin * N + i], samp0[i]);
+        phase = 1;
+      } else if (phase == 1) {
+        const double xplus = x0 + approxerr;
+        const double chip = compute_chisq<C, double, R>(c, N, K, S, f);
+        sigmaplus = fabs(xplus - x0) / sqrt(chip - chisq0);
+        if (!(x0 / sigmaplus > 0.5)) {
+          err = sigmaplus;
+          S.chisq = chisq0;
+          break;
+        }
+        const double xminus = (x0 - approxerr) > 0. ? (x0 - approxerr) : 0.;
+        S.amp[kin] = xminus;
+        for (int i = 0; i < N; ++i) S.samp[i] = fma(-xminus, c.P[kin * N + i], samp0[i]);
+        phase = 2;
+      } else {
+        const double xminus = (x0 - approxerr) > 0. ? (x0 - approxerr) : 0.;
+        const double chim = compute_chisq<C, double, R>(c, N, K, S, f);
+        const double sigmaminus = fabs(xminus - x0) / sqrt(chim - chisq0);
+        err = 0.5 * (sigmaplus + sigmaminus);
+        S.chisq = chisq0;
+        break;
+      }
+      // a refit: the whole Minimize loop, from the chi2 of the main fit
+      it = 0;
+      done = false;
+    }
+    finish(a, c);
+    return false;
   }
-  for (int k = K; k < out_width; ++k) out[k] = 0.;
-  a.chi2[ch] = S.chisq;
-  if (a.intime) a.intime[ch] = c.intime_col >= 0 ? ampmin[c.intime_col] : 0.;
-  if (a.errors) a.errors[ch] = err;
-  if (a.active_mask) {
-    // support of X(): the last FNNLS call restarts from an empty passive set
-    // and usually stops at once, so its passive set is not the fitted set
-    uint16_t support = 0;
-    for (int k = 0; k < K; ++k)
-      if (ampmin[k] > 0.) support |= uint16_t(1u << k);
-    a.active_mask[ch] = support;
+
+  __device__ void iterate(const FitArgs& a, const DevConditions& c, unsigned act) {
+    const int N = NT > 0 ? NT : c.N;
+    const int K = KT > 0 ? KT : c.K;
+    done = outer_iteration<NT, KT, C, double, R>(c, a.opt, N, K, pederr, S, f, act);
+    ++it;
   }
-  if (a.status) {
-    uint8_t st = 0;
-    if (!main_st.converged) st |= CH_NNLS_MAXITER;
-    if (main_maxed) st |= CH_OUTER_MAXITER;
-    if (!finite) st |= CH_NONFINITE;
-    if (bad) st |= CH_BADINPUT;
-    a.status[ch] = st;
+
+  __device__ void finish(const FitArgs& a, const DevConditions& c) {
+    const int K = KT > 0 ? KT : c.K;
+    double* out = a.amplitudes + ch * a.amp_stride;
+    bool finite = isfinite(S.chisq);
+    for (int k = 0; k < K; ++k) {
+      out[k] = ampmin[k];
+      finite = finite && isfinite(ampmin[k]);
+    }
+    for (int k = K; k < a.amp_stride && k < KMAX; ++k) out[k] = 0.;
+    a.chi2[ch] = S.chisq;
+    if (a.intime) a.intime[ch] = c.intime_col >= 0 ? ampmin[c.intime_col] : 0.;
+    if (a.errors) a.errors[ch] = err;
+    if (a.active_mask) {
+      // support of X(): the last FNNLS call restarts from an empty passive set
+      // and usually stops at once, so its passive set is not the fitted set
+      uint16_t support = 0;
+      for (int k = 0; k < K; ++k)
+        if (ampmin[k] > 0.) support |= uint16_t(1u << k);
+      a.active_mask[ch] = support;
+    }
+    if (a.status) {
+      uint8_t st = 0;
+      if (!main_st.converged) st |= CH_NNLS_MAXITER;
+      if (main_maxed) st |= CH_OUTER_MAXITER;
+      if (!finite) st |= CH_NONFINITE;
+      if (bad) st |= CH_BADINPUT;
+      a.status[ch] = st;
+    }
+    if (a.iters) {
+      const int o8 = main_outer < 255 ? main_outer : 255;
+      const int fo = main_st.outer < 4095 ? main_st.outer : 4095;
+      const int fi = main_st.inner < 4095 ? main_st.inner : 4095;
+      a.iters[ch] = o8 | (fo << 8) | (fi << 20);
+    }
+    if (C && a.flops) a.flops[ch] = f.f.v;
   }
-  if (a.iters) {
-    const int o8 = main_outer < 255 ? main_outer : 255;
-    const int fo = main_st.outer < 4095 ? main_st.outer : 4095;
-    const int fi = main_st.inner < 4095 ? main_st.inner : 4095;
-    a.iters[ch] = o8 | (fo << 8) | (fi << 20);
-  }
-  if (C && a.flops) a.flops[ch] = f.f.v;
-}
+};
 
 }  // namespace
 }  // namespace mfgb

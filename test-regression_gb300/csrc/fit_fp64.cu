@@ -22,21 +22,6 @@
 namespace mfgb {
 namespace {
 
-// DoFit with the FP64 Minimize: the plain drop-in (R = false), or the
-// per-channel form's FP64 continuation (R = true: the covariance factor's
-// diagonal inverted once per row, multiplications for the ~(K + 3) N
-// divisions of the factor, whitening and chi2 -- on this GPU an FP64 division
-// is a sequence of about ten FP64 instructions).
-template <int NT, int KT, bool C, bool R>
-__device__ void dofit(const FitArgs& a, const DevConditions& c, int64_t ch, unsigned lanes, double* row) {
-  const int N = NT > 0 ? NT : c.N;
-  const int K = KT > 0 ? KT : c.K;
-  Counter<C> f;
-  dofit_with<NT, KT, C, R>(a, c, ch, lanes, f, row, row, KMAX, [&](FitState<double>& S, double pederr, unsigned ln) {
-    minimize<NT, KT, C, double, R>(c, a.opt, N, K, pederr, S, f, ln);
-  });
-}
-
 constexpr int kFitBlock = 128;  // the largest block of the kernel (its launch bound)
 // Three blocks of 128 per SM: 168 registers a thread, with which the unrolled
 // 10 x 10 fit keeps its working set in registers and its packed arrays in a
@@ -44,59 +29,144 @@ constexpr int kFitBlock = 128;  // the largest block of the kernel (its launch b
 // 2.3 KB); 12 warps per SM keep the FP64 pipe ~90 % busy.
 constexpr int kFitBlocksPerSm = 3;
 
-// One launch per condition set (lanes of other sets idle); out-of-range set
-// indices are flagged by the first launch. A warp stages its 32 channels'
-// samples, and afterwards their amplitudes, through one shared-memory row per
-// channel with coalesced loads and stores.
-template <int NT, int KT, bool C, bool R = false>
-__global__ void __launch_bounds__(kFitBlock, kFitBlocksPerSm) fit_fp64_kernel(const FitArgs a, int set, int flag_bad) {
+// DoFit with the FP64 Minimize: the plain drop-in (R = false), or the
+// per-channel form's FP64 continuation (R = true: the covariance factor's
+// diagonal inverted once per row, multiplications for the ~(K + 3) N
+// divisions of the factor, whitening and chi2 -- on this GPU an FP64 division
+// is a sequence of about ten FP64 instructions).
+//
+// One wave of resident warps; warp w fits the channels of condition set `set`
+// in [w chunk, (w + 1) chunk), a lane one channel at a time, one outer
+// iteration per step (ChannelFit). The warp stages each batch of 32
+// channels' samples through one shared-memory row per channel with coalesced
+// loads; channels of other sets are skipped (their lanes do not idle through
+// another set's fits), those with an out-of-range set index flagged by the
+// first launch.
+//
+// Two ways to hand out channels. A channel's first outer iteration is its
+// costliest (its FNNLS starts from x = 0 and adds ~9 columns one by one; the
+// later ones, from the previous amplitudes, add ~0.3), so a warp fits the
+// first iterations of 32 channels side by side (REFILL = false: new channels
+// only once every lane is done). The later iterations (2 or 3 per channel, 3
+// in nearly every warp of 32) run with REFILL = true: a lane takes the warp's
+// next channel as soon as its own is done, so no lane idles through another
+// channel's third iteration. (Refilling the first pass too put a first
+// iteration's FNNLS into every step: 27.5 -> 36.5 ms per 1M channels.)
+template <int NT, int KT, bool C, bool R, bool REFILL>
+__global__ void __launch_bounds__(kFitBlock, kFitBlocksPerSm)
+    fit_fp64_kernel(const FitArgs a, int set, int flag_bad, int64_t chunk) {
   __shared__ double stage[kFitBlock * KMAX];
   const int lane = int(threadIdx.x & 31u);
-  const int64_t ch = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  bool mine = false;
-  if (ch < a.n) {
-    const int t = a.ctype ? int(a.ctype[ch]) : 0;
-    if (t >= a.n_ctypes) {
-      if (flag_bad) {
-        if (a.status) a.status[ch] = CH_BADINPUT;
-        a.chi2[ch] = 0.;
-      }
-    } else {
-      mine = t == set;
-    }
-  }
-  const unsigned lanes = __ballot_sync(0xffffffffu, mine);  // taken while the warp is converged
-  if (lanes == 0u) return;
+  const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  int64_t next = warp * chunk;  // the warp's next channel to stage
+  const int64_t end = next + chunk < a.n ? next + chunk : a.n;
+  if (next >= end) return;  // warp-uniform
   const DevConditions& c = a.cond[set];
   const int N = NT > 0 ? NT : c.N;
-  const int64_t ch0 = ch - lane;
-  const int nw = a.n - ch0 < 32 ? int(a.n - ch0) : 32;  // the warp's channels inside the batch
   double* const rows = stage + (threadIdx.x - lane) * KMAX;
-  stage_rows_in(a.samples, a.sample_stride, ch0, nw, N, rows, lane);
-  __syncwarp();
-  if (mine) dofit<NT, KT, C, R>(a, c, ch, lanes, rows + lane * KMAX);
-  __syncwarp();
-  // K amplitudes, then zeros up to the row's end or KMAX (amp_stride >= K)
-  stage_rows_out(rows, a.amplitudes, a.amp_stride, ch0, nw, a.amp_stride < KMAX ? a.amp_stride : KMAX, lanes, lane);
+  ChannelFit<NT, KT, C, R> fit;
+  bool busy = false;
+  unsigned avail = 0u;  // staged channels of this set not taken yet (warp-uniform)
+  int64_t sbase = 0;    // first channel of the staged batch
+  for (;;) {
+    if (busy) busy = fit.prepare(a, c);  // false: the channel is done, its outputs written
+    // idle lanes take the staged channels of this set in order, staging the
+    // next batch when these run out (without REFILL only once all are idle)
+    bool filling = REFILL;
+    for (;;) {
+      const unsigned idle = __ballot_sync(0xffffffffu, !busy);
+      if (idle == 0u) break;
+      if (!REFILL && idle == 0xffffffffu) filling = true;
+      if (!filling) break;
+      if (avail == 0u) {
+        if (next >= end) break;
+        const int nw = end - next < 32 ? int(end - next) : 32;
+        __syncwarp();  // every lane has copied its row of the previous batch
+        stage_rows_in(a.samples, a.sample_stride, next, nw, N, rows, lane);
+        bool mine = false;
+        if (lane < nw) {
+          const int64_t ch = next + lane;
+          const int t = a.ctype ? int(a.ctype[ch]) : 0;
+          if (t >= a.n_ctypes) {
+            if (flag_bad) {
+              if (a.status) a.status[ch] = CH_BADINPUT;
+              a.chi2[ch] = 0.;
+            }
+          } else {
+            mine = t == set;
+          }
+        }
+        avail = __ballot_sync(0xffffffffu, mine);
+        sbase = next;
+        next += nw;
+        __syncwarp();  // the staged rows are visible to every lane
+        continue;
+      }
+      const int navail = __popc(avail);
+      const int rank = __popc(idle & ((1u << lane) - 1u));  // among the idle lanes
+      if (!busy && rank < navail) {
+        unsigned m = avail;
+        for (int r = 0; r < rank; ++r) m &= m - 1u;  // drop the lower `rank` channels
+        const int row = __ffs(int(m)) - 1;
+        fit.start(a, c, sbase + row, rows + row * KMAX);
+        busy = fit.prepare(a, c);
+      }
+      const int taken = __popc(idle) < navail ? __popc(idle) : navail;
+      for (int r = 0; r < taken; ++r) avail &= avail - 1u;
+    }
+    const unsigned act = __ballot_sync(0xffffffffu, busy);
+    if (act == 0u) break;
+    if (busy) fit.iterate(a, c, act);
+  }
 }
 
 }  // namespace
 
+template <bool C, bool REFILL>
+cudaError_t launch_pass(const FitArgs& a, int t, unsigned grid, int block, int64_t chunk, cudaStream_t s) {
+  const DevConditions& c = a.cond[t];
+  const int flag = t == 0;
+  // the per-channel form's continuation with reciprocals (its instrumented
+  // count runs the division form)
+  if (a.seeded == 1 && !C && c.N == 10 && c.K == 10)
+    fit_fp64_kernel<10, 10, false, true, REFILL><<<grid, block, 0, s>>>(a, t, flag, chunk);
+  else if (a.seeded == 1 && !C) fit_fp64_kernel<0, 0, false, true, REFILL><<<grid, block, 0, s>>>(a, t, flag, chunk);
+  else if (c.N == 10 && c.K == 10) fit_fp64_kernel<10, 10, C, false, REFILL><<<grid, block, 0, s>>>(a, t, flag, chunk);
+  else if (c.N == 8 && c.K == 8) fit_fp64_kernel<8, 8, C, false, REFILL><<<grid, block, 0, s>>>(a, t, flag, chunk);
+  else fit_fp64_kernel<0, 0, C, false, REFILL><<<grid, block, 0, s>>>(a, t, flag, chunk);
+  return cudaGetLastError();
+}
+
+// Per condition set: the first outer iteration of every channel in lockstep,
+// then the rest of the fit (later iterations, error refits) with refill,
+// seeded from the first pass's outputs. A fit of one outer iteration at most,
+// and the per-channel form's continuation (seeded already), run in one pass.
 template <bool C>
 cudaError_t launch_sets(const FitArgs& a, int block, cudaStream_t s, LaunchTimer* tm) {
-  const unsigned grid = unsigned((a.n + block - 1) / block);
+  // one wave of resident blocks, the channels split evenly over its warps
+  const int64_t resident = int64_t(a.sms > 0 ? a.sms : 1) * kFitBlocksPerSm * (kFitBlock / block);
+  const int64_t needed = (a.n + block - 1) / block;
+  const unsigned grid = unsigned(needed < resident ? needed : resident);
+  const int64_t warps = int64_t(grid) * (block / 32);
+  const int64_t chunk = (a.n + warps - 1) / warps;
+  const bool two_pass = !a.seeded && a.opt.max_iter_outer > 1;
+  FitArgs first = a;
+  first.opt.max_iter_outer = 1;
+  first.opt.compute_errors = 0;
+  FitArgs rest = a;
+  rest.seeded = 2;
   for (int t = 0; t < a.n_ctypes; ++t) {
-    const DevConditions& c = a.cond[t];
-    const int flag = t == 0;
-    if (tm) tm->mark(MF_K_FIT_FP64, s);
-    // the seeded continuation of the per-channel form with reciprocals (its
-    // instrumented count runs the division form)
-    if (a.seeded && !C && c.N == 10 && c.K == 10) fit_fp64_kernel<10, 10, false, true><<<grid, block, 0, s>>>(a, t, flag);
-    else if (a.seeded && !C) fit_fp64_kernel<0, 0, false, true><<<grid, block, 0, s>>>(a, t, flag);
-    else if (c.N == 10 && c.K == 10) fit_fp64_kernel<10, 10, C><<<grid, block, 0, s>>>(a, t, flag);
-    else if (c.N == 8 && c.K == 8) fit_fp64_kernel<8, 8, C><<<grid, block, 0, s>>>(a, t, flag);
-    else fit_fp64_kernel<0, 0, C><<<grid, block, 0, s>>>(a, t, flag);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e;
+    if (two_pass) {
+      if (tm) tm->mark(MF_K_FIT_FP64, s);
+      e = launch_pass<C, false>(first, t, grid, block, chunk, s);
+      if (e != cudaSuccess) return e;
+      if (tm) tm->mark(MF_K_FIT_FP64, s);
+      e = launch_pass<C, true>(rest, t, grid, block, chunk, s);
+    } else {
+      if (tm) tm->mark(MF_K_FIT_FP64, s);
+      e = a.seeded ? launch_pass<C, true>(a, t, grid, block, chunk, s) : launch_pass<C, false>(a, t, grid, block, chunk, s);
+    }
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;

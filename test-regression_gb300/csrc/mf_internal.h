@@ -52,7 +52,12 @@ struct FitArgs {
   uint8_t* status;
   int32_t* iters;
   double* flops;  // optional per-channel executed-flop count (instrumented build only)
-  int seeded;     // 1: outputs hold the first outer iteration's amplitudes and chi2 (fit_core.cuh dofit_with)
+  // 1: the outputs hold the amplitudes, chi2 and status of a first outer
+  // iteration done elsewhere (the per-channel form's passive-set tables);
+  // 2: ... of the FP64 kernel's own first iteration, with its FNNLS counters
+  // in iters and its executed flops in flops (fit_core.cuh ChannelFit)
+  int seeded;
+  int sms;  // the device's SM count (the FP64 kernel launches one wave of resident blocks)
 };
 
 // Status bits (mirror of enum mf_channel_status).

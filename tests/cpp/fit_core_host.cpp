@@ -1,11 +1,11 @@
 // The FP64 drop-in's per-channel routines (test-regression_gb300/csrc/
 // fit_core.cuh) compiled for the host, so that the CPU suite checks the
-// kernel's own arithmetic and storage against the oracle and the golden
-// fixtures without a GPU. The warp-level pieces run one lane at a time: the
-// ballots of a single lane, and the kernel's coalesced staging of samples and
-// amplitudes through a warp's shared-memory rows, lane by lane over a
-// 32-channel block (each lane's part of a staging loop is independent of the
-// others, so running the lanes in turn gives the warp's result).
+// kernel's own arithmetic, storage and schedule against the oracle and the
+// golden fixtures without a GPU. run_warp() is fit_fp64_kernel's warp loop
+// with its 32 lanes in lockstep: the code between two ballots of the kernel
+// is independent across lanes, so running it for lane 0, 1, ..., 31 in turn
+// and forming each ballot from all lanes' values gives the warp's result
+// (which lane takes which channel, when the next batch is staged).
 //
 // Built by tests/test_fit_core_host.py with g++ -ffp-contract=off: fma(),
 // division and sqrt are IEEE-754 on the host as on the GPU, and nothing else
@@ -28,53 +28,117 @@ using namespace mfgb;
 
 namespace {
 
-// The kernel's body for one condition set, a warp (32 channels) at a time;
-// `skip_every` > 0 leaves every skip_every-th channel to "another set": it is
-// neither fitted nor written.
-template <int NT, int KT, bool C, bool R>
-void run(const FitArgs& a, int skip_every) {
-  const DevConditions& c = a.cond[0];
+int popc(unsigned m) { return __builtin_popcount(m); }
+
+// fit_fp64_kernel's loop for the warp fitting set `set` in [next, end)
+template <int NT, int KT, bool C, bool R, bool REFILL>
+void run_warp(const FitArgs& a, int set, int flag_bad, int64_t next, int64_t end) {
+  const DevConditions& c = a.cond[set];
   const int N = NT > 0 ? NT : c.N;
-  const int K = KT > 0 ? KT : c.K;
-  std::vector<double> rows(32 * KMAX);
-  for (int64_t ch0 = 0; ch0 < a.n; ch0 += 32) {
-    const int nw = a.n - ch0 < 32 ? int(a.n - ch0) : 32;
-    std::fill(rows.begin(), rows.end(), NAN);
-    for (int lane = 0; lane < 32; ++lane) stage_rows_in(a.samples, a.sample_stride, ch0, nw, N, rows.data(), lane);
-    unsigned sel = 0;
-    for (int lane = 0; lane < nw; ++lane) {
-      if (skip_every > 0 && (ch0 + lane) % skip_every == skip_every - 1) continue;
-      sel |= 1u << lane;
-      double* row = rows.data() + lane * KMAX;
-      Counter<C> f;
-      dofit_with<NT, KT, C, R>(a, c, ch0 + lane, 1u, f, row, row, KMAX,
-                               [&](FitState<double>& S, double pederr, unsigned ln) {
-                                 minimize<NT, KT, C, double, R>(c, a.opt, N, K, pederr, S, f, ln);
-                               });
+  std::vector<double> rows(32 * KMAX, NAN);
+  std::vector<ChannelFit<NT, KT, C, R>> fit(32);
+  bool busy[32] = {};
+  unsigned avail = 0u;
+  int64_t sbase = 0;
+  for (;;) {
+    for (int l = 0; l < 32; ++l)
+      if (busy[l]) busy[l] = fit[l].prepare(a, c);
+    bool filling = REFILL;
+    for (;;) {
+      unsigned idle = 0u;
+      for (int l = 0; l < 32; ++l)
+        if (!busy[l]) idle |= 1u << l;
+      if (idle == 0u) break;
+      if (!REFILL && idle == 0xffffffffu) filling = true;
+      if (!filling) break;
+      if (avail == 0u) {
+        if (next >= end) break;
+        const int nw = end - next < 32 ? int(end - next) : 32;
+        for (int l = 0; l < 32; ++l) stage_rows_in(a.samples, a.sample_stride, next, nw, N, rows.data(), l);
+        unsigned mine = 0u;
+        for (int l = 0; l < nw; ++l) {
+          const int64_t ch = next + l;
+          const int t = a.ctype ? int(a.ctype[ch]) : 0;
+          if (t >= a.n_ctypes) {
+            if (flag_bad) {
+              if (a.status) a.status[ch] = CH_BADINPUT;
+              a.chi2[ch] = 0.;
+            }
+          } else if (t == set) {
+            mine |= 1u << l;
+          }
+        }
+        avail = mine;
+        sbase = next;
+        next += nw;
+        continue;
+      }
+      const int navail = popc(avail);
+      for (int l = 0; l < 32; ++l) {
+        const int rank = popc(idle & ((1u << l) - 1u));
+        if (!busy[l] && rank < navail) {
+          unsigned m = avail;
+          for (int r = 0; r < rank; ++r) m &= m - 1u;
+          const int row = __builtin_ctz(m);
+          fit[l].start(a, c, sbase + row, rows.data() + row * KMAX);
+          busy[l] = fit[l].prepare(a, c);
+        }
+      }
+      const int taken = popc(idle) < navail ? popc(idle) : navail;
+      for (int r = 0; r < taken; ++r) avail &= avail - 1u;
     }
-    const int width = a.amp_stride < KMAX ? a.amp_stride : KMAX;
-    for (int lane = 0; lane < 32; ++lane)
-      stage_rows_out(rows.data(), a.amplitudes, a.amp_stride, ch0, nw, width, sel, lane);
+    unsigned act = 0u;
+    for (int l = 0; l < 32; ++l)
+      if (busy[l]) act |= 1u << l;
+    if (act == 0u) break;
+    for (int l = 0; l < 32; ++l)
+      if (busy[l]) fit[l].iterate(a, c, act);
   }
 }
 
-template <bool C, bool R>
-void dispatch(const FitArgs& a, bool generic, int skip_every) {
+template <bool C, bool R, bool REFILL>
+void pass(const FitArgs& a, bool generic, int64_t chunk) {
   const int N = a.cond[0].N, K = a.cond[0].K;
-  if (!generic && N == 10 && K == 10) run<10, 10, C, R>(a, skip_every);
-  else if (!generic && N == 8 && K == 8) run<8, 8, C, R>(a, skip_every);
-  else run<0, 0, C, R>(a, skip_every);
+  for (int64_t w0 = 0; w0 < a.n; w0 += chunk) {
+    const int64_t w1 = w0 + chunk < a.n ? w0 + chunk : a.n;
+    if (!generic && N == 10 && K == 10) run_warp<10, 10, C, R, REFILL>(a, 0, 1, w0, w1);
+    else if (!generic && N == 8 && K == 8) run_warp<8, 8, C, R, REFILL>(a, 0, 1, w0, w1);
+    else run_warp<0, 0, C, R, REFILL>(a, 0, 1, w0, w1);
+  }
+}
+
+// launch_sets' passes: the first outer iteration of every channel in
+// lockstep, then the rest with refill, seeded from the first pass's outputs
+template <bool C, bool R>
+void dispatch(const FitArgs& a, bool generic, int64_t chunk) {
+  if (!a.seeded && a.opt.max_iter_outer > 1) {
+    FitArgs* first = new FitArgs(a);
+    first->opt.max_iter_outer = 1;
+    first->opt.compute_errors = 0;
+    pass<C, R, false>(*first, generic, chunk);
+    FitArgs* rest = new FitArgs(a);
+    rest->seeded = 2;
+    pass<C, R, true>(*rest, generic, chunk);
+    delete first;
+    delete rest;
+  } else if (a.seeded) {
+    pass<C, R, true>(a, generic, chunk);
+  } else {
+    pass<C, R, false>(a, generic, chunk);
+  }
 }
 
 }  // namespace
 
 // Fits n channels of one condition set (mf_conditions layout) with the
-// kernel's routines. flags: 1 count flops, 2 reciprocal variant (the
-// per-channel form's continuation), 4 generic-shape instantiation, 8 seeded
-// (amplitudes, chi2 and status hold the first outer iteration on entry).
+// kernel's routines, `chunk` channels per warp. flags: 1 count flops, 2
+// reciprocal variant (the per-channel form's continuation), 4 generic-shape
+// instantiation, 8 seeded (amplitudes, chi2 and status hold the first outer
+// iteration on entry). ctype (or null): each channel's condition set; those
+// of set 1 belong to another launch, those of set 2 or above are flagged.
 extern "C" int fit_core_host(const mf_conditions* cond, const double* samples, int sample_stride,
-                             const double* pederr, int64_t n, int nnls_start, int max_iter_nnls, int compute_errors,
-                             int flags, int skip_every, double* amplitudes, int amp_stride, double* chi2,
+                             const double* pederr, const uint8_t* ctype, int64_t n, int nnls_start, int max_iter_nnls,
+                             int compute_errors, int flags, int64_t chunk, double* amplitudes, int amp_stride, double* chi2,
                              double* intime, double* errors, uint16_t* active_mask, uint8_t* status, int32_t* iters,
                              double* flops) {
   const int N = cond->nsamples, K = cond->npulses;
@@ -93,7 +157,9 @@ extern "C" int fit_core_host(const mf_conditions* cond, const double* samples, i
   for (int i = 0; i < N * N; ++i) d->R[i] = cond->noise_cor[i];
   d->has_fpc = cond->has_fullpulsecov ? 1 : 0;
   if (d->has_fpc) std::memcpy(d->fpc, cond->fullpulsecov, sizeof(double) * (N + 9) * (N + 9));
-  a->n_ctypes = 1;
+  a->cond[1] = a->cond[0];
+  a->n_ctypes = ctype ? 2 : 1;
+  a->ctype = ctype;
   a->opt.max_iter_nnls = max_iter_nnls;
   a->opt.max_iter_outer = 50;
   a->opt.dchi2_tol = 1e-3;
@@ -115,9 +181,10 @@ extern "C" int fit_core_host(const mf_conditions* cond, const double* samples, i
   a->flops = flops;
   a->seeded = (flags & 8) ? 1 : 0;
   const bool generic = (flags & 4) != 0;
-  if (flags & 1) dispatch<true, false>(*a, generic, skip_every);
-  else if (flags & 2) dispatch<false, true>(*a, generic, skip_every);
-  else dispatch<false, false>(*a, generic, skip_every);
+  if (chunk < 1) chunk = 1;
+  if (flags & 1) dispatch<true, false>(*a, generic, chunk);
+  else if (flags & 2) dispatch<false, true>(*a, generic, chunk);
+  else dispatch<false, false>(*a, generic, chunk);
   std::free(a);
   return 0;
 }

@@ -1,11 +1,14 @@
-"""The FP64 drop-in's device routines (csrc/fit_core.cuh) compiled for the host
-(tests/cpp/fit_core_host.cpp) and run on the CPU: bit for bit against the
-golden fixtures, the reference's own DoFit outputs and the oracle (executed
-flop counts included), for the specialised 10x10 / 8x8 and the generic-shape
-instantiations; the kernel's coalesced staging of samples and amplitudes with
-padded strides and with channels of another condition set in the warp; and
-the per-channel form's seeded continuation, which from the oracle's first
-outer iteration must finish the oracle's fit bit for bit.
+"""The FP64 drop-in's device routines (csrc/fit_core.cuh) and its warp loop
+compiled for the host (tests/cpp/fit_core_host.cpp, the warp's 32 lanes in
+lockstep) and run on the CPU: bit for bit against the golden fixtures, the
+reference's own DoFit outputs and the oracle (executed flop counts included),
+for the specialised 10x10 / 8x8 and the generic-shape instantiations and for
+warps given one batch, ragged ranges or hundreds of channels each (lanes
+taking their next channel as their own finishes); the warp's staging of
+samples with padded strides, amplitudes written to wider rows, channels of
+another condition set skipped and out-of-range set indices flagged; and the
+per-channel form's seeded continuation, which from the oracle's first outer
+iteration must finish the oracle's fit bit for bit.
 
 Tolerance: zero (same operations in the same order; IEEE fma, division and
 sqrt on both sides)."""
@@ -35,13 +38,15 @@ def lib(tmp_path_factory):
                     "-I", os.path.join(ROOT, "include"), "-I", os.path.join(ROOT, "test-regression_gb300", "csrc"),
                     os.path.join(ROOT, "tests", "cpp", "fit_core_host.cpp"), "-o", out], check=True)
     L = C.CDLL(out)
-    L.fit_core_host.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int64] + [C.c_int] * 5 + \
-        [C.c_void_p, C.c_int] + [C.c_void_p] * 7
+    L.fit_core_host.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int64] + \
+        [C.c_int] * 4 + [C.c_int64, C.c_void_p, C.c_int] + [C.c_void_p] * 7
     return L
 
 
-def fit(lib, cond, samples, pederr, start, max_iter, errors, flags=0, skip_every=0, sample_stride=None,
+def fit(lib, cond, samples, pederr, start, max_iter, errors, flags=0, chunk=96, ctype=None, sample_stride=None,
         amp_stride=None, seed=None, fill=0.0):
+    """chunk: channels per warp; ctype: per-channel condition set (1: another
+    launch's, 2: out of range), or None."""
     n = samples.shape[0]
     N, K = cond.nsamples, cond.npulses
     ss = sample_stride or N
@@ -56,8 +61,9 @@ def fit(lib, cond, samples, pederr, start, max_iter, errors, flags=0, skip_every
         o["amplitudes"][:, :K] = seed["amplitudes"]
         o["chi2"][:] = seed["chi2"]
         o["status"][:] = seed["status"]
-    rc = lib.fit_core_host(C.byref(cond), s.ctypes.data, ss, pe.ctypes.data, n, start, max_iter, errors, flags,
-                           skip_every, o["amplitudes"].ctypes.data, ast,
+    ct = None if ctype is None else np.ascontiguousarray(ctype, dtype=np.uint8)
+    rc = lib.fit_core_host(C.byref(cond), s.ctypes.data, ss, pe.ctypes.data, None if ct is None else ct.ctypes.data,
+                           n, start, max_iter, errors, flags, chunk, o["amplitudes"].ctypes.data, ast,
                            *[o[k].ctypes.data for k in ("chi2", "intime", "errors", "active_mask", "status", "iters",
                                                         "flops")])
     assert rc == 0
@@ -71,7 +77,9 @@ def test_fixture_bit_for_bit(mf, lib, name, mode, generic):
     d = dict(np.load(os.path.join(GOLDEN, f"fits_{name}.npz")))
     cond = mf.make_conditions(d["P"], d["R"], d["bxs"], fullpulsecov=d.get("fullpulsecov"))
     start, max_iter, errors = MODES[mode]
-    o = fit(lib, cond, d["samples"], d["pederr"], start, max_iter, errors, F_GENERIC if generic else 0)
+    # one warp for the whole fixture, or ragged 77-channel ranges
+    o = fit(lib, cond, d["samples"], d["pederr"], start, max_iter, errors, F_GENERIC if generic else 0,
+            chunk=77 if generic else 1 << 30)
     for k in ("amplitudes", "chi2", "active_mask", "status"):
         assert np.array_equal(o[k], d[f"{mode}_{k}"]), k
     assert np.array_equal(o["iters"], pack_iters(d[f"{mode}_iters"]))
@@ -117,8 +125,8 @@ def test_oracle_bit_for_bit_with_flop_counts(mf, oracle, lib, setting):
         cond = mf.make_conditions(P, R, bxs, fullpulsecov=F)
         ref = oracle.fit_batch(s, pe, P, R, bxs, fullpulsecov=F, max_iter_nnls=max_iter, start=start,
                                compute_errors=bool(errors), count_flops=True)
-        for flags in (0, F_COUNT):
-            o = fit(lib, cond, s, pe, start, max_iter, errors, flags)
+        for flags, chunk in ((0, 640), (F_COUNT, 32)):
+            o = fit(lib, cond, s, pe, start, max_iter, errors, flags, chunk=chunk)
             keys = ["amplitudes", "chi2", "active_mask", "status"] + (["errors"] if errors else [])
             keys += ["flops"] if flags == F_COUNT else []
             for k in keys:
@@ -126,21 +134,28 @@ def test_oracle_bit_for_bit_with_flop_counts(mf, oracle, lib, setting):
             assert np.array_equal(o["iters"], pack_iters(ref["iters"])), label
 
 
+@pytest.mark.parametrize("chunk", [20, 77, 1 << 30])
 @pytest.mark.parametrize("strides", [(13, 12), (10, 11), (16, 10), (10, 10)])
-def test_staging_padded_strides_and_other_sets(mf, lib, strides):
+def test_staging_strides_and_other_sets(mf, lib, strides, chunk):
     """Samples read from rows wider than N, amplitudes written to rows wider than
-    K (zeros up to KMAX, nothing beyond), and channels of another condition set
-    (every third one here) neither read as this set's nor written."""
+    K (zeros up to KMAX, nothing beyond); channels of another condition set
+    (every third one) neither fitted nor written, channels with an
+    out-of-range set index flagged (status BADINPUT, chi2 0)."""
     d = dict(np.load(os.path.join(GOLDEN, "fits_ecal_logamp.npz")))
     cond = mf.make_conditions(d["P"], d["R"], d["bxs"])
-    n = 77  # two full warps and a partial one
+    n = 250
     ss, ast = strides
-    o = fit(lib, cond, d["samples"][:n], d["pederr"][:n], 0, 10, 0, sample_stride=ss, amp_stride=ast,
-            skip_every=3, fill=-5.0)
-    mine = np.arange(n) % 3 != 2
+    idx = np.arange(n)
+    ctype = np.where(idx % 3 == 2, 1, 0)
+    ctype[idx % 41 == 40] = 2
+    o = fit(lib, cond, d["samples"][:n], d["pederr"][:n], 0, 10, 0, chunk=chunk, ctype=ctype, sample_stride=ss,
+            amp_stride=ast, fill=-5.0)
+    mine, other, bad = ctype == 0, ctype == 1, ctype == 2
     assert np.array_equal(o["amplitudes"][mine, :10], d["ref_amplitudes"][:n][mine])
     assert np.array_equal(o["chi2"][mine], d["ref_chi2"][:n][mine])
-    assert (o["amplitudes"][~mine] == -5.0).all()
+    assert np.array_equal(o["status"][mine], d["ref_status"][:n][mine])
+    assert (o["amplitudes"][other | bad] == -5.0).all() and (o["chi2"][other] == 0).all()
+    assert (o["status"][bad] == 8).all() and (o["chi2"][bad] == 0).all()
     assert (o["amplitudes"][:, 10:] == -5.0).all()
 
 
@@ -157,7 +172,7 @@ def test_seeded_continuation_finishes_the_oracle_fit(mf, oracle, lib, errors):
     first = oracle.fit_batch(s, pe, P, R, bxs, fullpulsecov=fpc, max_iter_nnls=1000, start=1, max_iter_outer=1)
     full = oracle.fit_batch(s, pe, P, R, bxs, fullpulsecov=fpc, max_iter_nnls=1000, start=1,
                             compute_errors=bool(errors))
-    o = fit(lib, cond, s, pe, 1, 1000, errors, F_SEEDED, seed=first)
+    o = fit(lib, cond, s, pe, 1, 1000, errors, F_SEEDED, chunk=500, seed=first)
     for k in ["amplitudes", "chi2", "active_mask"] + (["errors"] if errors else []):
         assert np.array_equal(o[k], full[k], equal_nan=True), k
     outer = pack_iters(full["iters"]) & 0xFF
