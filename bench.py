@@ -200,7 +200,7 @@ def default_workload(form: str) -> str:
 # profiles/ file given
 NCU_DRAM_BYTES_PER_CHANNEL = {
     ("judge_kernel", "warm"): (180.8, "profiles/judge_kernel_fp32_warm-2m.md"),
-    ("fit_fp64_kernel", "fp64"): (9400.5, "profiles/fit_fp64_kernel_ecal-1m-pu2.md"),
+    ("fit_fp64_kernel", "fp64"): (9016.8, "profiles/fit_fp64_kernel_ecal-1m-pu2.md"),  # both passes
 }
 # useful FLOPs of one warm-start prediction: 12 inputs -> 128 -> 128 -> 20
 # outputs, 2 per multiply-add (the network pads to 16 inputs and 32 outputs)
