@@ -54,6 +54,24 @@ def test_fp64_bitwise_ecal(mf, oracle, engine, cuda, wl, max_iter, start):
     assert np.array_equal(gpu["intime"], gpu["amplitudes"][:, 5])
 
 
+@pytest.mark.parametrize("block", [32, 64, 96, 128])
+def test_fp64_launch_shapes_bitwise(mf, oracle, engine, cuda, block):
+    """The kernel's schedule (one wave of resident blocks, each warp a range
+    of channels, the first outer iterations in lockstep, the rest with lanes
+    taking their warp's next channel) changes with the block size and the
+    batch size; the fits must not: every block size on an ECAL/HCAL batch
+    whose size is no multiple of 32, with the error refits, bit for bit."""
+    mixed_engine(mf, engine)
+    n = 50_021
+    db = DeviceBatch(mf, cuda, n, ctype=True)
+    db.generate(mf, mf.synth_params(seed=17, n=n, pileup_mean=-8.0, hcal_fraction=0.4))
+    opt = mf.default_options(compute_errors=1, block_size=block)
+    engine.fit_device(db.batch, opt)
+    gpu = db.outputs_host()
+    ref = oracle_fit_sets(mf, oracle, engine, db.inputs_host(), compute_errors=True)
+    assert_bitwise(gpu, ref, fields=("amplitudes", "chi2", "active_mask", "status", "errors"))
+
+
 @pytest.mark.parametrize("start", [0, 1])
 def test_fp64_bitwise_mixed_ecal_hcal(mf, oracle, engine, cuda, start):
     mixed_engine(mf, engine)
