@@ -25,8 +25,8 @@ namespace {
 constexpr int kFitBlock = 128;  // the largest block of the kernel (its launch bound)
 // Three blocks of 128 per SM: 168 registers a thread, with which the unrolled
 // 10 x 10 fit keeps its working set in registers and its packed arrays in a
-// 2.4 KB local frame (left free, the compiler chose 128 registers and spilled
-// 2.3 KB); 12 warps per SM keep the FP64 pipe ~90 % busy.
+// ~2.5 KB local frame (left free, the compiler chose 128 registers and
+// spilled 2.3 KB); 12 warps per SM keep the FP64 pipe ~90 % busy.
 constexpr int kFitBlocksPerSm = 3;
 
 // DoFit with the FP64 Minimize: the plain drop-in (R = false), or the
@@ -127,11 +127,15 @@ cudaError_t launch_pass(const FitArgs& a, int t, unsigned grid, int block, int64
   const DevConditions& c = a.cond[t];
   const int flag = t == 0;
   // the per-channel form's continuation with reciprocals (its instrumented
-  // count runs the division form)
-  if (a.seeded == 1 && !C && c.N == 10 && c.K == 10)
-    fit_fp64_kernel<10, 10, false, true, REFILL><<<grid, block, 0, s>>>(a, t, flag, chunk);
-  else if (a.seeded == 1 && !C) fit_fp64_kernel<0, 0, false, true, REFILL><<<grid, block, 0, s>>>(a, t, flag, chunk);
-  else if (c.N == 10 && c.K == 10) fit_fp64_kernel<10, 10, C, false, REFILL><<<grid, block, 0, s>>>(a, t, flag, chunk);
+  // count runs the division form); it always refills
+  if constexpr (REFILL && !C) {
+    if (a.seeded == 1) {
+      if (c.N == 10 && c.K == 10) fit_fp64_kernel<10, 10, false, true, true><<<grid, block, 0, s>>>(a, t, flag, chunk);
+      else fit_fp64_kernel<0, 0, false, true, true><<<grid, block, 0, s>>>(a, t, flag, chunk);
+      return cudaGetLastError();
+    }
+  }
+  if (c.N == 10 && c.K == 10) fit_fp64_kernel<10, 10, C, false, REFILL><<<grid, block, 0, s>>>(a, t, flag, chunk);
   else if (c.N == 8 && c.K == 8) fit_fp64_kernel<8, 8, C, false, REFILL><<<grid, block, 0, s>>>(a, t, flag, chunk);
   else fit_fp64_kernel<0, 0, C, false, REFILL><<<grid, block, 0, s>>>(a, t, flag, chunk);
   return cudaGetLastError();
