@@ -169,7 +169,10 @@ void mf_destroy(mf_context* ctx);
 /* Copies a condition set into the context. For a set without a pulse
  * covariance it also builds, once, the tables of the mixed-precision and
  * warm-start forms (whitening operator and the least-squares operator of every
- * passive set, ~0.6 MB for N = K = 10) and uploads them to the device
+ * passive set, ~0.6 MB for N = K = 10) and uploads them to the device;
+ * with the first such set it allocates the context's workspace for those
+ * forms (one chunk of 16,777,216 channels: ~1 GB, plus 672 MB for the warm
+ * start's predictions when the network is initialised)
  * (synchronous; not a hot-path call). */
 int mf_set_conditions(mf_context* ctx, int ctype, const mf_conditions* cond);
 
@@ -189,7 +192,7 @@ int mf_fit_count_flops(mf_context* ctx, const mf_batch* batch, const mf_options*
  * of a multi-threaded event-processing framework whose caching allocator owns
  * the device memory, where cudaMalloc/cudaFree would synchronise the device
  * under every other event in flight. The search-to-judge hand-off lives in a
- * static device array (about 6.5 MB per device) instead of the context's
+ * static device array (about 6.8 MB per device) instead of the context's
  * workspace; the call allocates nothing. No counterpart in the reference
  * (multifit_cpu allocates nothing on the device).
  *  - n > MF_NOALLOC_MAX_CHANNELS: MF_EINVAL, mf_last_error says why.

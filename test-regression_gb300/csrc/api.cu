@@ -71,6 +71,7 @@ struct Lane {
   float* x = nullptr;
   int* queue = nullptr;
   int* fixq = nullptr;
+  uint16_t* add = nullptr;
   unsigned* qcount = nullptr;
   int* list = nullptr;
   unsigned* sched = nullptr;
@@ -99,6 +100,7 @@ struct mf_context {
   float* ws_x = nullptr;
   int* ws_queue = nullptr;
   int* ws_fixq = nullptr;
+  uint16_t* ws_add = nullptr;
   unsigned* ws_qcount = nullptr;
   // persistent schedule: per-set channel lists and counters; tuned launch shape
   int* ws_list = nullptr;
@@ -248,6 +250,7 @@ int dispatch_mixed(mf_context* c, const FitArgs& a, const mf_options* o, cudaStr
   m.ws_x = c->ws_x;
   m.ws_queue = c->ws_queue;
   m.ws_fixq = c->ws_fixq;
+  m.ws_add = c->ws_add;
   m.ws_qcount = c->ws_qcount;
   m.sms = c->sms;
   m.ws_list = c->ws_list;
@@ -261,6 +264,7 @@ int dispatch_mixed(mf_context* c, const FitArgs& a, const mf_options* o, cudaStr
     m.ws_x = L.x;
     m.ws_queue = L.queue;
     m.ws_fixq = L.fixq;
+    m.ws_add = L.add;
     m.ws_qcount = L.qcount;
     m.ws_list = L.list;
     m.ws_sched = L.sched;
@@ -283,8 +287,11 @@ int dispatch_mixed(mf_context* c, const FitArgs& a, const mf_options* o, cudaStr
   const int64_t cap = warm && MlpState::kChunk < MIXED_CHUNK ? MlpState::kChunk : MIXED_CHUNK;
   // every launch of the fit, chunk by chunk, on stream st
   auto enqueue = [&](cudaStream_t st, LaunchTimer* tm) -> cudaError_t {
-  for (int64_t off = 0; off < a.n; off += cap) {
-    const int64_t cnt = a.n - off < cap ? a.n - off : cap;
+  // chunks of equal size, at most cap each
+  const int64_t nch = (a.n + cap - 1) / cap;
+  const int64_t even = (a.n + nch - 1) / nch;
+  for (int64_t off = 0; off < a.n; off += even) {
+    const int64_t cnt = a.n - off < even ? a.n - off : even;
     MixedArgs mc = m;
     mc.n = cnt;
     mc.samples = a.samples + off * a.sample_stride;
@@ -438,12 +445,13 @@ void destroy_timer(LaunchTimer& t) {
 }
 
 void free_lane(Lane& L) {
-  void* ps[] = {L.mask, L.count, L.x, L.queue, L.fixq, L.qcount, L.list, L.sched, L.warm_mask, L.warm_amp};
+  void* ps[] = {L.mask, L.count, L.x, L.queue, L.fixq, L.add, L.qcount, L.list, L.sched, L.warm_mask, L.warm_amp};
   for (void* p : ps) cudaFree(p);
   L = Lane();
 }
 
-// Lane 1 and the second compute stream of mf_fit_host (200 MB), once.
+// Lane 1 and the second compute stream of mf_fit_host (~1.7 GB with the
+// warm-start predictions), once.
 int grow_lane1(mf_context* c) {
   if (c->lane1.mask) return MF_OK;
   Lane& L = c->lane1;
@@ -452,6 +460,7 @@ int grow_lane1(mf_context* c) {
   if (e == cudaSuccess) e = cudaMalloc(&L.x, sizeof(float) * MIXED_CHUNK * KMAX);
   if (e == cudaSuccess) e = cudaMalloc(&L.queue, sizeof(int) * MIXED_CHUNK);
   if (e == cudaSuccess) e = cudaMalloc(&L.fixq, sizeof(int) * MIXED_CHUNK);
+  if (e == cudaSuccess) e = cudaMalloc(&L.add, sizeof(uint16_t) * MIXED_CHUNK);
   if (e == cudaSuccess) e = cudaMalloc(&L.qcount, 2 * sizeof(unsigned));
   if (e == cudaSuccess) e = cudaMalloc(&L.list, sizeof(int) * MIXED_CHUNK * MF_MAX_CTYPES);
   if (e == cudaSuccess) e = cudaMalloc(&L.sched, sizeof(unsigned) * SCHED_WORDS);
@@ -539,6 +548,7 @@ int upload_tables(mf_context* c, int t) {
     if (e == cudaSuccess) e = cudaMalloc(&c->ws_x, sizeof(float) * MIXED_CHUNK * KMAX);
     if (e == cudaSuccess) e = cudaMalloc(&c->ws_queue, sizeof(int) * MIXED_CHUNK);
     if (e == cudaSuccess) e = cudaMalloc(&c->ws_fixq, sizeof(int) * MIXED_CHUNK);
+    if (e == cudaSuccess) e = cudaMalloc(&c->ws_add, sizeof(uint16_t) * MIXED_CHUNK);
     if (e == cudaSuccess) e = cudaMalloc(&c->ws_qcount, 2 * sizeof(unsigned));  // repair and fix queues
     if (e == cudaSuccess) e = cudaMalloc(&c->ws_list, sizeof(int) * MIXED_CHUNK * MF_MAX_CTYPES);
     if (e == cudaSuccess) e = cudaMalloc(&c->ws_sched, sizeof(unsigned) * SCHED_WORDS);
@@ -680,6 +690,7 @@ void mf_destroy(mf_context* c) {
   cudaFree(c->ws_x);
   cudaFree(c->ws_queue);
   cudaFree(c->ws_fixq);
+  cudaFree(c->ws_add);
   cudaFree(c->ws_qcount);
   cudaFree(c->ws_list);
   cudaFree(c->ws_sched);
@@ -850,7 +861,7 @@ int mf_fit_count_flops(mf_context* c, const mf_batch* b, const mf_options* o, do
 // is on the critical path. Batches too small for the ramp are cut into up to
 // eight equal chunks of at least B/8.
 int host_chunks(int64_t n, int64_t* offs, bool taper) {
-  constexpr int64_t B = MIXED_CHUNK, R = B / 8;
+  constexpr int64_t B = int64_t(1) << 21, R = B / 8;  // the ramp's unit (2M channels)
   constexpr int64_t up[2] = {B / 4, B / 2};
   constexpr int64_t down[2][3] = {{B / 2, B / 4, 0}, {B / 2, B / 4, B / 8}};
   const int64_t* dn = down[taper ? 1 : 0];
@@ -1158,8 +1169,9 @@ constexpr size_t kOffQueue = kOffX + kAlignUp(sizeof(float) * kNoallocMax * KMAX
 constexpr size_t kOffFixq = kOffQueue + kAlignUp(sizeof(int) * kNoallocMax);       // int [max]
 constexpr size_t kOffMask = kOffFixq + kAlignUp(sizeof(int) * kNoallocMax);        // uint16 [max]
 constexpr size_t kOffCount = kOffMask + kAlignUp(sizeof(uint16_t) * kNoallocMax);  // uint16 [max]
-constexpr size_t kOffQcount = kOffCount + kAlignUp(sizeof(uint16_t) * kNoallocMax);  // unsigned [2]
-constexpr size_t kNoallocBytes = kOffQcount + 256;  // 6,816,000 bytes for 131,072 channels
+constexpr size_t kOffAdd = kOffCount + kAlignUp(sizeof(uint16_t) * kNoallocMax);    // uint16 [max]
+constexpr size_t kOffQcount = kOffAdd + kAlignUp(sizeof(uint16_t) * kNoallocMax);   // unsigned [2]
+constexpr size_t kNoallocBytes = kOffQcount + 256;  // 7,078,144 bytes for 131,072 channels
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
 
@@ -1254,6 +1266,7 @@ extern "C" int mf_fit_noalloc(mf_context* c, const mf_batch* b, const mf_options
   m.ws_fixq = reinterpret_cast<int*>(scratch + kOffFixq);
   m.ws_mask = reinterpret_cast<uint16_t*>(scratch + kOffMask);
   m.ws_count = reinterpret_cast<uint16_t*>(scratch + kOffCount);
+  m.ws_add = reinterpret_cast<uint16_t*>(scratch + kOffAdd);
   m.ws_qcount = reinterpret_cast<unsigned*>(scratch + kOffQcount);
   m.sms = c->sms;
   m.judge_df = o->precision == MF_PREC_FP32 ? 1 : 0;

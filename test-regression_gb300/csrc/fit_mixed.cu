@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(128, DF ? 4 : 6) judge_fixed_kernel(const __gr
                                                                           const __grid_constant__ DevMixed T, int set) {
   const unsigned cnt = a.ws_qcount[1];
   for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
-    const int64_t ch = int64_t(unsigned(a.ws_fixq[i]) & 0x1fffffu);
+    const int64_t ch = int64_t(unsigned(a.ws_fixq[i]));
     if constexpr (DF) judge_df_body<N, K>(a, T, ch, a.ws_qcount, nullptr);
     else judge_body<N, K>(a, a.tab[set], ch, a.ws_qcount, nullptr);
   }

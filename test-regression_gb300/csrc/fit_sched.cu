@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(128, DF ? 4 : 6) judge_fixed_persist(const __g
     if (base >= total) break;
     const unsigned i = base + unsigned(lane);
     if (i < total) {
-      const int64_t ch = int64_t(unsigned(a.ws_fixq[i]) & 0x1fffffu);
+      const int64_t ch = int64_t(unsigned(a.ws_fixq[i]));
       if constexpr (DF) judge_df_body<N, K>(a, T, ch, a.ws_sched + SCHED_QUEUE + set, nullptr);
       else judge_body<N, K>(a, a.tab[set], ch, a.ws_sched + SCHED_QUEUE + set, nullptr);
     }

@@ -171,7 +171,8 @@ struct MixedArgs {
   uint16_t* ws_count;
   float* ws_x;
   int* ws_queue;           // channels the judge queues for the FP64 repair
-  int* ws_fixq;            // channels the first judge pass queues for the FP32 fix (ch | add << 21)
+  int* ws_fixq;            // channels queued for the FP32 fix (their index in the chunk)
+  uint16_t* ws_add;        // per channel: the columns the fix adds (written with its queue entry)
   unsigned* ws_qcount;     // [0] repair queue, [1] fix queue sizes (zeroed by the search launch)
   int sms;
   // persistent schedule (fit_sched.cu): per-set channel lists [MF_MAX_CTYPES][MIXED_CHUNK]
@@ -183,8 +184,13 @@ struct MixedArgs {
   int judge_df;            // MF_PREC_FP32: the judge in double-float FP32 arithmetic instead of FP64
 };
 constexpr int SCHED_WORDS = 32;
-// Channels per chunk of a mixed fit (the size of the hand-off workspace).
-constexpr int64_t MIXED_CHUNK = int64_t(1) << 21;
+// Channels per chunk of a mixed fit (the size of the hand-off workspace,
+// 62 B per channel: 1 GB, and 672 MB of warm-start predictions). A chunk's
+// queue kernels (fix, second judge, repair) hold a few per cent of its
+// channels and are latency-bound: fewer, larger chunks give them more warps
+// to hide their latency behind (10M warm channels: 5.24 ms per fit in chunks
+// of 2M, 4.96 ms in chunks of 4M).
+constexpr int64_t MIXED_CHUNK = int64_t(1) << 24;
 cudaError_t launch_fit_mixed(const MixedArgs& a, int block, cudaStream_t s, LaunchTimer* tm = nullptr);
 // Persistent work-stealing schedule: per-set channel lists, then per set the
 // FP32 search (block threads, `lanes` lanes per channel), judge and repair.

@@ -523,7 +523,7 @@ __device__ __forceinline__ void judge_repair(const MixedArgs& a, const DevMixed&
 // The KKT screen of channel ch (one lane, FP32, branch-free), run on cold
 // starts before the judge: refines the search's amplitudes on its set and,
 // when columns provably violate the KKT condition, queues the channel for
-// fix_body (ws_fixq, entry ch | add mask << 21).
+// fix_body (ws_fixq, the columns to add in ws_add).
 template <int N, int K>
 __device__ __forceinline__ void screen_body(const MixedArgs& a, const DevMixed& T, int64_t ch, unsigned* fix_count) {
   const unsigned m = a.ws_mask[ch];
@@ -540,12 +540,15 @@ __device__ __forceinline__ void screen_body(const MixedArgs& a, const DevMixed& 
                                            [&](unsigned mm, const float* rhs, float* out) { solve32<N, K>(T, mm, rhs, out); });
 #pragma unroll
   for (int k = 0; k < K; ++k) wx[k] = x32[k];
-  if (add) enqueue(fix_count, a.ws_fixq, int(unsigned(ch) | (add << 21)));
+  if (add) {
+    a.ws_add[ch] = uint16_t(add);
+    enqueue(fix_count, a.ws_fixq, int(ch));
+  }
 }
 
-// A channel queued for fixing by the screen or the judge (entry = ch | add <<
-// 21, add = the columns that provably violate the KKT condition; ch <
-// MIXED_CHUNK = 2^21):
+// A channel queued for fixing by the screen or the judge (entry = the
+// channel's index in the chunk; ws_add[ch] = the columns that provably
+// violate the KKT condition):
 // the FNNLS step with the added columns in FP32 (the inner loop drops those
 // that come out non-positive), then, with rounds = 2, the double-float screen
 // of the new set and, if it finds more, one more step. Writes the hand-off for
@@ -555,8 +558,8 @@ __device__ __forceinline__ void screen_body(const MixedArgs& a, const DevMixed& 
 // per 10M with one round; cold with one round 9.5 -> 13.0 ms, repairs x9).
 template <int N, int K>
 __device__ __forceinline__ void fix_body(const MixedArgs& a, const DevMixed& T, unsigned entry, int rounds) {
-  const int64_t ch = int64_t(entry & 0x1fffffu);
-  unsigned add = entry >> 21;
+  const int64_t ch = int64_t(entry);
+  unsigned add = a.ws_add[ch];
   unsigned m = a.ws_mask[ch];
   const unsigned cnt = a.ws_count[ch];
   int adds = int(cnt & 255u), solves = int(cnt >> 8);
@@ -627,7 +630,7 @@ __device__ __forceinline__ bool kkt_screen32(const DevMixed& T, const double* r,
 // The FP64 judge of channel ch (one lane): writes the outputs; or, when
 // columns provably violate the KKT condition and the amplitudes are positive
 // and fix_count is given, queues the channel for the FP32 fix (ws_fixq,
-// entry ch | add << 21); otherwise queues it for the FP64 repair (ws_queue).
+// the columns to add in ws_add); otherwise queues it for the FP64 repair (ws_queue).
 // The FP64 solve on the search's passive set and the residual run column by
 // column over the set only (each lane its own trip count; a warp runs as many
 // iterations as its largest set): x_k = G_S^+_k y from the FP64 table, then
@@ -686,8 +689,12 @@ __device__ __forceinline__ void judge_body(const MixedArgs& a, const DevMixed& T
   const bool pos_ok = ok;
   if (ok) ok = kkt_screen32<N, K>(T, r, m, float(a.eps * sig * sig), add);
   if (!ok) {  // compaction into the fix or the repair queue
-    if (fix_count && pos_ok && add) enqueue(fix_count, a.ws_fixq, int(unsigned(ch) | (add << 21)));
-    else enqueue(qcount, a.ws_queue, int(ch));
+    if (fix_count && pos_ok && add) {
+      a.ws_add[ch] = uint16_t(add);
+      enqueue(fix_count, a.ws_fixq, int(ch));
+    } else {
+      enqueue(qcount, a.ws_queue, int(ch));
+    }
     return;
   }
   double chi2 = 0.;
@@ -884,8 +891,12 @@ __device__ __forceinline__ void judge_df_body(const MixedArgs& a, const DevMixed
     }
   }
   if (!ok) {  // compaction into the fix or the repair queue
-    if (fix_count && pos_ok && add) enqueue(fix_count, a.ws_fixq, int(unsigned(ch) | (add << 21)));
-    else enqueue(qcount, a.ws_queue, int(ch));
+    if (fix_count && pos_ok && add) {
+      a.ws_add[ch] = uint16_t(add);
+      enqueue(fix_count, a.ws_fixq, int(ch));
+    } else {
+      enqueue(qcount, a.ws_queue, int(ch));
+    }
     return;
   }
   // chi2 = ||r||^2 / pederr^2, the sum in double-float

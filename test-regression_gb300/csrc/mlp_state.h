@@ -32,7 +32,7 @@ struct MlpState {
   __nv_bfloat16* W3t = nullptr;
   // predictions of one chunk of a warm fit (allocated with the network, so a
   // warm fit allocates nothing)
-  static constexpr int64_t kChunk = int64_t(1) << 21;
+  static constexpr int64_t kChunk = MIXED_CHUNK;
   uint16_t* warm_mask = nullptr;
   float* warm_amp = nullptr;
   unsigned* infer_err = nullptr;  // inference error word (MLP_ERR_* bits)
