@@ -288,8 +288,8 @@ int dispatch_mixed(mf_context* c, const FitArgs& a, const mf_options* o, cudaStr
   // every launch of the fit, chunk by chunk, on stream st
   auto enqueue = [&](cudaStream_t st, LaunchTimer* tm) -> cudaError_t {
   // chunks of equal size, at most cap each
-  const int64_t nch = (a.n + cap - 1) / cap;
-  const int64_t even = (a.n + nch - 1) / nch;
+  const int64_t nch = a.n > cap ? (a.n + cap - 1) / cap : 1;
+  const int64_t even = a.n > 0 ? (a.n + nch - 1) / nch : 1;
   for (int64_t off = 0; off < a.n; off += even) {
     const int64_t cnt = a.n - off < even ? a.n - off : even;
     MixedArgs mc = m;
