@@ -37,10 +37,10 @@
   ``+=``), as the oracle does; ``-fsigned-char`` because the fit keeps its
   BX offsets in plain char. Built only where the reference tree exists.
 
-The reference tree is read from MULTIFIT_REFERENCE_ROOT, by default the
-location this recipe was written against; where it is absent, every _ref
-library is skipped and the tests fall back on the committed outputs in
-tests/golden/.
+The reference tree is read from MULTIFIT_REFERENCE_ROOT, by default a
+checkout named ``reference`` beside the repository's root; where it is
+absent, every _ref library is skipped and the tests fall back on the
+committed outputs in tests/golden/.
 """
 from __future__ import annotations
 
@@ -52,7 +52,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-REFERENCE_ROOT = os.environ.get("MULTIFIT_REFERENCE_ROOT", "/root/reference")
+REFERENCE_ROOT = os.environ.get("MULTIFIT_REFERENCE_ROOT",
+                                os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 
 ORACLE_LIB = os.path.join(BUILD, "liboracle.so")
 ORACLE_SEP_LIB = os.path.join(BUILD, "liboracle_sep.so")
