@@ -86,17 +86,41 @@ void cold_pipeline(const MixedArgs& a, const DevMixed& T, unsigned* qc) {
   for (unsigned i = 0; i < qc[0]; ++i) judge_repair<N, K>(a, T, int64_t(a.ws_queue[i]));
 }
 
+// the warm start's order (launch_set): search from the predicted sets, judge
+// (queueing channels with provably missing columns for the fix), fix (one
+// round), the judge again on the fixed channels, repair
+template <int N, int K>
+void warm_pipeline(const MixedArgs& a, const DevMixed& T, unsigned* qc) {
+  qc[0] = qc[1] = 0u;
+  for (int64_t ch = 0; ch < a.n; ++ch) search_body<N, K, true>(a, T, ch);
+  for (int64_t ch = 0; ch < a.n; ++ch) {
+    if (a.judge_df) judge_df_body<N, K>(a, T, ch, qc, qc + 1);
+    else judge_body<N, K>(a, T, ch, qc, qc + 1);
+  }
+  for (unsigned i = 0; i < qc[1]; ++i) fix_body<N, K>(a, T, unsigned(a.ws_fixq[i]), 1);
+  for (unsigned i = 0; i < qc[1]; ++i) {
+    const int64_t ch = int64_t(unsigned(a.ws_fixq[i]));
+    if (a.judge_df) judge_df_body<N, K>(a, T, ch, qc, nullptr);
+    else judge_body<N, K>(a, T, ch, qc, nullptr);
+  }
+  for (unsigned i = 0; i < qc[0]; ++i) judge_repair<N, K>(a, T, int64_t(a.ws_queue[i]));
+}
+
 }  // namespace
 
 // Fits n channels of one condition set (mf_conditions layout, no pulse
-// covariance, N = K = 10 or 8) with the cold-start pipeline; judge_df: the
-// judge in double-float FP32 arithmetic (MF_PREC_FP32) instead of FP64.
-// queues[2] returns the fix and repair queue lengths.
+// covariance, N = K = 10 or 8) with the cold-start pipeline, or, given
+// predicted passive sets warm_mask[n] and amplitudes warm_amp[n][10] (N = K =
+// 10), with the warm start's; judge_df: the judge in double-float FP32
+// arithmetic (MF_PREC_FP32) instead of FP64. queues[2] returns the fix and
+// repair queue lengths.
 extern "C" int mixed_host(const mf_conditions* cond, const double* samples, const double* pederr, int64_t n,
                           int judge_df, int max_iter_nnls, double* amplitudes, double* chi2, uint16_t* active_mask,
-                          uint8_t* status, int32_t* iters, unsigned* queues) {
+                          uint8_t* status, int32_t* iters, unsigned* queues, const uint16_t* warm_mask,
+                          const float* warm_amp) {
   const int N = cond->nsamples, K = cond->npulses;
   if (!((N == 10 && K == 10) || (N == 8 && K == 8)) || cond->has_fullpulsecov) return 1;
+  if (warm_mask && N != 10) return 1;
   DevConditions* d = static_cast<DevConditions*>(std::calloc(1, sizeof(DevConditions)));
   if (!d) return 2;
   d->N = N;
@@ -188,8 +212,17 @@ extern "C" int mixed_host(const mf_conditions* cond, const double* samples, cons
   a->sms = 1;
   a->list_identity = 1;
   a->judge_df = judge_df ? 1 : 0;
-  if (N == 10) cold_pipeline<10, 10>(*a, a->tab[0], qc);
-  else cold_pipeline<8, 8>(*a, a->tab[0], qc);
+  if (warm_mask) {
+    a->warm_mask = warm_mask;
+    a->warm_amp = warm_amp;
+    a->warm_stride = 10;
+    a->warm_set = 0;
+    warm_pipeline<10, 10>(*a, a->tab[0], qc);
+  } else if (N == 10) {
+    cold_pipeline<10, 10>(*a, a->tab[0], qc);
+  } else {
+    cold_pipeline<8, 8>(*a, a->tab[0], qc);
+  }
   queues[0] = qc[1];
   queues[1] = qc[0];
   std::free(a);

@@ -2,11 +2,13 @@
 their passive-set tables (csrc/tables.cu), compiled for the host
 (tests/cpp/mixed_host.cpp) and run on the CPU through the grid schedule's
 cold-start pipeline -- FP32 search, double-float KKT screen, FP32 fix, the FP64
-(mixed) or double-float (FP32) judge, FP64 repair, queues included -- against
-the oracle's fits to KKT convergence: the golden fixtures, seeded ECAL and HCAL
-channels of the benchmark generators, and noise-free channels whose fits are
-exact (where the double-float judge's round-off bounds must send undecidable
-channels to the FP64 repair rather than return a wrong active set).
+(mixed) or double-float (FP32) judge, FP64 repair, queues included -- and its
+warm-start pipeline from given predictions, against the oracle's fits to KKT
+convergence: the golden fixtures, seeded ECAL and HCAL channels of the
+benchmark generators, imperfect predictions, and noise-free channels whose fits
+are exact (where the double-float judge's round-off bounds must send
+undecidable channels to the FP64 repair rather than return a wrong active
+set).
 
 Tolerance: the forms' own bar, <= 1e-4 normwise relative amplitude error
 against the FP64 KKT point, identical active sets (on noise-free channels a
@@ -39,11 +41,13 @@ def lib(tmp_path_factory):
                     "-I", os.path.join(ROOT, "include"), "-I", CSRC, os.path.join(ROOT, "tests", "cpp", "mixed_host.cpp"),
                     "-x", "c++", os.path.join(CSRC, "tables.cu"), "-o", out], check=True)
     L = C.CDLL(out)
-    L.mixed_host.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_int] + [C.c_void_p] * 6
+    L.mixed_host.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_int] + [C.c_void_p] * 8
     return L
 
 
-def fit(lib, cond, samples, pederr, judge_df, max_iter=1000):
+def fit(lib, cond, samples, pederr, judge_df, max_iter=1000, warm_mask=None, warm_amp=None):
+    """warm_mask / warm_amp: predicted passive sets and amplitudes (the warm
+    start's pipeline), or None (cold start)."""
     n = samples.shape[0]
     N, K = cond.nsamples, cond.npulses
     s = np.ascontiguousarray(samples[:, :N], dtype=np.float64)
@@ -51,9 +55,11 @@ def fit(lib, cond, samples, pederr, judge_df, max_iter=1000):
     o = {"amplitudes": np.zeros((n, K)), "chi2": np.zeros(n), "active_mask": np.zeros(n, np.uint16),
          "status": np.zeros(n, np.uint8), "iters": np.zeros(n, np.int32)}
     q = np.zeros(2, np.uint32)
+    wm = None if warm_mask is None else np.ascontiguousarray(warm_mask, dtype=np.uint16)
+    wa = None if warm_amp is None else np.ascontiguousarray(warm_amp, dtype=np.float32)
     rc = lib.mixed_host(C.byref(cond), s.ctypes.data, pe.ctypes.data, n, judge_df, max_iter,
                         *[o[k].ctypes.data for k in ("amplitudes", "chi2", "active_mask", "status", "iters")],
-                        q.ctypes.data)
+                        q.ctypes.data, None if wm is None else wm.ctypes.data, None if wa is None else wa.ctypes.data)
     assert rc == 0
     o["fix_queue"], o["repair_queue"] = int(q[0]), int(q[1])
     return o
@@ -151,3 +157,33 @@ def test_exact_fits_keep_their_active_sets(mf, oracle, lib, prec):
     extra = o["amplitudes"] * ((x == 0) & (o["amplitudes"] > 0))
     assert (extra.max(axis=1) <= 1e-9 * np.abs(x).max(axis=1)).all()  # others at round-off at most
     assert (rel_err(o["amplitudes"], x) <= 1e-6).all()
+
+
+@pytest.mark.parametrize("prec", list(PRECISIONS))
+def test_warm_pipeline_from_imperfect_predictions(mf, oracle, lib, prec):
+    """The warm start's pipeline (search from a predicted set, judge queueing
+    channels with provably missing columns for the fix, fix, second judge,
+    repair), fed predictions that are the KKT sets with columns dropped and
+    spurious ones added and amplitudes off by up to a factor of two, as a
+    network's might be: every channel still ends within the bar of the KKT
+    fit with the same active set, and the fix and second judge run."""
+    P, R, bxs, _ = oracle.synth_conditions(0)
+    inp = oracle.synth_generate("warm-eval-10m", 0, 6000)
+    s, pe = inp["samples"], inp["pederr"]
+    ref = oracle.fit_batch(s, pe, P, R, bxs, max_iter_nnls=1000, start=1)
+    rng = np.random.default_rng(31)
+    mask = ref["active_mask"].astype(np.uint32)
+    drop = rng.random((len(pe), 10)) < 0.15
+    add = rng.random((len(pe), 10)) < 0.05
+    bits = 1 << np.arange(10)
+    pred = (mask & ~(drop * bits).sum(axis=1)) | (add * bits).sum(axis=1)
+    amp = (np.abs(ref["amplitudes"]) * rng.uniform(0.5, 2.0, size=(len(pe), 10)) + 0.01).astype(np.float32)
+    o = fit(lib, mf.make_conditions(P, R, bxs), s, pe, PRECISIONS[prec], warm_mask=pred, warm_amp=amp)
+    ok = ref["status"] == 0
+    check_against_kkt(o, ref["amplitudes"], ref["active_mask"], ok)
+    assert o["fix_queue"] > 0
+    # a perfect prediction leaves nearly nothing to fix
+    o2 = fit(lib, mf.make_conditions(P, R, bxs), s, pe, PRECISIONS[prec], warm_mask=ref["active_mask"],
+             warm_amp=np.abs(ref["amplitudes"]).astype(np.float32))
+    check_against_kkt(o2, ref["amplitudes"], ref["active_mask"], ok)
+    assert o2["fix_queue"] < o["fix_queue"] / 4
