@@ -183,6 +183,11 @@ extern "C" int mixed_host(const mf_conditions* cond, const double* samples, cons
   std::vector<int> ws_queue(n), ws_fixq(n);
   unsigned qc[2] = {0u, 0u};
   MixedArgs* a = static_cast<MixedArgs*>(std::calloc(1, sizeof(MixedArgs)));
+  if (!a) {
+    delete h;
+    std::free(d);
+    return 2;
+  }
   a->tab[0] = T;
   a->n_ctypes = 1;
   a->skip_set = -1;
