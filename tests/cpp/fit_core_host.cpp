@@ -136,9 +136,11 @@ void dispatch(const FitArgs& a, bool generic, int64_t chunk) {
 // instantiation, 8 seeded (amplitudes, chi2 and status hold the first outer
 // iteration on entry). ctype (or null): each channel's condition set; those
 // of set 1 belong to another launch, those of set 2 or above are flagged.
+// max_iter_outer: Minimize's iteration cap (50 in the reference).
 extern "C" int fit_core_host(const mf_conditions* cond, const double* samples, int sample_stride,
                              const double* pederr, const uint8_t* ctype, int64_t n, int nnls_start, int max_iter_nnls,
-                             int compute_errors, int flags, int64_t chunk, double* amplitudes, int amp_stride, double* chi2,
+                             int compute_errors, int flags, int64_t chunk, int max_iter_outer, double* amplitudes,
+                             int amp_stride, double* chi2,
                              double* intime, double* errors, uint16_t* active_mask, uint8_t* status, int32_t* iters,
                              double* flops) {
   const int N = cond->nsamples, K = cond->npulses;
@@ -161,7 +163,7 @@ extern "C" int fit_core_host(const mf_conditions* cond, const double* samples, i
   a->n_ctypes = ctype ? 2 : 1;
   a->ctype = ctype;
   a->opt.max_iter_nnls = max_iter_nnls;
-  a->opt.max_iter_outer = 50;
+  a->opt.max_iter_outer = max_iter_outer;
   a->opt.dchi2_tol = 1e-3;
   a->opt.nnls_eps = 1e-11;
   a->opt.nnls_start = nnls_start;

@@ -39,12 +39,12 @@ def lib(tmp_path_factory):
                     os.path.join(ROOT, "tests", "cpp", "fit_core_host.cpp"), "-o", out], check=True)
     L = C.CDLL(out)
     L.fit_core_host.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int64] + \
-        [C.c_int] * 4 + [C.c_int64, C.c_void_p, C.c_int] + [C.c_void_p] * 7
+        [C.c_int] * 4 + [C.c_int64, C.c_int, C.c_void_p, C.c_int] + [C.c_void_p] * 7
     return L
 
 
 def fit(lib, cond, samples, pederr, start, max_iter, errors, flags=0, chunk=96, ctype=None, sample_stride=None,
-        amp_stride=None, seed=None, fill=0.0):
+        amp_stride=None, seed=None, fill=0.0, max_iter_outer=50):
     """chunk: channels per warp; ctype: per-channel condition set (1: another
     launch's, 2: out of range), or None."""
     n = samples.shape[0]
@@ -63,7 +63,7 @@ def fit(lib, cond, samples, pederr, start, max_iter, errors, flags=0, chunk=96, 
         o["status"][:] = seed["status"]
     ct = None if ctype is None else np.ascontiguousarray(ctype, dtype=np.uint8)
     rc = lib.fit_core_host(C.byref(cond), s.ctypes.data, ss, pe.ctypes.data, None if ct is None else ct.ctypes.data,
-                           n, start, max_iter, errors, flags, chunk, o["amplitudes"].ctypes.data, ast,
+                           n, start, max_iter, errors, flags, chunk, max_iter_outer, o["amplitudes"].ctypes.data, ast,
                            *[o[k].ctypes.data for k in ("chi2", "intime", "errors", "active_mask", "status", "iters",
                                                         "flops")])
     assert rc == 0
@@ -179,3 +179,24 @@ def test_seeded_continuation_finishes_the_oracle_fit(mf, oracle, lib, errors):
     assert np.array_equal(o["iters"] & 0xFF, outer)
     # the pulse covariance makes the loop iterate: most channels go on past the first iteration
     assert (outer > 2).mean() > 0.5
+
+
+@pytest.mark.parametrize("max_outer", [0, 1, 2, 3])
+def test_outer_iteration_caps_bit_for_bit(mf, oracle, lib, max_outer):
+    """Minimize's iteration cap decides the kernel's passes (one lockstep pass
+    for a cap of one or less, else the lockstep first iteration and the
+    refilled rest): at every cap, with and without the error refits and a
+    pulse covariance, the oracle's outputs (status bits included) bit for bit."""
+    fpc = dict(np.load(os.path.join(GOLDEN, "fits_ecal_fpc.npz")))["fullpulsecov"] * 3.0
+    P, R, bxs, _ = oracle.synth_conditions(0)
+    inp = oracle.synth_generate("ecal-1m-pu2", 0, 1500)
+    s, pe = inp["samples"], inp["pederr"]
+    for F in (None, fpc):
+        cond = mf.make_conditions(P, R, bxs, fullpulsecov=F)
+        for errors in (0, 1):
+            ref = oracle.fit_batch(s, pe, P, R, bxs, fullpulsecov=F, max_iter_nnls=10, start=0,
+                                   compute_errors=bool(errors), max_iter_outer=max_outer)
+            o = fit(lib, cond, s, pe, 0, 10, errors, chunk=300, max_iter_outer=max_outer)
+            for k in ["amplitudes", "chi2", "active_mask", "status"] + (["errors"] if errors else []):
+                assert np.array_equal(o[k], ref[k], equal_nan=True), (F is not None, errors, k)
+            assert np.array_equal(o["iters"], pack_iters(ref["iters"]))
