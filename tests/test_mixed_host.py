@@ -187,3 +187,53 @@ def test_warm_pipeline_from_imperfect_predictions(mf, oracle, lib, prec):
              warm_amp=np.abs(ref["amplitudes"]).astype(np.float32))
     check_against_kkt(o2, ref["amplitudes"], ref["active_mask"], ok)
     assert o2["fix_queue"] < o["fix_queue"] / 4
+
+
+@pytest.fixture(scope="module")
+def fit_core_lib(tmp_path_factory):
+    """The FP64 drop-in's routines compiled for the host (tests/cpp/fit_core_host.cpp)."""
+    if not shutil.which("g++") or not os.path.exists(os.path.join(CUDA_INCLUDE, "cuda_runtime.h")):
+        pytest.skip("needs g++ and the CUDA headers")
+    out = str(tmp_path_factory.mktemp("fitcore_mixed") / "libfit_core_host.so")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-w", "-I", CUDA_INCLUDE,
+                    "-I", os.path.join(ROOT, "include"), "-I", CSRC,
+                    os.path.join(ROOT, "tests", "cpp", "fit_core_host.cpp"), "-o", out], check=True)
+    L = C.CDLL(out)
+    L.fit_core_host.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int64] + \
+        [C.c_int] * 4 + [C.c_int64, C.c_int, C.c_void_p, C.c_int] + [C.c_void_p] * 7
+    return L
+
+
+@pytest.mark.parametrize("errors", [0, 1])
+@pytest.mark.parametrize("prec", list(PRECISIONS))
+def test_per_channel_form_pulse_covariance(mf, oracle, lib, fit_core_lib, prec, errors):
+    """The per-channel form on the CPU, as the engine composes it: the outer
+    loop's first iteration through the tables (its covariance is pederr^2
+    samplecor whatever the pulse covariance, the tables' problem), then the
+    FP64 continuation with the pulse covariance and the reciprocal factor
+    diagonal, seeded with that iteration's amplitudes, chi2 and status;
+    against the oracle's FP64 fit to KKT convergence with the same pulse
+    covariance: amplitudes and MINOS errors within 1e-4, identical active sets
+    and outer-iteration counts."""
+    import test_fit_core_host as fch
+
+    F = np.zeros((19, 19))
+    idx = np.arange(7, 19)
+    F[np.ix_(idx, idx)] = 3e-4 * np.exp(-np.abs(np.subtract.outer(idx, idx)) / 3.0)
+    P, R, bxs, _ = oracle.synth_conditions(0)
+    inp = oracle.synth_generate("ecal-1m-pu2", 0, 3000)
+    s, pe = inp["samples"], inp["pederr"]
+    first = fit(lib, mf.make_conditions(P, R, bxs), s, pe, PRECISIONS[prec])
+    o = fch.fit(fit_core_lib, mf.make_conditions(P, R, bxs, fullpulsecov=F), s, pe, 1, 1000, errors,
+                fch.F_SEEDED | fch.F_RECIP, chunk=300, seed=first)
+    ref = oracle.fit_batch(s, pe, P, R, bxs, fullpulsecov=F, max_iter_nnls=1000, start=1, compute_errors=bool(errors))
+    ok = ref["status"] == 0
+    assert ok.mean() > 0.99
+    check_against_kkt(o, ref["amplitudes"], ref["active_mask"], ok)
+    assert np.array_equal(o["iters"][ok] & 0xFF, np.minimum(ref["iters"][ok, 0], 255))
+    assert (np.abs(o["chi2"] - ref["chi2"])[ok] <= 1e-6 * np.maximum(ref["chi2"][ok], 1.0)).all()
+    if errors:
+        fin = ok & np.isfinite(ref["errors"])
+        assert (np.abs(o["errors"] - ref["errors"])[fin] <= 1e-4 * np.abs(ref["errors"][fin])).all()
+    # the pulse covariance makes the outer loop iterate past the tables' first iteration
+    assert (ref["iters"][:, 0] > 2).mean() > 0.5
